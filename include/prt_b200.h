@@ -1,0 +1,120 @@
+/*
+ * prt_b200.h - C ABI of the GB300 (sm_103a) ray-query backend for portableRT.
+ *
+ * The C++ backend class (include/portableRT/intersect_b200.hpp) and any FFI caller
+ * reach the CUDA kernels only through these functions: plain pointers and sizes, no
+ * CUDA or torch types.  Every function returns 0 on success and a PRT_ERR_* code
+ * otherwise; the message is kept per context (prt_b200_last_error).  Nothing aborts.
+ *
+ * Ownership: input arrays are borrowed for the duration of a call; the scene built by
+ * prt_b200_set_tris lives in device memory owned by the context until the next
+ * set_tris or prt_b200_destroy; output buffers belong to the caller.
+ *
+ * Threading: calls on one context are serialised by a mutex inside the context.
+ * Different contexts are independent.
+ */
+#ifndef PRT_B200_H
+#define PRT_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct prt_b200_ctx prt_b200_ctx;
+
+enum {
+	PRT_OK = 0,
+	PRT_ERR_ARG = 1,          /* bad argument (null pointer, bad layout, size) */
+	PRT_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+	PRT_ERR_NO_DEVICE = 3,    /* no sm_103 device */
+	PRT_ERR_NO_SCENE = 4,     /* nearest_hits before set_tris */
+	PRT_ERR_DEVICE = 5,       /* a kernel reported an error (see last_error) */
+	PRT_ERR_OOM = 6,          /* device allocation failed */
+	PRT_ERR_LIMIT = 7         /* a documented size limit was exceeded */
+};
+
+/* Field bits of the hit record, one per portableRT filter tag. */
+#define PRT_FIELD_UV 1u
+#define PRT_FIELD_T 2u
+#define PRT_FIELD_PRIMITIVE_ID 4u
+#define PRT_FIELD_P 8u
+#define PRT_FIELD_VALID 16u
+
+/* Byte offsets inside one HitReg<Tags...> record, in this order:
+ * u, v, t, primitive_id, valid, px, py, pz.  Offsets of absent fields are ignored. */
+#define PRT_OFF_U 0
+#define PRT_OFF_V 1
+#define PRT_OFF_T 2
+#define PRT_OFF_PID 3
+#define PRT_OFF_VALID 4
+#define PRT_OFF_PX 5
+#define PRT_OFF_PY 6
+#define PRT_OFF_PZ 7
+
+/* Acceleration-structure node formats (option "node_format"). */
+#define PRT_NODES_FP32 0       /* 8-wide nodes, FP32 child boxes (224 B) */
+#define PRT_NODES_COMPRESSED 1 /* 8-wide nodes, 8-bit child boxes rounded outward (80 B) */
+
+/* Replaces CPUBackend::is_available (portableRT src/intersect_cpu.cpp:9) for this
+ * backend: 1 when a device of compute capability 10.3 is visible.  Cheap, no context. */
+int prt_b200_available(void);
+
+/* Replaces Backend::init (include/portableRT/backend.hpp:21): creates the per-backend
+ * state (stream, error word) on `device`. */
+int prt_b200_create(int device, prt_b200_ctx **out);
+
+/* Replaces Backend::shutdown (backend.hpp:22): frees every device and host resource. */
+void prt_b200_destroy(prt_b200_ctx *ctx);
+
+/* Message of the last failing call on ctx ("" if none).  With ctx == NULL: the last
+ * failure of prt_b200_create in this thread. */
+const char *prt_b200_last_error(const prt_b200_ctx *ctx);
+
+/* Replaces Backend::device_name (backend.hpp:23). */
+int prt_b200_device_name(prt_b200_ctx *ctx, char *buf, size_t len);
+
+/* Replaces Backend::set_tris -> BVH2::build (backend.hpp:19, src/intersect_cpu.cpp:12,
+ * include/portableRT/bvh.hpp:158-193).  tris9: n x 9 floats (v0, v1, v2), host memory.
+ * Builds an 8-wide LBVH on the device; primitive_id of triangle i is i. */
+int prt_b200_set_tris(prt_b200_ctx *ctx, const float *tris9, uint64_t n);
+
+/* As prt_b200_set_tris with tris9 already in device memory (read on the context's
+ * stream; the build is complete when the call returns). */
+int prt_b200_set_tris_dev(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n);
+
+/* Replaces CPUBackend::nearest_hits<Tags...> (include/portableRT/intersect_cpu.hpp:20-43)
+ * and BVH2::nearest_tri (bvh.hpp:224-265).  rays6: n x 6 floats (origin, direction) in
+ * host memory; out_host: n records of rec_size bytes laid out by `offs` (see
+ * PRT_OFF_*), written only for the fields in field_mask.  Synchronous. */
+int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n,
+                          uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                          void *out_host);
+
+/* Device-resident variant: d_rays6 and d_out are device pointers; the work is queued
+ * on `stream` (a cudaStream_t, NULL = the context's stream) and the call returns
+ * without waiting.  prt_b200_sync waits and reports kernel-side errors. */
+int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n,
+                              uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                              void *d_out, void *stream);
+
+/* Waits for the context's queued work and reports errors the kernels flagged. */
+int prt_b200_sync(prt_b200_ctx *ctx);
+
+/* Tuning and statistics.  Options (take effect at the next set_tris unless noted):
+ *   "leaf_size"    1..8  triangles per leaf of the 8-wide tree (default 4)
+ *   "node_format"  PRT_NODES_FP32 or PRT_NODES_COMPRESSED (default FP32; applies to the
+ *                  next nearest_hits when both formats have been built)
+ *   "block"        threads per block of the traversal kernel (default 128)
+ *   "count_visits" 1 = the traversal also accumulates node / triangle visit counts
+ * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "node_bytes", "tri_bytes",
+ *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
+int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
+int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PRT_B200_H */

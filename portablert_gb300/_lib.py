@@ -1,0 +1,82 @@
+"""ctypes binding of libprt_b200.so (the C ABI declared in include/prt_b200.h).
+
+The library is the only compute path: if it is missing this module raises instead of
+falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+# Every symbol include/prt_b200.h declares.
+EXPORTS = (
+    "prt_b200_available", "prt_b200_create", "prt_b200_destroy", "prt_b200_last_error",
+    "prt_b200_device_name", "prt_b200_set_tris", "prt_b200_set_tris_dev",
+    "prt_b200_nearest_hits", "prt_b200_nearest_hits_dev", "prt_b200_sync",
+    "prt_b200_set_option", "prt_b200_get_stat",
+)
+
+PRT_OK = 0
+ERRORS = {1: "PRT_ERR_ARG", 2: "PRT_ERR_CUDA", 3: "PRT_ERR_NO_DEVICE", 4: "PRT_ERR_NO_SCENE",
+          5: "PRT_ERR_DEVICE", 6: "PRT_ERR_OOM", 7: "PRT_ERR_LIMIT"}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Loads the library and declares the signatures (no CUDA call is made)."""
+    global _lib
+    if _lib is not None and path == LIB_PATH:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA extension first "
+            "(python -c 'import __graft_entry__ as g; g.build()')")
+    L = ctypes.CDLL(path)
+    vp, c_int, c_u64, c_u32 = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_uint32
+    L.prt_b200_available.restype = c_int
+    L.prt_b200_available.argtypes = []
+    L.prt_b200_create.restype = c_int
+    L.prt_b200_create.argtypes = [c_int, ctypes.POINTER(vp)]
+    L.prt_b200_destroy.restype = None
+    L.prt_b200_destroy.argtypes = [vp]
+    L.prt_b200_last_error.restype = ctypes.c_char_p
+    L.prt_b200_last_error.argtypes = [vp]
+    L.prt_b200_device_name.restype = c_int
+    L.prt_b200_device_name.argtypes = [vp, ctypes.c_char_p, ctypes.c_size_t]
+    L.prt_b200_set_tris.restype = c_int
+    L.prt_b200_set_tris.argtypes = [vp, vp, c_u64]
+    L.prt_b200_set_tris_dev.restype = c_int
+    L.prt_b200_set_tris_dev.argtypes = [vp, vp, c_u64]
+    L.prt_b200_nearest_hits.restype = c_int
+    L.prt_b200_nearest_hits.argtypes = [vp, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp]
+    L.prt_b200_nearest_hits_dev.restype = c_int
+    L.prt_b200_nearest_hits_dev.argtypes = [vp, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp, vp]
+    L.prt_b200_sync.restype = c_int
+    L.prt_b200_sync.argtypes = [vp]
+    L.prt_b200_set_option.restype = c_int
+    L.prt_b200_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
+    L.prt_b200_get_stat.restype = c_int
+    L.prt_b200_get_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+    if path == LIB_PATH:
+        _lib = L
+    return L
+
+
+class PrtError(RuntimeError):
+    """A non-zero status from the C ABI (the reference throws std::runtime_error)."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+def check(rc: int, ctx=None, L=None) -> None:
+    if rc != PRT_OK:
+        L = L or load()
+        msg = L.prt_b200_last_error(ctx)
+        raise PrtError(rc, msg.decode() if msg else "")

@@ -1,0 +1,418 @@
+// prt_capi.cu - the extern "C" boundary of the GB300 ray-query backend.
+//
+// Each entry point validates its arguments, takes the context's mutex, runs on the
+// context's device and stream, and turns every CUDA or kernel-reported failure into a
+// PRT_ERR_* status plus a message (prt_b200_last_error); nothing aborts or throws
+// across the boundary.  The reference reports errors by printing and carrying on
+// (portableRT include/portableRT/intersect_optix.hpp:34-50); here the C++ wrapper
+// turns a status into std::runtime_error, the reference's exception type for an
+// unusable backend (include/portableRT/nearest_hits_impl.hpp:31-32).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/prt_b200.h"
+#include "prt_build.cuh"
+#include "prt_traverse.cuh"
+
+struct prt_b200_ctx {
+	int device = 0;
+	int sms = 0;
+	cudaStream_t stream = nullptr;
+	std::mutex mu;
+	std::string err;
+	prt::SceneGPU scene;
+	bool scene_set = false;
+	prt::BuildScratch ws;
+	prt::DevBuf tris_in;
+	prt::DevBuf rays_buf, out_buf;
+	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters
+	uint32_t *h_err = nullptr;
+	int leaf_size = 4;
+	int node_format = PRT_NODES_FP32;
+	int block = 128;
+	bool count = false;
+	bool build_compressed = true;
+	double build_ms = 0.0;
+	unsigned long long visits[2] = {0, 0};
+
+	uint32_t *d_work() { return work.as<uint32_t>(); }
+	uint32_t *d_err() { return work.as<uint32_t>() + 1; }
+	unsigned long long *d_visits() {
+		return reinterpret_cast<unsigned long long *>(work.as<uint8_t>() + 16);
+	}
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int fail(prt_b200_ctx *ctx, int code, const std::string &msg) {
+	if (ctx)
+		ctx->err = msg;
+	return code;
+}
+
+int cuda_fail(prt_b200_ctx *ctx, cudaError_t e, const char *what) {
+	return fail(ctx, e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA,
+	            std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CAPI_TRY(ctx, call)                                                                    \
+	do {                                                                                       \
+		cudaError_t e_ = (call);                                                               \
+		if (e_ != cudaSuccess)                                                                 \
+			return cuda_fail((ctx), e_, #call);                                                \
+	} while (0)
+
+bool cc_ok(int dev) {
+	int major = 0, minor = 0;
+	if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess)
+		return false;
+	if (cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
+		return false;
+	return major == 10 && minor == 3;
+}
+
+// Validates a HitReg layout descriptor.
+bool layout_ok(uint32_t mask, uint32_t rec, const uint8_t *off, std::string &why) {
+	if (mask == 0 || mask > 31u) {
+		why = "field_mask must be a non-empty subset of PRT_FIELD_*";
+		return false;
+	}
+	if (rec < 4 || rec > 32 || rec % 4 != 0) {
+		why = "rec_size must be a multiple of 4 in [4, 32]";
+		return false;
+	}
+	if (!off) {
+		why = "offsets pointer is null";
+		return false;
+	}
+	struct F {
+		uint32_t bit;
+		int idx;
+		uint32_t size;
+	} fields[] = {{PRT_FIELD_UV, PRT_OFF_U, 4},      {PRT_FIELD_UV, PRT_OFF_V, 4},
+	              {PRT_FIELD_T, PRT_OFF_T, 4},       {PRT_FIELD_PRIMITIVE_ID, PRT_OFF_PID, 4},
+	              {PRT_FIELD_VALID, PRT_OFF_VALID, 1}, {PRT_FIELD_P, PRT_OFF_PX, 4},
+	              {PRT_FIELD_P, PRT_OFF_PY, 4},      {PRT_FIELD_P, PRT_OFF_PZ, 4}};
+	for (const F &f : fields) {
+		if (!(mask & f.bit))
+			continue;
+		uint32_t o = off[f.idx];
+		if (o + f.size > rec || (f.size == 4 && o % 4 != 0)) {
+			why = "field offset out of range or misaligned";
+			return false;
+		}
+	}
+	return true;
+}
+
+int check_device_errors(prt_b200_ctx *ctx) {
+	CAPI_TRY(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err(), 4, cudaMemcpyDeviceToHost,
+	                              ctx->stream));
+	CAPI_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	uint32_t e = *ctx->h_err;
+	if (e) {
+		cudaMemsetAsync(ctx->d_err(), 0, 4, ctx->stream);
+		cudaStreamSynchronize(ctx->stream);
+		std::string m = "kernel reported:";
+		if (e & prt::kErrStack)
+			m += " traversal stack overflow;";
+		if (e & prt::kErrLookback)
+			m += " radix-sort look-back timed out;";
+		if (e & prt::kErrCollapse)
+			m += " collapse exceeded the node budget;";
+		return fail(ctx, PRT_ERR_DEVICE, m);
+	}
+	return PRT_OK;
+}
+
+int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
+	cudaEvent_t e0, e1;
+	CAPI_TRY(ctx, cudaEventCreate(&e0));
+	CAPI_TRY(ctx, cudaEventCreate(&e1));
+	cudaEventRecord(e0, ctx->stream);
+	std::string msg;
+	int rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
+	                          ctx->ws, ctx->stream, ctx->d_err(), msg);
+	cudaEventRecord(e1, ctx->stream);
+	cudaEventSynchronize(e1);
+	float ms = 0.0f;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	ctx->build_ms = ms;
+	ctx->scene_set = false;
+	if (rc != PRT_OK)
+		return fail(ctx, rc, msg);
+	rc = check_device_errors(ctx);
+	if (rc != PRT_OK)
+		return rc;
+	if (7u * ctx->scene.depth + 1u > 192u)
+		return fail(ctx, PRT_ERR_LIMIT, "tree too deep for the traversal stack");
+	ctx->scene_set = true;
+	return PRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int prt_b200_available(void) {
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess) {
+		cudaGetLastError();
+		return 0;
+	}
+	for (int d = 0; d < n; ++d)
+		if (cc_ok(d))
+			return 1;
+	return 0;
+}
+
+int prt_b200_create(int device, prt_b200_ctx **out) {
+	if (!out) {
+		g_create_error = "out pointer is null";
+		return PRT_ERR_ARG;
+	}
+	*out = nullptr;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n || !cc_ok(device)) {
+		cudaGetLastError();
+		g_create_error = "no compute capability 10.3 device at this index";
+		return PRT_ERR_NO_DEVICE;
+	}
+	prt_b200_ctx *ctx = new (std::nothrow) prt_b200_ctx();
+	if (!ctx) {
+		g_create_error = "out of host memory";
+		return PRT_ERR_OOM;
+	}
+	ctx->device = device;
+	cudaError_t e = cudaSetDevice(device);
+	if (e == cudaSuccess)
+		e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+	if (e == cudaSuccess)
+		e = ctx->work.reserve(64);
+	if (e == cudaSuccess)
+		e = cudaMemset(ctx->work.p, 0, 64);
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&ctx->h_err, 16);
+	if (e == cudaSuccess)
+		e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+	if (e != cudaSuccess) {
+		g_create_error = std::string("create: ") + cudaGetErrorString(e);
+		prt_b200_destroy(ctx);
+		return e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA;
+	}
+	*out = ctx;
+	return PRT_OK;
+}
+
+void prt_b200_destroy(prt_b200_ctx *ctx) {
+	if (!ctx)
+		return;
+	cudaSetDevice(ctx->device);
+	if (ctx->stream)
+		cudaStreamSynchronize(ctx->stream);
+	ctx->scene.release();
+	ctx->ws.release();
+	ctx->tris_in.release();
+	ctx->rays_buf.release();
+	ctx->out_buf.release();
+	ctx->work.release();
+	if (ctx->h_err)
+		cudaFreeHost(ctx->h_err);
+	if (ctx->stream)
+		cudaStreamDestroy(ctx->stream);
+	delete ctx;
+}
+
+const char *prt_b200_last_error(const prt_b200_ctx *ctx) {
+	return ctx ? ctx->err.c_str() : g_create_error.c_str();
+}
+
+int prt_b200_device_name(prt_b200_ctx *ctx, char *buf, size_t len) {
+	if (!ctx || !buf || len == 0)
+		return fail(ctx, PRT_ERR_ARG, "device_name: bad argument");
+	cudaDeviceProp p;
+	CAPI_TRY(ctx, cudaGetDeviceProperties(&p, ctx->device));
+	std::snprintf(buf, len, "%s", p.name);
+	return PRT_OK;
+}
+
+int prt_b200_set_tris(prt_b200_ctx *ctx, const float *tris9, uint64_t n) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	if (!tris9 && n)
+		return fail(ctx, PRT_ERR_ARG, "set_tris: null triangle pointer");
+	if (n > prt::kMaxTris)
+		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 268435455 triangles per scene");
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	if (n) {
+		CAPI_TRY(ctx, ctx->tris_in.reserve(36ull * n));
+		CAPI_TRY(ctx, cudaMemcpyAsync(ctx->tris_in.p, tris9, 36ull * n, cudaMemcpyHostToDevice,
+		                              ctx->stream));
+	}
+	return do_build(ctx, ctx->tris_in.as<float>(), n);
+}
+
+int prt_b200_set_tris_dev(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	if (!d_tris9 && n)
+		return fail(ctx, PRT_ERR_ARG, "set_tris_dev: null triangle pointer");
+	if (n > prt::kMaxTris)
+		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 268435455 triangles per scene");
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	return do_build(ctx, d_tris9, n);
+}
+
+int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n,
+                              uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                              void *d_out, void *stream) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!layout_ok(field_mask, rec_size, offs, why))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
+	if (n && (!d_rays6 || !d_out))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
+	if (reinterpret_cast<uintptr_t>(d_rays6) % 8 != 0)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: rays must be 8-byte aligned");
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	if (!ctx->scene_set)
+		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
+	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: compressed nodes were not built");
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	if (n == 0)
+		return PRT_OK;
+	prt::OutLayout lay;
+	lay.mask = field_mask;
+	lay.rec_size = rec_size;
+	std::memcpy(lay.off, offs, 8);
+	prt::TravConfig cfg;
+	cfg.format = ctx->node_format;
+	cfg.block = ctx->block;
+	cfg.count = ctx->count;
+	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays6, n, lay, d_out, cfg,
+	                                       ctx->d_work(), ctx->d_visits(), ctx->d_err(), st,
+	                                       ctx->sms));
+	return PRT_OK;
+}
+
+int prt_b200_sync(prt_b200_ctx *ctx) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	CAPI_TRY(ctx, cudaDeviceSynchronize());
+	if (ctx->count) {
+		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
+	}
+	return check_device_errors(ctx);
+}
+
+int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uint32_t field_mask,
+                          uint32_t rec_size, const uint8_t offs[8], void *out_host) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!layout_ok(field_mask, rec_size, offs, why))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
+	if (n && (!rays6 || !out_host))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
+	{
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		if (!ctx->scene_set)
+			return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
+		if (n == 0)
+			return PRT_OK;
+		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+		CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
+		CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
+		CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.p, rays6, 24ull * n, cudaMemcpyHostToDevice,
+		                              ctx->stream));
+	}
+	int rc = prt_b200_nearest_hits_dev(ctx, ctx->rays_buf.as<float>(), n, field_mask, rec_size,
+	                                   offs, ctx->out_buf.p, nullptr);
+	if (rc != PRT_OK)
+		return rc;
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	CAPI_TRY(ctx, cudaMemcpyAsync(out_host, ctx->out_buf.p, (uint64_t)rec_size * n,
+	                              cudaMemcpyDeviceToHost, ctx->stream));
+	CAPI_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	if (ctx->count)
+		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
+	return check_device_errors(ctx);
+}
+
+int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
+	if (!ctx || !key)
+		return PRT_ERR_ARG;
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	std::string k(key);
+	if (k == "leaf_size") {
+		if (v < 1 || v > prt::kMaxLeaf)
+			return fail(ctx, PRT_ERR_ARG, "leaf_size must be in [1, 8]");
+		ctx->leaf_size = (int)v;
+	} else if (k == "node_format") {
+		if (v != PRT_NODES_FP32 && v != PRT_NODES_COMPRESSED)
+			return fail(ctx, PRT_ERR_ARG, "node_format must be 0 or 1");
+		ctx->node_format = (int)v;
+	} else if (k == "block") {
+		if (v < 32 || v > 128 || v % 32)
+			return fail(ctx, PRT_ERR_ARG, "block must be 32, 64, 96 or 128");
+		ctx->block = (int)v;
+	} else if (k == "count_visits") {
+		ctx->count = v != 0;
+	} else if (k == "build_compressed") {
+		ctx->build_compressed = v != 0;
+	} else {
+		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
+	}
+	return PRT_OK;
+}
+
+int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
+	if (!ctx || !key || !value)
+		return PRT_ERR_ARG;
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	std::string k(key);
+	const prt::SceneGPU &s = ctx->scene;
+	if (k == "n_tris")
+		*value = (double)s.n_tris;
+	else if (k == "n_nodes")
+		*value = s.n_nodes;
+	else if (k == "depth")
+		*value = s.depth;
+	else if (k == "build_ms")
+		*value = ctx->build_ms;
+	else if (k == "node_bytes")
+		*value = (double)s.n_nodes *
+		         (ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8) : sizeof(prt::Node8));
+	else if (k == "node_size")
+		*value = (double)(ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8)
+		                                                            : sizeof(prt::Node8));
+	else if (k == "tri_bytes")
+		*value = 48.0 * (double)s.n_tris;
+	else if (k == "visits_nodes")
+		*value = (double)ctx->visits[0];
+	else if (k == "visits_tris")
+		*value = (double)ctx->visits[1];
+	else if (k == "sms")
+		*value = ctx->sms;
+	else if (k == "leaf_size")
+		*value = s.leaf_size;
+	else
+		return fail(ctx, PRT_ERR_ARG, "unknown statistic " + k);
+	return PRT_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,66 @@
+"""CPU-only checks of the C ABI library: it loads, exports every symbol the header
+declares, and reports (not crashes) when no GPU is present.  No compute call is made."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+from portablert_gb300 import _lib, build, hitreg
+
+HEADER = os.path.join(ROOT, "include", "prt_b200.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"\b(prt_b200_\w+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build_library()
+    return _lib.load()
+
+
+def test_header_and_binding_agree():
+    assert declared_functions() == sorted(_lib.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r"\bT (prt_b200_\w+)", out))
+    missing = set(declared_functions()) - exported
+    assert not missing, missing
+    for name in declared_functions():
+        assert hasattr(lib, name)
+
+
+def test_no_gpu_is_reported_not_fatal(lib):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    assert lib.prt_b200_available() == 0
+    h = ctypes.c_void_p()
+    rc = lib.prt_b200_create(0, ctypes.byref(h))
+    assert rc == 3 and not h.value
+    assert b"10.3" in lib.prt_b200_last_error(None)
+
+
+def test_null_context_is_an_argument_error(lib):
+    assert lib.prt_b200_set_tris(None, None, 0) == 1
+    lay = hitreg.layout(hitreg.TAGS)
+    assert lib.prt_b200_nearest_hits(None, None, 0, lay.mask, lay.size, lay.offsets8(),
+                                     None) == 1
+    assert lib.prt_b200_set_option(None, b"leaf_size", 4) == 1
+
+
+def test_cpp_api_compiles_and_links():
+    exe = build.build_cpp_test()
+    assert os.path.exists(exe)
