@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(128)
                const uint32_t *__restrict__ left, const uint32_t *__restrict__ right,
                const uint32_t *__restrict__ rfirst, const uint32_t *__restrict__ rlast,
                const float4 *__restrict__ ibox, const float4 *__restrict__ lbox,
-               uint32_t leaf_size, uint32_t *err) {
+               uint32_t leaf_size, uint32_t n_tris, uint32_t *err) {
 	const uint32_t n_in = *in_count;
 	for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_in;
 	     w += gridDim.x * blockDim.x) {
@@ -303,6 +303,10 @@ __global__ void __launch_bounds__(128)
 			continue;
 		}
 		uint32_t tbase = n_leaf_tris ? atomicAdd(tri_counter, n_leaf_tris) : 0u;
+		if (tbase + n_leaf_tris > n_tris) {
+			atomicOr(err, kErrCollapse);
+			continue;
+		}
 		Node8 *nd = nodes + it.slot;
 		uint32_t k_inner = 0, toff = 0;
 		for (int c = 0; c < 8; ++c) {
@@ -552,7 +556,7 @@ int build_scene(const float *d_tris, uint64_t n64, int leaf_size, bool compresse
 		                                 ws.left.as<uint32_t>(), ws.right.as<uint32_t>(),
 		                                 ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>(),
 		                                 ws.ibox.as<float4>(), ws.lbox.as<float4>(),
-		                                 (uint32_t)leaf_size, d_err);
+		                                 (uint32_t)leaf_size, n, d_err);
 		++level;
 		BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ctr, 16, cudaMemcpyDeviceToHost, st));
 		BUILD_TRY(cudaStreamSynchronize(st));
