@@ -75,7 +75,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -231,8 +231,12 @@ def run_gpu(args, world, rank):
     d_rays = torch.from_numpy(rays).cuda()
     d_out = torch.empty(n * lay.size, dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device="cuda")
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: the kernels, the events and the L2 flush all go on it (the
+    # legacy default stream has handle 0, which the C ABI reads as "context stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
+    assert sptr != 0
 
     def step():
         b.nearest_hits_dev(d_rays.data_ptr(), n, d_out.data_ptr(), TAGS, sptr)
@@ -348,7 +352,7 @@ def run_gpu(args, world, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="b200", choices=["b200", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
