@@ -258,12 +258,15 @@ __global__ void __launch_bounds__(128)
 		uint32_t C[8];
 		int nc = 1;
 		C[0] = it.ref;
+		// Open the binary child of largest surface area until 8 children: any binary
+		// node can be opened, so nodes fill up and small subtrees end as single
+		// triangles (whose box is then tested exactly like the reference's leaf box).
 		while (nc < 8) {
 			int best = -1;
 			float best_area = -1.0f;
 			for (int c = 0; c < nc; ++c) {
 				uint32_t r = C[c];
-				if (!(r & kLeafBit) && bcount(r, rfirst, rlast) > leaf_size) {
+				if (!(r & kLeafBit)) {
 					float a = half_area(ibox[2 * r], ibox[2 * r + 1]);
 					if (a > best_area) {
 						best_area = a;
@@ -347,11 +350,13 @@ __global__ void __launch_bounds__(128)
 }
 
 __global__ void k_relayout(const float *__restrict__ tris, const uint32_t *__restrict__ vals,
-                           const uint32_t *__restrict__ perm, uint32_t n, float4 *tri4) {
+                           const uint32_t *__restrict__ perm, uint32_t n, float4 *tri4,
+                           uint32_t *inv) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n)
 		return;
 	uint32_t pid = vals[perm[i]];
+	inv[pid] = i;
 	const float *t = tris + 9 * (size_t)pid;
 	tri4[3 * (size_t)i] = make_float4(t[0], t[1], t[2], __uint_as_float(pid));
 	tri4[3 * (size_t)i + 1] = make_float4(t[3], t[4], t[5], 0.0f);
@@ -509,6 +514,7 @@ int build_scene(const float *d_tris, uint64_t n64, int leaf_size, bool compresse
 	BUILD_TRY(ws.sort_status.reserve(4 * sort_status_words(n)));
 	BUILD_TRY(ws.bounds.reserve(32));
 	BUILD_TRY(sc.tri4.reserve(48ull * n));
+	BUILD_TRY(sc.inv.reserve(4ull * n));
 	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)node_cap));
 	if (!ws.h_counters)
 		BUILD_TRY(cudaMallocHost(&ws.h_counters, 64));
@@ -577,7 +583,7 @@ int build_scene(const float *d_tris, uint64_t n64, int leaf_size, bool compresse
 		return PRT_ERR_DEVICE;
 	}
 	k_relayout<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, ws.perm.as<uint32_t>(), n,
-	                                               sc.tri4.as<float4>());
+	                                               sc.tri4.as<float4>(), sc.inv.as<uint32_t>());
 	if (compressed) {
 		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * (size_t)sc.n_nodes));
 		k_compress<<<blocks_for(sc.n_nodes, 128), 128, 0, st>>>(sc.nodes.as<Node8>(), sc.n_nodes,

@@ -43,10 +43,12 @@ struct SceneGPU {
 	int leaf_size = 4;
 	bool has_cnodes = false;
 	DevBuf tri4;   // float4[3 n]
+	DevBuf inv;    // uint32[n]: primitive id -> position in tri4
 	DevBuf nodes;  // Node8[n_nodes]
 	DevBuf cnodes; // CNode8[n_nodes]
 	void release() {
 		tri4.release();
+		inv.release();
 		nodes.release();
 		cnodes.release();
 		n_tris = 0;

@@ -151,7 +151,7 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	rc = check_device_errors(ctx);
 	if (rc != PRT_OK)
 		return rc;
-	if (7u * ctx->scene.depth + 1u > 192u)
+	if ((int)ctx->scene.depth > prt::traversal_stack_depth())
 		return fail(ctx, PRT_ERR_LIMIT, "tree too deep for the traversal stack");
 	ctx->scene_set = true;
 	return PRT_OK;

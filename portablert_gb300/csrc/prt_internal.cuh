@@ -254,18 +254,36 @@ __device__ __forceinline__ void best_offer(Best &b, float t, float u, float v, u
 }
 
 // Exact per-triangle test: the reference slab test on the triangle's own bounding
-// box (make_aabb, bvh.hpp:28-37, select semantics) and then Moller-Trumbore.
-__device__ __forceinline__ void test_triangle(const RayC &r, const float4 a, const float4 b,
-                                              const float4 c, Best &best) {
+// box (make_aabb, bvh.hpp:28-37, select semantics) and then Moller-Trumbore.  True
+// when the reference would accept the triangle (its t may still be +inf or NaN, which
+// the reference never records).
+__device__ __forceinline__ bool tri_test(const RayC &r, const float4 a, const float4 b,
+                                         const float4 c, float &t, float &u, float &v) {
 	float lx = rmin(a.x, rmin(b.x, c.x)), ly = rmin(a.y, rmin(b.y, c.y)),
 	      lz = rmin(a.z, rmin(b.z, c.z));
 	float hx = rmax(a.x, rmax(b.x, c.x)), hy = rmax(a.y, rmax(b.y, c.y)),
 	      hz = rmax(a.z, rmax(b.z, c.z));
 	if (!ref_slab(r, lx, ly, lz, hx, hy, hz))
-		return;
+		return false;
+	return ref_mt(r, a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, t, u, v);
+}
+
+__device__ __forceinline__ void test_triangle(const RayC &r, const float4 a, const float4 b,
+                                              const float4 c, Best &best) {
 	float t, u, v;
-	if (ref_mt(r, a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, t, u, v))
+	if (tri_test(r, a, b, c, t, u, v))
 		best_offer(best, t, u, v, __float_as_uint(a.w));
+}
+
+// The closest hit as one 64-bit key: order-preserving bits of t above the primitive
+// id, so the minimum key is the smallest t and, among equal t, the smallest id (the
+// same rule as best_offer).  -0 and +0 compare equal as floats, so both map to +0's
+// key; the hit itself is recomputed from the winning id.  kNoHit: nothing recorded.
+constexpr unsigned long long kNoHit = ~0ull;
+
+__device__ __forceinline__ unsigned long long hit_key(float t, uint32_t pid) {
+	float tc = (t == 0.0f) ? 0.0f : t;
+	return ((unsigned long long)f2ord(tc) << 32) | pid;
 }
 
 } // namespace prt

@@ -7,14 +7,24 @@
 // triangles whose own bounding box passes the reference slab test and which
 // Moller-Trumbore accepts; t may be negative, there is no t-min and no culling by t,
 // exactly as in the reference.  Inner nodes only prune with tests that are
-// conservative for that set (prt_internal.cuh), so the tree's shape and the visit
-// order do not change the answer; ties in t go to the smaller primitive id.
+// conservative for that set (prt_internal.cuh), so neither the tree's shape nor the
+// visit order changes the answer; ties in t go to the smaller primitive id.
 //
-// Execution: a persistent grid (resident blocks on every SM); each warp takes 32
-// consecutive rays at a time from a global counter, one ray per thread, with a
-// per-thread stack of child references.  Hit records are assembled in shared memory
-// in the caller's HitReg<Tags...> layout and the warp writes its 32 records (a
-// contiguous, 128-B aligned run) with 16-byte stores.
+// Execution (one warp = 4 groups of 8 lanes):
+//  * A warp takes 32 consecutive rays from a global counter; their origin, direction,
+//    reciprocal and best-hit key live in shared memory ("slots").  Groups take slots
+//    one after another until the 32 are done.
+//  * Node step: a group holds one ray; lane c loads child c of the current node (each
+//    field of the 8 children is one 32-byte row, so the group's loads are coalesced)
+//    and runs the slab test.  Ballots give the children hit; inner children of a node
+//    are contiguous (child_base + rank), so the group's stack keeps one 8-byte entry
+//    (child_base, inner bits, pending bits) per tree level in shared memory.
+//  * Leaf triangles that pass the node test are appended to a warp queue; whenever 32
+//    are pending, the 32 lanes test one triangle each with the exact reference test
+//    and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
+//  * When the batch is done the warp recomputes the winning triangle of each slot
+//    (identical arithmetic, so identical t, u, v), writes the 32 records in the caller's
+//    HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
 //
 // Algorithmic bytes per ray: 24 (ray) + R (record) + node bytes visited + 48 per
 // triangle tested; the counting variant (COUNT) measures the visits.
@@ -27,10 +37,13 @@ namespace prt {
 
 namespace {
 
-constexpr int kStack = 192;
+constexpr int kWarpsPerBlock = 4;
+constexpr int kStackDepth = 32;
+constexpr int kQueueCap = 32 + 4 * 8 * kMaxLeaf; // pending < 32 + one step's worth
 
 struct TravArgs {
 	const float4 *tri4;
+	const uint32_t *inv;
 	const void *nodes;
 	const float *rays;
 	uint8_t *out;
@@ -45,6 +58,15 @@ struct TravArgs {
 	unsigned long long *visits;
 };
 
+struct WarpSmem {
+	uint2 stack[4][kStackDepth];     // per group: (child_base, inner << 8 | pending)
+	uint2 queue[kQueueCap];          // (slot, triangle position)
+	unsigned long long key[32];      // best (t, primitive id) per slot
+	float ray[32][9];                // origin, direction, reciprocal per slot
+	int kind[32];
+	uint32_t stage[32 * 8];          // output records, 32 x 32 B
+};
+
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
 	return r.kind == 0 ? regular_box(r, lx, hx, ly, hy, lz, hz)
@@ -53,107 +75,45 @@ __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, floa
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 
-template <int FMT, bool COUNT>
-__device__ __forceinline__ bool trace(const TravArgs &a, const RayC &r, Best &best,
-                                      uint32_t &n_nodes, uint32_t &n_tris) {
-	uint32_t stack[kStack];
-	int sp = 0;
-	stack[sp++] = 0u;
-	while (sp > 0) {
-		const uint32_t ref = stack[--sp];
-		if (ref_is_leaf(ref)) {
-			const uint32_t cnt = leaf_count(ref);
-			const float4 *p = a.tri4 + 3 * (size_t)leaf_first(ref);
-			for (uint32_t k = 0; k < cnt; ++k) {
-				float4 A = __ldg(p + 3 * k), B = __ldg(p + 3 * k + 1), C = __ldg(p + 3 * k + 2);
-				test_triangle(r, A, B, C, best);
-			}
-			if (COUNT)
-				n_tris += cnt;
-			continue;
-		}
+__device__ __forceinline__ RayC slot_ray(const WarpSmem &S, int s) {
+	RayC r;
+	r.ox = S.ray[s][0];
+	r.oy = S.ray[s][1];
+	r.oz = S.ray[s][2];
+	r.dx = S.ray[s][3];
+	r.dy = S.ray[s][4];
+	r.dz = S.ray[s][5];
+	r.fx = S.ray[s][6];
+	r.fy = S.ray[s][7];
+	r.fz = S.ray[s][8];
+	r.kind = S.kind[s];
+	return r;
+}
+
+// Tests queue entries [lo, lo + n) (n <= 32), one per lane.
+template <bool COUNT>
+__device__ __forceinline__ void test_queued(const TravArgs &a, WarpSmem &S, uint32_t lo,
+                                            uint32_t n, int lane, uint32_t &n_tests) {
+	if ((uint32_t)lane < n) {
+		const uint2 e = S.queue[lo + lane];
+		const RayC r = slot_ray(S, (int)e.x);
+		const float4 *p = a.tri4 + 3 * (size_t)e.y;
+		const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
+		float t, u, v;
+		if (tri_test(r, A, B, C, t, u, v) && t < INFINITY)
+			atomicMin(&S.key[e.x], hit_key(t, __float_as_uint(A.w)));
 		if (COUNT)
-			++n_nodes;
-		if (FMT == PRT_NODES_FP32) {
-			const float4 *np = reinterpret_cast<const float4 *>(
-			    static_cast<const Node8 *>(a.nodes) + ref);
-			float4 q[12];
-#pragma unroll
-			for (int i = 0; i < 12; ++i)
-				q[i] = __ldg(np + i);
-			const uint4 r0 = __ldg(reinterpret_cast<const uint4 *>(np) + 12);
-			const uint4 r1 = __ldg(reinterpret_cast<const uint4 *>(np) + 13);
-			const float lx[8] = {q[0].x, q[0].y, q[0].z, q[0].w, q[1].x, q[1].y, q[1].z, q[1].w};
-			const float hx[8] = {q[2].x, q[2].y, q[2].z, q[2].w, q[3].x, q[3].y, q[3].z, q[3].w};
-			const float ly[8] = {q[4].x, q[4].y, q[4].z, q[4].w, q[5].x, q[5].y, q[5].z, q[5].w};
-			const float hy[8] = {q[6].x, q[6].y, q[6].z, q[6].w, q[7].x, q[7].y, q[7].z, q[7].w};
-			const float lz[8] = {q[8].x, q[8].y, q[8].z, q[8].w, q[9].x, q[9].y, q[9].z, q[9].w};
-			const float hz[8] = {q[10].x, q[10].y, q[10].z, q[10].w,
-			                     q[11].x, q[11].y, q[11].z, q[11].w};
-			const uint32_t rf[8] = {r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w};
-#pragma unroll
-			for (int c = 0; c < 8; ++c) {
-				if (rf[c] == kNone)
-					continue;
-				if (box_test(r, lx[c], hx[c], ly[c], hy[c], lz[c], hz[c])) {
-					if (sp >= kStack)
-						return false;
-					stack[sp++] = rf[c];
-				}
-			}
-		} else {
-			const uint4 *np = reinterpret_cast<const uint4 *>(
-			    static_cast<const CNode8 *>(a.nodes) + ref);
-			const uint4 w0 = __ldg(np), w1 = __ldg(np + 1), w2 = __ldg(np + 2), w3 = __ldg(np + 3),
-			            w4 = __ldg(np + 4);
-			const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
-			            oz = __uint_as_float(w0.z);
-			const float sx = cscale((uint8_t)byte_of(w0.w, 0)), sy = cscale((uint8_t)byte_of(w0.w, 1)),
-			            sz = cscale((uint8_t)byte_of(w0.w, 2));
-			const uint32_t imask = byte_of(w0.w, 3);
-			const uint32_t child_base = w1.x, tri_base = w1.y;
-			const uint32_t meta[2] = {w1.z, w1.w};
-			// q rows: lo_x = w2.x,w2.y  hi_x = w2.z,w2.w  lo_y = w3.x,w3.y  hi_y = w3.z,w3.w
-			//         lo_z = w4.x,w4.y  hi_z = w4.z,w4.w
-			uint32_t inner_rank = 0, toff = 0;
-#pragma unroll
-			for (int c = 0; c < 8; ++c) {
-				const int h = c >> 2, b = c & 3;
-				const uint32_t m = byte_of(meta[h], b);
-				const bool inner = (imask >> c) & 1u;
-				uint32_t child;
-				if (inner)
-					child = child_base + inner_rank++;
-				else if (m)
-					child = make_leaf(tri_base + toff, m);
-				else
-					continue;
-				toff += m;
-				const float lxc = __fadd_rn(ox, __fmul_rn((float)byte_of(h ? w2.y : w2.x, b), sx));
-				const float hxc = __fadd_rn(ox, __fmul_rn((float)byte_of(h ? w2.w : w2.z, b), sx));
-				const float lyc = __fadd_rn(oy, __fmul_rn((float)byte_of(h ? w3.y : w3.x, b), sy));
-				const float hyc = __fadd_rn(oy, __fmul_rn((float)byte_of(h ? w3.w : w3.z, b), sy));
-				const float lzc = __fadd_rn(oz, __fmul_rn((float)byte_of(h ? w4.y : w4.x, b), sz));
-				const float hzc = __fadd_rn(oz, __fmul_rn((float)byte_of(h ? w4.w : w4.z, b), sz));
-				if (box_test(r, lxc, hxc, lyc, hyc, lzc, hzc)) {
-					if (sp >= kStack)
-						return false;
-					stack[sp++] = child;
-				}
-			}
-		}
+			++n_tests;
 	}
-	return true;
 }
 
 template <int FMT, bool COUNT>
-__global__ void __launch_bounds__(128) k_nearest(TravArgs a) {
-	extern __shared__ __align__(16) uint32_t stage_all[];
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	uint32_t *stage = stage_all + warp * 256; // 32 records x 32 B
-	uint8_t *stage_b = reinterpret_cast<uint8_t *>(stage);
-	const uint32_t rw = a.rec_size >> 2;
-	uint32_t n_nodes = 0, n_tris = 0;
+__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
+	extern __shared__ __align__(16) unsigned char smem_raw[];
+	WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
+	const int lane = threadIdx.x & 31, g = lane >> 3, c = lane & 7;
+	uint32_t n_visits = 0, n_tests = 0;
+
 	for (;;) {
 		uint32_t base = 0;
 		if (lane == 0)
@@ -161,23 +121,204 @@ __global__ void __launch_bounds__(128) k_nearest(TravArgs a) {
 		base = __shfl_sync(0xFFFFFFFFu, base, 0);
 		if (base >= a.n_rays)
 			break;
-		const uint32_t i = base + lane;
-		const bool active = i < a.n_rays;
-		Best best;
-		best_init(best);
-		RayC r;
-		if (active) {
-			const float2 *rp = reinterpret_cast<const float2 *>(a.rays + 6 * (size_t)i);
+		const uint32_t nb = min(32u, a.n_rays - base);
+
+		if ((uint32_t)lane < nb) {
+			const float2 *rp = reinterpret_cast<const float2 *>(a.rays + 6 * (size_t)(base + lane));
 			const float2 p0 = __ldg(rp), p1 = __ldg(rp + 1), p2 = __ldg(rp + 2);
-			r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
-			if (a.n_tris && !trace<FMT, COUNT>(a, r, best, n_nodes, n_tris))
-				atomicOr(a.err, kErrStack);
+			const RayC r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+			float *sr = S.ray[lane];
+			sr[0] = r.ox; sr[1] = r.oy; sr[2] = r.oz;
+			sr[3] = r.dx; sr[4] = r.dy; sr[5] = r.dz;
+			sr[6] = r.fx; sr[7] = r.fy; sr[8] = r.fz;
+			S.kind[lane] = r.kind;
 		}
-		for (uint32_t w = 0; w < rw; ++w)
-			stage[lane * rw + w] = 0u;
+		S.key[lane] = kNoHit;
 		__syncwarp();
-		if (active) {
-			uint8_t *rb = stage_b + lane * a.rec_size;
+
+		if (a.n_tris) {
+			int slot = -1;          // group's ray slot (-1: none)
+			RayC r;
+			uint32_t cur_base = 0, cur_inner = 0, cur_pend = 0;
+			int sp = 0;
+			uint32_t next = 0;      // next slot to hand out (warp-uniform)
+			uint32_t q = 0;         // queued triangles (warp-uniform)
+			for (;;) {
+				// Hand the next slots to groups that have no pending work.
+				const bool idle = slot < 0 || (cur_pend == 0 && sp == 0);
+				const uint32_t idle_lead = __ballot_sync(0xFFFFFFFFu, idle && c == 0);
+				if (idle) {
+					const uint32_t s = next + __popc(idle_lead & ((1u << (8 * g)) - 1u));
+					if (s < nb) {
+						slot = (int)s;
+						r = slot_ray(S, slot);
+						cur_base = 0; // the root is node 0: "inner child 0 of a virtual parent"
+						cur_inner = 1;
+						cur_pend = 1;
+						sp = 0;
+					} else {
+						slot = -1;
+					}
+				}
+				next = min(nb, next + __popc(idle_lead));
+				const bool work = slot >= 0;
+				if (!__any_sync(0xFFFFFFFFu, work))
+					break;
+
+				// Next node of this group: a pending inner child at the current level,
+				// else the top of the stack.
+				uint32_t node = 0;
+				if (work) {
+					if (cur_pend == 0) {
+						--sp;
+						const uint2 e = S.stack[g][sp];
+						cur_base = e.x;
+						cur_inner = e.y >> 8;
+						cur_pend = e.y & 0xFFu;
+					}
+					const int cc = __ffs(cur_pend) - 1;
+					node = cur_base + __popc(cur_inner & ((1u << cc) - 1u));
+					cur_pend &= cur_pend - 1u;
+					if (COUNT && c == 0)
+						++n_visits;
+				}
+
+				// Lane c tests child c of `node`.
+				bool hit = false, inner = false;
+				uint32_t leaf_first_tri = 0, leaf_n = 0, child_base = 0;
+				if (work) {
+					if (FMT == PRT_NODES_FP32) {
+						const Node8 *nd = static_cast<const Node8 *>(a.nodes) + node;
+						const uint32_t ref = __ldg(&nd->ref[c]);
+						if (ref != kNone) {
+							inner = !ref_is_leaf(ref);
+							hit = box_test(r, __ldg(&nd->lo_x[c]), __ldg(&nd->hi_x[c]),
+							               __ldg(&nd->lo_y[c]), __ldg(&nd->hi_y[c]),
+							               __ldg(&nd->lo_z[c]), __ldg(&nd->hi_z[c]));
+							if (!inner) {
+								leaf_first_tri = leaf_first(ref);
+								leaf_n = leaf_count(ref);
+							} else {
+								child_base = ref; // fixed up below from the first inner child
+							}
+						}
+					} else {
+						const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
+						const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
+						const uint4 w1 = __ldg(reinterpret_cast<const uint4 *>(cn) + 1);
+						const uint32_t imask = byte_of(w0.w, 3);
+						const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
+						inner = (imask >> c) & 1u;
+						if (inner || m) {
+							const uint8_t *qb = reinterpret_cast<const uint8_t *>(cn) + 32 + c;
+							const float sx = cscale((uint8_t)byte_of(w0.w, 0));
+							const float sy = cscale((uint8_t)byte_of(w0.w, 1));
+							const float sz = cscale((uint8_t)byte_of(w0.w, 2));
+							const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
+							            oz = __uint_as_float(w0.z);
+							const float lx = __fadd_rn(ox, __fmul_rn((float)__ldg(qb + 0), sx));
+							const float hx = __fadd_rn(ox, __fmul_rn((float)__ldg(qb + 8), sx));
+							const float ly = __fadd_rn(oy, __fmul_rn((float)__ldg(qb + 16), sy));
+							const float hy = __fadd_rn(oy, __fmul_rn((float)__ldg(qb + 24), sy));
+							const float lz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 32), sz));
+							const float hz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 40), sz));
+							hit = box_test(r, lx, hx, ly, hy, lz, hz);
+							if (!inner) {
+								// first triangle = tri_base + counts of the leaf children before c
+								const uint32_t lo_w = w1.z, hi_w = w1.w;
+								uint32_t before;
+								if (c < 4)
+									before = __dp4a(lo_w & ((1u << (8 * c)) - 1u), 0x01010101u, 0u);
+								else
+									before = __dp4a(lo_w, 0x01010101u, 0u) +
+									         __dp4a(hi_w & ((1u << (8 * (c - 4))) - 1u), 0x01010101u, 0u);
+								leaf_first_tri = w1.y + before;
+								leaf_n = m;
+							}
+						}
+						child_base = w1.x;
+					}
+				}
+				const uint32_t inner_all = __ballot_sync(0xFFFFFFFFu, inner);
+				const uint32_t inner_hit = __ballot_sync(0xFFFFFFFFu, inner && hit);
+				if (FMT == PRT_NODES_FP32) {
+					// child_base = reference of the group's first inner child (rank 0).
+					const uint32_t gi = (inner_all >> (8 * g)) & 0xFFu;
+					const int src = gi ? (8 * g + __ffs(gi) - 1) : lane;
+					child_base = __shfl_sync(0xFFFFFFFFu, child_base, src);
+				}
+				if (work) {
+					// Descend into the hit inner children of `node`; the siblings still
+					// pending at this level go on the stack (one entry per level).
+					const uint32_t gh = (inner_hit >> (8 * g)) & 0xFFu;
+					if (gh) {
+						if (cur_pend) {
+							if (sp < kStackDepth) {
+								if (c == 0)
+									S.stack[g][sp] = make_uint2(cur_base, (cur_inner << 8) | cur_pend);
+								++sp;
+							} else if (c == 0) {
+								atomicOr(a.err, kErrStack);
+							}
+						}
+						cur_base = child_base;
+						cur_inner = (inner_all >> (8 * g)) & 0xFFu;
+						cur_pend = gh;
+					}
+				}
+
+				// Queue the triangles of the leaf children that were hit.
+				const uint32_t cnt = (hit && !inner) ? leaf_n : 0u;
+				uint32_t incl = cnt;
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+					if (lane >= o)
+						incl += y;
+				}
+				const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+				const uint32_t pos = q + incl - cnt;
+				for (uint32_t k = 0; k < cnt; ++k)
+					S.queue[pos + k] = make_uint2((uint32_t)slot, leaf_first_tri + k);
+				q += total;
+				__syncwarp();
+				while (q >= 32u) {
+					q -= 32u;
+					test_queued<COUNT>(a, S, q, 32u, lane, n_tests);
+					__syncwarp();
+				}
+			}
+			while (q > 0u) {
+				const uint32_t n = min(q, 32u);
+				q -= n;
+				test_queued<COUNT>(a, S, q, n, lane, n_tests);
+				__syncwarp();
+			}
+		}
+		__syncwarp();
+
+		// Finalise: recompute the winning triangle of each slot and stage the record.
+		const uint32_t rw = a.rec_size >> 2;
+		for (uint32_t w = 0; w < rw; ++w)
+			S.stage[lane * rw + w] = 0u;
+		__syncwarp();
+		if ((uint32_t)lane < nb) {
+			const RayC r = slot_ray(S, lane);
+			Best best;
+			best_init(best);
+			const unsigned long long key = S.key[lane];
+			if (key != kNoHit) {
+				const uint32_t pid = (uint32_t)key;
+				const float4 *p = a.tri4 + 3 * (size_t)__ldg(&a.inv[pid]);
+				float t, u, v;
+				if (tri_test(r, __ldg(p), __ldg(p + 1), __ldg(p + 2), t, u, v)) {
+					best.t = t;
+					best.u = u;
+					best.v = v;
+					best.pid = pid;
+				}
+			}
+			uint8_t *rb = reinterpret_cast<uint8_t *>(S.stage) + lane * a.rec_size;
 			if (a.mask & PRT_FIELD_UV) {
 				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_U]) = best.u;
 				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_V]) = best.v;
@@ -199,26 +340,26 @@ __global__ void __launch_bounds__(128) k_nearest(TravArgs a) {
 			}
 		}
 		__syncwarp();
-		const uint32_t nrec = min(32u, a.n_rays - base);
 		uint8_t *dst = a.out + (size_t)base * a.rec_size;
-		const uint32_t bytes = nrec * a.rec_size;
-		if (a.store_mode == 0 && nrec == 32u) {
+		const uint32_t bytes = nb * a.rec_size;
+		if (a.store_mode == 0 && nb == 32u) {
 			uint4 *d4 = reinterpret_cast<uint4 *>(dst);
-			const uint4 *s4 = reinterpret_cast<const uint4 *>(stage);
-			for (uint32_t c = lane; c < bytes / 16u; c += 32u)
-				d4[c] = s4[c];
+			const uint4 *s4 = reinterpret_cast<const uint4 *>(S.stage);
+			for (uint32_t k = lane; k < bytes / 16u; k += 32u)
+				d4[k] = s4[k];
 		} else if (a.store_mode <= 1) {
 			uint32_t *d1 = reinterpret_cast<uint32_t *>(dst);
-			for (uint32_t c = lane; c < bytes / 4u; c += 32u)
-				d1[c] = stage[c];
+			for (uint32_t k = lane; k < bytes / 4u; k += 32u)
+				d1[k] = S.stage[k];
 		} else {
-			for (uint32_t c = lane; c < bytes; c += 32u)
-				dst[c] = stage_b[c];
+			const uint8_t *sb = reinterpret_cast<const uint8_t *>(S.stage);
+			for (uint32_t k = lane; k < bytes; k += 32u)
+				dst[k] = sb[k];
 		}
 		__syncwarp();
 	}
 	if (COUNT) {
-		unsigned long long a0 = n_nodes, a1 = n_tris;
+		unsigned long long a0 = n_visits, a1 = n_tests;
 		for (int o = 16; o > 0; o >>= 1) {
 			a0 += __shfl_xor_sync(0xFFFFFFFFu, a0, o);
 			a1 += __shfl_xor_sync(0xFFFFFFFFu, a1, o);
@@ -230,27 +371,32 @@ __global__ void __launch_bounds__(128) k_nearest(TravArgs a) {
 	}
 }
 
-template <int FMT, bool COUNT> int blocks_per_sm(int block) {
-	static int cached_block = -1, cached = 0;
-	if (cached_block != block) {
+// Resident blocks per SM for a block of `warps` warps (cached per block size).
+template <int FMT, bool COUNT> int blocks_per_sm(int warps) {
+	static int cached[kWarpsPerBlock + 1] = {0};
+	if (!cached[warps]) {
+		const size_t smem = sizeof(WarpSmem) * warps;
+		cudaFuncSetAttribute(k_trace8<FMT, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                     (int)(sizeof(WarpSmem) * kWarpsPerBlock));
 		int b = 0;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_nearest<FMT, COUNT>, block,
-		                                              (block / 32) * 1024);
-		cached = b > 0 ? b : 1;
-		cached_block = block;
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT>, 32 * warps, smem);
+		cached[warps] = b > 0 ? b : 1;
 	}
-	return cached;
+	return cached[warps];
 }
 
 template <int FMT, bool COUNT>
-void launch(const TravArgs &a, int block, int sm_count, cudaStream_t st) {
-	const int bps = blocks_per_sm<FMT, COUNT>(block);
-	uint64_t need = (a.n_rays + (uint64_t)block - 1) / block;
-	uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
-	k_nearest<FMT, COUNT><<<(unsigned)grid, block, (block / 32) * 1024, st>>>(a);
+void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
+	const int bps = blocks_per_sm<FMT, COUNT>(warps);
+	const uint64_t warps_needed = (a.n_rays + 31ull) / 32ull;
+	const uint64_t need = (warps_needed + warps - 1) / warps;
+	const uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
+	k_trace8<FMT, COUNT><<<(unsigned)grid, 32 * warps, sizeof(WarpSmem) * warps, st>>>(a);
 }
 
 } // namespace
+
+int traversal_stack_depth() { return kStackDepth; }
 
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
@@ -259,11 +405,14 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 	if (cfg.count)
 		cudaMemsetAsync(d_visits, 0, 2 * sizeof(unsigned long long), st);
 	const uint64_t chunk = 1ull << 31;
-	const int block = (cfg.block >= 32 && cfg.block <= 128 && cfg.block % 32 == 0) ? cfg.block : 128;
+	const int warps = (cfg.block >= 32 && cfg.block <= 32 * kWarpsPerBlock && cfg.block % 32 == 0)
+	                      ? cfg.block / 32
+	                      : kWarpsPerBlock;
 	for (uint64_t s = 0; s < n; s += chunk) {
 		const uint64_t m = std::min(chunk, n - s);
 		TravArgs a;
 		a.tri4 = sc.tri4.as<float4>();
+		a.inv = sc.inv.as<uint32_t>();
 		a.nodes = cfg.format == PRT_NODES_COMPRESSED ? sc.cnodes.p : sc.nodes.p;
 		a.rays = d_rays + 6 * s;
 		a.out = static_cast<uint8_t *>(d_out) + s * lay.rec_size;
@@ -273,7 +422,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.mask = lay.mask;
 		for (int k = 0; k < 8; ++k)
 			a.off[k] = lay.off[k];
-		uintptr_t addr = reinterpret_cast<uintptr_t>(a.out);
+		const uintptr_t addr = reinterpret_cast<uintptr_t>(a.out);
 		a.store_mode = (addr % 16 == 0) ? 0u : ((addr % 4 == 0) ? 1u : 2u);
 		a.counter = d_work;
 		a.err = d_err;
@@ -283,14 +432,14 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 			return e;
 		if (cfg.format == PRT_NODES_COMPRESSED) {
 			if (cfg.count)
-				launch<PRT_NODES_COMPRESSED, true>(a, block, sm_count, st);
+				launch<PRT_NODES_COMPRESSED, true>(a, warps, sm_count, st);
 			else
-				launch<PRT_NODES_COMPRESSED, false>(a, block, sm_count, st);
+				launch<PRT_NODES_COMPRESSED, false>(a, warps, sm_count, st);
 		} else {
 			if (cfg.count)
-				launch<PRT_NODES_FP32, true>(a, block, sm_count, st);
+				launch<PRT_NODES_FP32, true>(a, warps, sm_count, st);
 			else
-				launch<PRT_NODES_FP32, false>(a, block, sm_count, st);
+				launch<PRT_NODES_FP32, false>(a, warps, sm_count, st);
 		}
 		e = cudaGetLastError();
 		if (e != cudaSuccess)

@@ -20,6 +20,9 @@ struct TravConfig {
 	bool count = false;   // accumulate visit counters into d_visits[0..1]
 };
 
+// Levels of the 8-wide tree the traversal stack can hold.
+int traversal_stack_depth();
+
 // Queues one nearest-hit pass over n rays (device memory, 6 floats each) on `st`.
 // d_work: 16 bytes of device scratch (ray counter); d_visits: 2 uint64 counters
 // (node visits, triangle tests), used when cfg.count.
