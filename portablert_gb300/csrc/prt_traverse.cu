@@ -48,6 +48,7 @@ struct TravArgs {
 	const float *rays;
 	uint8_t *out;
 	uint32_t n_tris;
+	uint32_t n_nodes;
 	uint32_t n_rays;
 	uint32_t rec_size;
 	uint32_t mask;
@@ -140,6 +141,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 			int slot = -1;          // group's ray slot (-1: none)
 			RayC r;
 			uint32_t cur_base = 0, cur_inner = 0, cur_pend = 0;
+			uint32_t visits = 0;    // nodes visited by the group's ray (at most n_nodes in a tree)
 			int sp = 0;
 			uint32_t next = 0;      // next slot to hand out (warp-uniform)
 			uint32_t q = 0;         // queued triangles (warp-uniform)
@@ -156,6 +158,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 						cur_inner = 1;
 						cur_pend = 1;
 						sp = 0;
+						visits = 0;
 					} else {
 						slot = -1;
 					}
@@ -179,6 +182,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 					const int cc = __ffs(cur_pend) - 1;
 					node = cur_base + __popc(cur_inner & ((1u << cc) - 1u));
 					cur_pend &= cur_pend - 1u;
+					if (++visits > a.n_nodes || node >= a.n_nodes) {
+						// Only a malformed tree can get here: report it and drop the ray.
+						if (c == 0)
+							atomicOr(a.err, kErrStack);
+						node = 0;
+						cur_pend = 0;
+						sp = 0;
+					}
 					if (COUNT && c == 0)
 						++n_visits;
 				}
@@ -417,6 +428,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.rays = d_rays + 6 * s;
 		a.out = static_cast<uint8_t *>(d_out) + s * lay.rec_size;
 		a.n_tris = (uint32_t)sc.n_tris;
+		a.n_nodes = sc.n_nodes;
 		a.n_rays = (uint32_t)m;
 		a.rec_size = lay.rec_size;
 		a.mask = lay.mask;
