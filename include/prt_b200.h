@@ -104,7 +104,7 @@ int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t 
 int prt_b200_sync(prt_b200_ctx *ctx);
 
 /* Tuning and statistics.  Options (take effect at the next set_tris unless noted):
- *   "leaf_size"    1..8  triangles per leaf of the 8-wide tree (default 4)
+ *   "leaf_size"    1..8  most triangles per leaf of the 8-wide tree (default 1)
  *   "node_format"  PRT_NODES_FP32 or PRT_NODES_COMPRESSED (default FP32; applies to the
  *                  next nearest_hits when both formats have been built)
  *   "block"        threads per block of the traversal kernel (default 128)

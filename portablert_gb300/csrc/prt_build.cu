@@ -474,7 +474,7 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 int build_scene(const float *d_tris, uint64_t n64, int leaf_size, bool compressed, SceneGPU &sc,
                 BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg) {
 	if (n64 > kMaxTris) {
-		msg = "set_tris: at most 268435455 triangles per scene";
+		msg = "set_tris: at most 134217727 triangles per scene";
 		return PRT_ERR_LIMIT;
 	}
 	if (leaf_size < 1 || leaf_size > kMaxLeaf) {

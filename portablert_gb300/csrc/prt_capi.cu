@@ -30,7 +30,7 @@ struct prt_b200_ctx {
 	prt::DevBuf rays_buf, out_buf;
 	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters
 	uint32_t *h_err = nullptr;
-	int leaf_size = 4;
+	int leaf_size = 1;
 	int node_format = PRT_NODES_FP32;
 	int block = 128;
 	bool count = false;
@@ -249,7 +249,7 @@ int prt_b200_set_tris(prt_b200_ctx *ctx, const float *tris9, uint64_t n) {
 	if (!tris9 && n)
 		return fail(ctx, PRT_ERR_ARG, "set_tris: null triangle pointer");
 	if (n > prt::kMaxTris)
-		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 268435455 triangles per scene");
+		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
 	std::lock_guard<std::mutex> lk(ctx->mu);
 	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
 	if (n) {
@@ -266,7 +266,7 @@ int prt_b200_set_tris_dev(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n) {
 	if (!d_tris9 && n)
 		return fail(ctx, PRT_ERR_ARG, "set_tris_dev: null triangle pointer");
 	if (n > prt::kMaxTris)
-		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 268435455 triangles per scene");
+		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
 	std::lock_guard<std::mutex> lk(ctx->mu);
 	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
 	return do_build(ctx, d_tris9, n);

@@ -20,7 +20,11 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kFirstMask = 0x0FFFFFFFu;
 constexpr int kMaxLeaf = 8;
-constexpr uint64_t kMaxTris = (1ull << 28) - 1;
+// Triangles per scene: the traversal packs (ray slot, node or triangle index) into 32
+// bits with 27 bits for the index.
+constexpr uint64_t kMaxTris = (1ull << 27) - 1;
+constexpr uint32_t kIndexBits = 27;
+constexpr uint32_t kIndexMask = (1u << kIndexBits) - 1u;
 
 // Bits of the device error word.
 enum : uint32_t {

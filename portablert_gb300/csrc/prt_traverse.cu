@@ -10,21 +10,21 @@
 // conservative for that set (prt_internal.cuh), so neither the tree's shape nor the
 // visit order changes the answer; ties in t go to the smaller primitive id.
 //
-// Execution (one warp = 4 groups of 8 lanes):
-//  * A warp takes 32 consecutive rays from a global counter; their origin, direction,
-//    reciprocal and best-hit key live in shared memory ("slots").  Groups take slots
-//    one after another until the 32 are done.
-//  * Node step: a group holds one ray; lane c loads child c of the current node (each
-//    field of the 8 children is one 32-byte row, so the group's loads are coalesced)
-//    and runs the slab test.  Ballots give the children hit; inner children of a node
-//    are contiguous (child_base + rank), so the group's stack keeps one 8-byte entry
-//    (child_base, inner bits, pending bits) per tree level in shared memory.
-//  * Leaf triangles that pass the node test are appended to a warp queue; whenever 32
-//    are pending, the 32 lanes test one triangle each with the exact reference test
-//    and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
-//  * When the batch is done the warp recomputes the winning triangle of each slot
-//    (identical arithmetic, so identical t, u, v), writes the 32 records in the caller's
-//    HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
+// Execution: one warp = 4 groups of 8 lanes, with all state for 32 rays in shared
+// memory.
+//  * A warp takes 32 consecutive rays from a global counter ("slots"): origin,
+//    direction, reciprocal and best-hit key per slot live in shared memory.
+//  * Work items (slot, node) sit in a warp-local LIFO pool.  Each step every group
+//    pops one item; lane c loads child c of the node (each field of the 8 children is
+//    one 32-byte row, so a group's loads are coalesced) and runs the slab test.  Hit
+//    inner children are pushed back as items, hit leaf triangles are appended to a
+//    triangle queue, both at positions from one ballot + popc.  Roots of new rays are
+//    pushed whenever fewer than 4 items are left, so the 4 groups stay busy.
+//  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
+//    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
+//  * When the pool and the queue are empty the warp recomputes each slot's winning
+//    triangle (identical arithmetic, identical t, u, v), writes the 32 records in the
+//    caller's HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
 //
 // Algorithmic bytes per ray: 24 (ray) + R (record) + node bytes visited + 48 per
 // triangle tested; the counting variant (COUNT) measures the visits.
@@ -38,8 +38,13 @@ namespace prt {
 namespace {
 
 constexpr int kWarpsPerBlock = 4;
-constexpr int kStackDepth = 32;
-constexpr int kQueueCap = 32 + 4 * 8 * kMaxLeaf; // pending < 32 + one step's worth
+// Pool size: each step pops 4 items and pushes at most 32, so every level of descent
+// leaves at most 28 items behind; with roots admitted only below 4 items, trees up to
+// kMaxDepth levels stay within kPoolCap (a push that would not fit is reported as an
+// error instead of written).
+constexpr int kMaxDepth = 32;
+constexpr int kPoolCap = 960;
+constexpr int kQueueCap = 32 + 32 * kMaxLeaf; // pending < 32 plus one step's worth
 
 struct TravArgs {
 	const float4 *tri4;
@@ -60,13 +65,22 @@ struct TravArgs {
 };
 
 struct WarpSmem {
-	uint2 stack[4][kStackDepth];     // per group: (child_base, inner << 8 | pending)
-	uint2 queue[kQueueCap];          // (slot, triangle position)
-	unsigned long long key[32];      // best (t, primitive id) per slot
-	float ray[32][9];                // origin, direction, reciprocal per slot
+	union {
+		uint32_t pool[kPoolCap];   // (slot << 27) | node, while traversing
+		uint32_t stage[32 * 8];    // output records (32 x 32 B), while writing
+	};
+	uint32_t queue[kQueueCap];     // (slot << 27) | triangle position
+	unsigned long long key[32];    // best (t, primitive id) per slot
+	float ray[32][9];              // origin, direction, reciprocal per slot
 	int kind[32];
-	uint32_t stage[32 * 8];          // output records, 32 x 32 B
 };
+static_assert(kPoolCap >= 32 * 8, "stage aliases the pool");
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+	uint32_t m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
 
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
@@ -76,7 +90,7 @@ __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, floa
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 
-__device__ __forceinline__ RayC slot_ray(const WarpSmem &S, int s) {
+__device__ __forceinline__ RayC slot_ray(const WarpSmem &S, uint32_t s) {
 	RayC r;
 	r.ox = S.ray[s][0];
 	r.oy = S.ray[s][1];
@@ -96,13 +110,14 @@ template <bool COUNT>
 __device__ __forceinline__ void test_queued(const TravArgs &a, WarpSmem &S, uint32_t lo,
                                             uint32_t n, int lane, uint32_t &n_tests) {
 	if ((uint32_t)lane < n) {
-		const uint2 e = S.queue[lo + lane];
-		const RayC r = slot_ray(S, (int)e.x);
-		const float4 *p = a.tri4 + 3 * (size_t)e.y;
+		const uint32_t e = S.queue[lo + lane];
+		const uint32_t slot = e >> kIndexBits;
+		const RayC r = slot_ray(S, slot);
+		const float4 *p = a.tri4 + 3 * (size_t)(e & kIndexMask);
 		const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
 		float t, u, v;
 		if (tri_test(r, A, B, C, t, u, v) && t < INFINITY)
-			atomicMin(&S.key[e.x], hit_key(t, __float_as_uint(A.w)));
+			atomicMin(&S.key[slot], hit_key(t, __float_as_uint(A.w)));
 		if (COUNT)
 			++n_tests;
 	}
@@ -113,7 +128,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
 	const int lane = threadIdx.x & 31, g = lane >> 3, c = lane & 7;
+	const uint32_t lt = lanemask_lt();
 	uint32_t n_visits = 0, n_tests = 0;
+	// A tree is visited at most once per ray; more steps than this means a malformed
+	// tree, which is reported instead of looping.
+	const uint64_t step_limit = 32ull * a.n_nodes + 64ull;
 
 	for (;;) {
 		uint32_t base = 0;
@@ -138,65 +157,42 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 		__syncwarp();
 
 		if (a.n_tris) {
-			int slot = -1;          // group's ray slot (-1: none)
-			RayC r;
-			uint32_t cur_base = 0, cur_inner = 0, cur_pend = 0;
-			uint32_t visits = 0;    // nodes visited by the group's ray (at most n_nodes in a tree)
-			int sp = 0;
-			uint32_t next = 0;      // next slot to hand out (warp-uniform)
-			uint32_t q = 0;         // queued triangles (warp-uniform)
+			uint32_t top = 0;  // items in the pool (warp-uniform)
+			uint32_t q = 0;    // queued triangles (warp-uniform)
+			uint32_t next = 0; // next slot whose root is not yet in the pool
+			uint64_t steps = 0;
 			for (;;) {
-				// Hand the next slots to groups that have no pending work.
-				const bool idle = slot < 0 || (cur_pend == 0 && sp == 0);
-				const uint32_t idle_lead = __ballot_sync(0xFFFFFFFFu, idle && c == 0);
-				if (idle) {
-					const uint32_t s = next + __popc(idle_lead & ((1u << (8 * g)) - 1u));
-					if (s < nb) {
-						slot = (int)s;
-						r = slot_ray(S, slot);
-						cur_base = 0; // the root is node 0: "inner child 0 of a virtual parent"
-						cur_inner = 1;
-						cur_pend = 1;
-						sp = 0;
-						visits = 0;
-					} else {
-						slot = -1;
-					}
+				// Admit new rays while fewer than 4 items are pending.
+				if (top < 4u && next < nb) {
+					const uint32_t add = min(4u - top, nb - next);
+					if ((uint32_t)lane < add)
+						S.pool[top + lane] = (next + lane) << kIndexBits; // root = node 0
+					top += add;
+					next += add;
+					__syncwarp();
 				}
-				next = min(nb, next + __popc(idle_lead));
-				const bool work = slot >= 0;
-				if (!__any_sync(0xFFFFFFFFu, work))
+				if (top == 0u)
 					break;
-
-				// Next node of this group: a pending inner child at the current level,
-				// else the top of the stack.
-				uint32_t node = 0;
-				if (work) {
-					if (cur_pend == 0) {
-						--sp;
-						const uint2 e = S.stack[g][sp];
-						cur_base = e.x;
-						cur_inner = e.y >> 8;
-						cur_pend = e.y & 0xFFu;
-					}
-					const int cc = __ffs(cur_pend) - 1;
-					node = cur_base + __popc(cur_inner & ((1u << cc) - 1u));
-					cur_pend &= cur_pend - 1u;
-					if (++visits > a.n_nodes || node >= a.n_nodes) {
-						// Only a malformed tree can get here: report it and drop the ray.
-						if (c == 0)
-							atomicOr(a.err, kErrStack);
-						node = 0;
-						cur_pend = 0;
-						sp = 0;
-					}
-					if (COUNT && c == 0)
-						++n_visits;
+				if (++steps > step_limit) {
+					if (lane == 0)
+						atomicOr(a.err, kErrStack);
+					break;
 				}
+				const uint32_t take = min(top, 4u);
+				top -= take;
+				const bool work = (uint32_t)g < take;
+				const uint32_t item = work ? S.pool[top + g] : 0u;
+				__syncwarp(); // the pops above are read before the pushes below overwrite them
+				const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
+				RayC r;
+				if (work)
+					r = slot_ray(S, slot);
+				if (COUNT && work && c == 0)
+					++n_visits;
 
 				// Lane c tests child c of `node`.
 				bool hit = false, inner = false;
-				uint32_t leaf_first_tri = 0, leaf_n = 0, child_base = 0;
+				uint32_t child = 0, leaf_n = 0;
 				if (work) {
 					if (FMT == PRT_NODES_FP32) {
 						const Node8 *nd = static_cast<const Node8 *>(a.nodes) + node;
@@ -206,12 +202,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 							hit = box_test(r, __ldg(&nd->lo_x[c]), __ldg(&nd->hi_x[c]),
 							               __ldg(&nd->lo_y[c]), __ldg(&nd->hi_y[c]),
 							               __ldg(&nd->lo_z[c]), __ldg(&nd->hi_z[c]));
-							if (!inner) {
-								leaf_first_tri = leaf_first(ref);
-								leaf_n = leaf_count(ref);
-							} else {
-								child_base = ref; // fixed up below from the first inner child
-							}
+							child = inner ? ref : leaf_first(ref);
+							leaf_n = inner ? 0u : leaf_count(ref);
 						}
 					} else {
 						const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
@@ -234,64 +226,58 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 							const float lz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 32), sz));
 							const float hz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 40), sz));
 							hit = box_test(r, lx, hx, ly, hy, lz, hz);
-							if (!inner) {
-								// first triangle = tri_base + counts of the leaf children before c
+							if (inner) {
+								child = w1.x + __popc(imask & ((1u << c) - 1u));
+							} else {
+								// tri_base + triangle counts of the leaf children before c
 								const uint32_t lo_w = w1.z, hi_w = w1.w;
 								uint32_t before;
 								if (c < 4)
 									before = __dp4a(lo_w & ((1u << (8 * c)) - 1u), 0x01010101u, 0u);
 								else
 									before = __dp4a(lo_w, 0x01010101u, 0u) +
-									         __dp4a(hi_w & ((1u << (8 * (c - 4))) - 1u), 0x01010101u, 0u);
-								leaf_first_tri = w1.y + before;
+									         __dp4a(hi_w & ((1u << (8 * (c - 4))) - 1u), 0x01010101u,
+									                0u);
+								child = w1.y + before;
 								leaf_n = m;
 							}
 						}
-						child_base = w1.x;
-					}
-				}
-				const uint32_t inner_all = __ballot_sync(0xFFFFFFFFu, inner);
-				const uint32_t inner_hit = __ballot_sync(0xFFFFFFFFu, inner && hit);
-				if (FMT == PRT_NODES_FP32) {
-					// child_base = reference of the group's first inner child (rank 0).
-					const uint32_t gi = (inner_all >> (8 * g)) & 0xFFu;
-					const int src = gi ? (8 * g + __ffs(gi) - 1) : lane;
-					child_base = __shfl_sync(0xFFFFFFFFu, child_base, src);
-				}
-				if (work) {
-					// Descend into the hit inner children of `node`; the siblings still
-					// pending at this level go on the stack (one entry per level).
-					const uint32_t gh = (inner_hit >> (8 * g)) & 0xFFu;
-					if (gh) {
-						if (cur_pend) {
-							if (sp < kStackDepth) {
-								if (c == 0)
-									S.stack[g][sp] = make_uint2(cur_base, (cur_inner << 8) | cur_pend);
-								++sp;
-							} else if (c == 0) {
-								atomicOr(a.err, kErrStack);
-							}
-						}
-						cur_base = child_base;
-						cur_inner = (inner_all >> (8 * g)) & 0xFFu;
-						cur_pend = gh;
 					}
 				}
 
-				// Queue the triangles of the leaf children that were hit.
-				const uint32_t cnt = (hit && !inner) ? leaf_n : 0u;
-				uint32_t incl = cnt;
-#pragma unroll
-				for (int o = 1; o < 32; o <<= 1) {
-					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-					if (lane >= o)
-						incl += y;
+				// Push the hit inner children as new items.
+				const bool push = hit && inner;
+				const uint32_t bp = __ballot_sync(0xFFFFFFFFu, push);
+				const uint32_t n_push = __popc(bp);
+				if (top + n_push > (uint32_t)kPoolCap) {
+					if (lane == 0)
+						atomicOr(a.err, kErrStack);
+				} else {
+					if (push)
+						S.pool[top + __popc(bp & lt)] = (slot << kIndexBits) | child;
+					top += n_push;
 				}
-				const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-				const uint32_t pos = q + incl - cnt;
-				for (uint32_t k = 0; k < cnt; ++k)
-					S.queue[pos + k] = make_uint2((uint32_t)slot, leaf_first_tri + k);
-				q += total;
+
+				// Queue the triangles of the hit leaf children.
+				const uint32_t cnt = (hit && !inner) ? leaf_n : 0u;
+				const uint32_t bl = __ballot_sync(0xFFFFFFFFu, cnt != 0u);
+				if (__all_sync(0xFFFFFFFFu, cnt <= 1u)) {
+					if (cnt)
+						S.queue[q + __popc(bl & lt)] = (slot << kIndexBits) | child;
+					q += __popc(bl);
+				} else {
+					uint32_t incl = cnt;
+#pragma unroll
+					for (int o = 1; o < 32; o <<= 1) {
+						const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+						if (lane >= o)
+							incl += y;
+					}
+					const uint32_t pos = q + incl - cnt;
+					for (uint32_t k = 0; k < cnt; ++k)
+						S.queue[pos + k] = (slot << kIndexBits) | (child + k);
+					q += __shfl_sync(0xFFFFFFFFu, incl, 31);
+				}
 				__syncwarp();
 				while (q >= 32u) {
 					q -= 32u;
@@ -407,7 +393,7 @@ void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
 
 } // namespace
 
-int traversal_stack_depth() { return kStackDepth; }
+int traversal_stack_depth() { return kMaxDepth; }
 
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
