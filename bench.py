@@ -320,6 +320,7 @@ def run_gpu(args, world, rank):
     torch.cuda.synchronize()
     b.sync()
     comp_ms = float(sum(s.elapsed_time(e) for s, e in ev2))
+    comp_node_size = b.stat("node_size")
     b.set_option("node_format", 0)
 
     out = {"metric": METRIC, "value": mrays, "unit": "Mrays/s", "n_gpus": world,
@@ -339,7 +340,7 @@ def run_gpu(args, world, rank):
                      "ms_device": build_dev_ms, "nodes": b.stat("n_nodes"),
                      "depth": b.stat("depth")},
            "compressed": {"value": world * n * args.steps / (comp_ms / 1e3) / 1e6,
-                          "unit": "Mrays/s", "node_bytes": 80},
+                          "unit": "Mrays/s", "node_bytes": comp_node_size},
            "clocks": clk}
     if rank == 0 and not args.no_cpu:
         _, cb = cpu_baseline(tris, rays, sample_rays=131_072)

@@ -338,13 +338,16 @@ __global__ void __launch_bounds__(128)
 					ref = make_leaf(dst, cnt);
 				}
 			}
-			nd->lo_x[c] = lo.x;
-			nd->hi_x[c] = hi.x;
-			nd->lo_y[c] = lo.y;
-			nd->hi_y[c] = hi.y;
-			nd->lo_z[c] = lo.z;
-			nd->hi_z[c] = hi.z;
-			nd->ref[c] = ref;
+			Child8 ch;
+			ch.lo_x = lo.x;
+			ch.lo_y = lo.y;
+			ch.lo_z = lo.z;
+			ch.ref = ref;
+			ch.hi_x = hi.x;
+			ch.hi_y = hi.y;
+			ch.hi_z = hi.z;
+			ch.pad = 0u;
+			nd->c[c] = ch;
 		}
 	}
 }
@@ -396,31 +399,47 @@ __global__ void k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes, CN
 	if (i >= n_nodes)
 		return;
 	const Node8 &nd = nodes[i];
-	const float *lo[3] = {nd.lo_x, nd.lo_y, nd.lo_z};
-	const float *hi[3] = {nd.hi_x, nd.hi_y, nd.hi_z};
+	float lo[3][8], hi[3][8];
+	uint32_t ref[8];
+	for (int k = 0; k < 8; ++k) {
+		const Child8 &ch = nd.c[k];
+		lo[0][k] = ch.lo_x;
+		lo[1][k] = ch.lo_y;
+		lo[2][k] = ch.lo_z;
+		hi[0][k] = ch.hi_x;
+		hi[1][k] = ch.hi_y;
+		hi[2][k] = ch.hi_z;
+		ref[k] = ch.ref;
+	}
 	CNode8 c;
 	memset(&c, 0, sizeof c);
 	uint32_t child_base = kNone, tri_base = kNone;
 	for (int k = 0; k < 8; ++k) {
-		uint32_t r = nd.ref[k];
+		const uint32_t r = ref[k];
 		if (r == kNone)
 			continue;
-		if (r & kLeafBit) {
-			c.meta[k] = (uint8_t)leaf_count(r);
+		if (r & kLeafBit)
 			tri_base = min(tri_base, leaf_first(r));
-		} else {
+		else {
 			c.imask |= (uint8_t)(1u << k);
 			child_base = min(child_base, r);
 		}
 	}
 	c.child_base = child_base == kNone ? 0u : child_base;
 	c.tri_base = tri_base == kNone ? 0u : tri_base;
+	for (int k = 0; k < 8; ++k) {
+		const uint32_t r = ref[k];
+		if (r != kNone && (r & kLeafBit)) {
+			c.c[k].count = (uint8_t)leaf_count(r);
+			c.c[k].first = (uint8_t)(leaf_first(r) - c.tri_base);
+		}
+	}
 	float org[3];
 	uint8_t ex[3];
 	for (int a = 0; a < 3; ++a) {
 		float mn = INFINITY, mx = -INFINITY;
 		for (int k = 0; k < 8; ++k) {
-			if (nd.ref[k] == kNone)
+			if (ref[k] == kNone)
 				continue;
 			mn = fminf(mn, lo[a][k]);
 			mx = fmaxf(mx, hi[a][k]);
@@ -449,10 +468,11 @@ __global__ void k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes, CN
 	for (int a = 0; a < 3; ++a) {
 		float s = cscale(ex[a]);
 		for (int k = 0; k < 8; ++k) {
-			if (nd.ref[k] == kNone)
+			if (ref[k] == kNone)
 				continue;
-			c.q[2 * a][k] = (uint8_t)quant_lo(org[a], s, lo[a][k]);
-			c.q[2 * a + 1][k] = (uint8_t)quant_hi(org[a], s, hi[a][k]);
+			uint8_t *qk = &c.c[k].qlo_x;
+			qk[2 * a] = (uint8_t)quant_lo(org[a], s, lo[a][k]);
+			qk[2 * a + 1] = (uint8_t)quant_hi(org[a], s, hi[a][k]);
 		}
 	}
 	cn[i] = c;

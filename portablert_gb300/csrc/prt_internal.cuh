@@ -33,29 +33,43 @@ enum : uint32_t {
 	kErrCollapse = 4u, // 8-wide collapse ran out of node slots
 };
 
-struct alignas(16) Node8 {
-	float lo_x[8], hi_x[8], lo_y[8], hi_y[8], lo_z[8], hi_z[8];
-	uint32_t ref[8];
+// One child of an 8-wide FP32 node: its box and its reference, 32 B, so the lane that
+// tests child c reads it with two 16-byte loads and a node's 8 children are 256
+// contiguous bytes.
+struct alignas(16) Child8 {
+	float lo_x, lo_y, lo_z;
+	uint32_t ref;
+	float hi_x, hi_y, hi_z;
+	uint32_t pad;
 };
-static_assert(sizeof(Node8) == 224, "Node8 layout");
+struct alignas(16) Node8 {
+	Child8 c[8];
+};
+static_assert(sizeof(Node8) == 256, "Node8 layout");
 
-// Compressed 8-wide node (80 B), the same tree as Node8.  Child box k, per axis:
-//   lo = origin + q[2a][k] * 2^(e-127),  hi = origin + q[2a+1][k] * 2^(e-127)
-// evaluated in FP32 by cdecode(); the builder chooses each q so that the decoded box
-// contains the child's FP32 box (rounded outward), so every box test stays
-// conservative.  Child k is an inner node when bit k of imask is set, at index
-// child_base + (number of inner children before k); otherwise, when meta[k] > 0, it is
-// a leaf of meta[k] triangles starting at tri_base + (sum of meta[j] for j < k).
+// Compressed 8-wide node (96 B = 37.5 % of Node8), the same tree as Node8.  Child box
+// k, per axis a: lo = origin_a + q_lo * 2^(e_a - 127), hi = origin_a + q_hi * 2^(e_a - 127),
+// evaluated in FP32 exactly as the traversal does (cdec); the builder chooses each q so
+// that the decoded box contains the child's FP32 box (rounded outward), which keeps
+// every box test conservative.  Child k is an inner node when bit k of imask is set, at
+// index child_base + (number of inner children before k); otherwise, when count > 0,
+// a leaf of `count` triangles starting at tri_base + first.
+struct alignas(8) CChild8 {
+	uint8_t qlo_x, qhi_x, qlo_y, qhi_y, qlo_z, qhi_z;
+	uint8_t count; // leaf triangles (0 = inner child or empty slot)
+	uint8_t first; // leaf: first triangle relative to tri_base
+};
 struct alignas(16) CNode8 {
 	float ox, oy, oz;       // frame origin (the node's lower corner)
 	uint8_t ex, ey, ez;     // scale exponents, IEEE-biased
 	uint8_t imask;          // inner-node children
 	uint32_t child_base;    // first inner child
 	uint32_t tri_base;      // first triangle of the node's leaf children
-	uint8_t meta[8];        // leaf triangle counts (0 = inner or empty)
-	uint8_t q[6][8];        // lo_x, hi_x, lo_y, hi_y, lo_z, hi_z
+	uint32_t pad[2];
+	CChild8 c[8];
 };
-static_assert(sizeof(CNode8) == 80, "CNode8 layout");
+static_assert(sizeof(CChild8) == 8, "CChild8 layout");
+static_assert(sizeof(CNode8) == 96, "CNode8 layout");
 
 // Decodes one quantised bound.  2^(e-127) * q is exact (q < 256, e in [1, 254]); the
 // sum is rounded once, and the builder verified the rounded value, so this exact

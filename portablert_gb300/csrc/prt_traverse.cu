@@ -195,50 +195,41 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 				uint32_t child = 0, leaf_n = 0;
 				if (work) {
 					if (FMT == PRT_NODES_FP32) {
-						const Node8 *nd = static_cast<const Node8 *>(a.nodes) + node;
-						const uint32_t ref = __ldg(&nd->ref[c]);
+						const float4 *cp = reinterpret_cast<const float4 *>(
+						    &(static_cast<const Node8 *>(a.nodes) + node)->c[c]);
+						const float4 lo = __ldg(cp), hi = __ldg(cp + 1);
+						const uint32_t ref = __float_as_uint(lo.w);
 						if (ref != kNone) {
 							inner = !ref_is_leaf(ref);
-							hit = box_test(r, __ldg(&nd->lo_x[c]), __ldg(&nd->hi_x[c]),
-							               __ldg(&nd->lo_y[c]), __ldg(&nd->hi_y[c]),
-							               __ldg(&nd->lo_z[c]), __ldg(&nd->hi_z[c]));
+							hit = box_test(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
 							child = inner ? ref : leaf_first(ref);
 							leaf_n = inner ? 0u : leaf_count(ref);
 						}
 					} else {
 						const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
 						const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
-						const uint4 w1 = __ldg(reinterpret_cast<const uint4 *>(cn) + 1);
+						const uint2 w1 = __ldg(reinterpret_cast<const uint2 *>(cn) + 2);
+						const uint2 ck = __ldg(reinterpret_cast<const uint2 *>(&cn->c[c]));
 						const uint32_t imask = byte_of(w0.w, 3);
-						const uint32_t m = byte_of(c < 4 ? w1.z : w1.w, c & 3);
+						const uint32_t m = byte_of(ck.y, 2);
 						inner = (imask >> c) & 1u;
 						if (inner || m) {
-							const uint8_t *qb = reinterpret_cast<const uint8_t *>(cn) + 32 + c;
 							const float sx = cscale((uint8_t)byte_of(w0.w, 0));
 							const float sy = cscale((uint8_t)byte_of(w0.w, 1));
 							const float sz = cscale((uint8_t)byte_of(w0.w, 2));
 							const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
 							            oz = __uint_as_float(w0.z);
-							const float lx = __fadd_rn(ox, __fmul_rn((float)__ldg(qb + 0), sx));
-							const float hx = __fadd_rn(ox, __fmul_rn((float)__ldg(qb + 8), sx));
-							const float ly = __fadd_rn(oy, __fmul_rn((float)__ldg(qb + 16), sy));
-							const float hy = __fadd_rn(oy, __fmul_rn((float)__ldg(qb + 24), sy));
-							const float lz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 32), sz));
-							const float hz = __fadd_rn(oz, __fmul_rn((float)__ldg(qb + 40), sz));
+							const float lx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 0), sx));
+							const float hx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 1), sx));
+							const float ly = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 2), sy));
+							const float hy = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 3), sy));
+							const float lz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 0), sz));
+							const float hz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 1), sz));
 							hit = box_test(r, lx, hx, ly, hy, lz, hz);
 							if (inner) {
 								child = w1.x + __popc(imask & ((1u << c) - 1u));
 							} else {
-								// tri_base + triangle counts of the leaf children before c
-								const uint32_t lo_w = w1.z, hi_w = w1.w;
-								uint32_t before;
-								if (c < 4)
-									before = __dp4a(lo_w & ((1u << (8 * c)) - 1u), 0x01010101u, 0u);
-								else
-									before = __dp4a(lo_w, 0x01010101u, 0u) +
-									         __dp4a(hi_w & ((1u << (8 * (c - 4))) - 1u), 0x01010101u,
-									                0u);
-								child = w1.y + before;
+								child = w1.y + byte_of(ck.y, 3);
 								leaf_n = m;
 							}
 						}
