@@ -10,21 +10,24 @@
 // conservative for that set (prt_internal.cuh), so neither the tree's shape nor the
 // visit order changes the answer; ties in t go to the smaller primitive id.
 //
-// Execution: one warp = 4 groups of 8 lanes, with all state for 32 rays in shared
-// memory.
+// Execution: one warp = 8 groups of 4 lanes; all state for 32 rays is in shared memory.
 //  * A warp takes 32 consecutive rays from a global counter ("slots"): origin,
 //    direction, reciprocal and best-hit key per slot live in shared memory.
 //  * Work items (slot, node) sit in a warp-local LIFO pool.  Each step every group
-//    pops one item; lane c loads child c of the node (each field of the 8 children is
-//    one 32-byte row, so a group's loads are coalesced) and runs the slab test.  Hit
-//    inner children are pushed back as items, hit leaf triangles are appended to a
-//    triangle queue, both at positions from one ballot + popc.  Roots of new rays are
-//    pushed whenever fewer than 4 items are left, so the 4 groups stay busy.
+//    pops one item and each of its 4 lanes loads and slab-tests 2 of the node's 8
+//    children (each child is one 32-byte record, so a group reads the node's 256 bytes
+//    in one coalesced sweep).  Hit inner children are pushed back as items and hit
+//    leaf triangles are appended to a triangle queue, at positions from ballots and
+//    popc.  Roots of new rays are admitted whenever fewer than 8 items are left.
 //  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
 //    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
 //  * When the pool and the queue are empty the warp recomputes each slot's winning
 //    triangle (identical arithmetic, identical t, u, v), writes the 32 records in the
 //    caller's HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
+//  * The pool holds at most 7 K (D - 1) + K items for K = 8 items per step and a tree of
+//    depth D (each step's pushes leave at most 7 K items behind per level); it is sized
+//    per launch as 7 K (D - 1) + 2 K, and a push that would not fit is reported as an
+//    error instead of written.
 //
 // Algorithmic bytes per ray: 24 (ray) + R (record) + node bytes visited + 48 per
 // triangle tested; the counting variant (COUNT) measures the visits.
@@ -38,13 +41,10 @@ namespace prt {
 namespace {
 
 constexpr int kWarpsPerBlock = 4;
-// Pool size: each step pops 4 items and pushes at most 32, so every level of descent
-// leaves at most 28 items behind; with roots admitted only below 4 items, trees up to
-// kMaxDepth levels stay within kPoolCap (a push that would not fit is reported as an
-// error instead of written).
+constexpr int kLanesPerNode = 4;
+constexpr int kItems = 32 / kLanesPerNode;       // items per step (K)
+constexpr int kChildPerLane = 8 / kLanesPerNode;
 constexpr int kMaxDepth = 32;
-constexpr int kPoolCap = 960;
-constexpr int kQueueCap = 32 + 32 * kMaxLeaf; // pending < 32 plus one step's worth
 
 struct TravArgs {
 	const float4 *tri4;
@@ -59,22 +59,24 @@ struct TravArgs {
 	uint32_t mask;
 	uint32_t off[8];
 	uint32_t store_mode; // 0: 16-B stores, 1: 4-B stores, 2: byte stores
+	uint32_t pool_cap;   // entries of the pool (>= 256, it also holds the staged records)
+	uint32_t queue_cap;  // entries of the triangle queue
+	uint32_t warp_bytes; // shared memory per warp
 	uint32_t *counter;
 	uint32_t *err;
 	unsigned long long *visits;
 };
 
-struct WarpSmem {
-	union {
-		uint32_t pool[kPoolCap];   // (slot << 27) | node, while traversing
-		uint32_t stage[32 * 8];    // output records (32 x 32 B), while writing
-	};
-	uint32_t queue[kQueueCap];     // (slot << 27) | triangle position
-	unsigned long long key[32];    // best (t, primitive id) per slot
-	float ray[32][9];              // origin, direction, reciprocal per slot
+// Per-warp shared memory: fixed part, then the queue and the pool (sizes per launch).
+struct WarpFixed {
+	unsigned long long key[32]; // best (t, primitive id) per slot
+	float ray[32][9];           // origin, direction, reciprocal per slot
 	int kind[32];
 };
-static_assert(kPoolCap >= 32 * 8, "stage aliases the pool");
+
+__host__ __device__ inline uint32_t warp_smem_bytes(uint32_t pool_cap, uint32_t queue_cap) {
+	return (uint32_t)sizeof(WarpFixed) + 4u * (queue_cap + pool_cap);
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
 	uint32_t m;
@@ -90,7 +92,7 @@ __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, floa
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 
-__device__ __forceinline__ RayC slot_ray(const WarpSmem &S, uint32_t s) {
+__device__ __forceinline__ RayC slot_ray(const WarpFixed &S, uint32_t s) {
 	RayC r;
 	r.ox = S.ray[s][0];
 	r.oy = S.ray[s][1];
@@ -107,10 +109,11 @@ __device__ __forceinline__ RayC slot_ray(const WarpSmem &S, uint32_t s) {
 
 // Tests queue entries [lo, lo + n) (n <= 32), one per lane.
 template <bool COUNT>
-__device__ __forceinline__ void test_queued(const TravArgs &a, WarpSmem &S, uint32_t lo,
-                                            uint32_t n, int lane, uint32_t &n_tests) {
+__device__ __forceinline__ void test_queued(const TravArgs &a, WarpFixed &S,
+                                            const uint32_t *queue, uint32_t lo, uint32_t n,
+                                            int lane, uint32_t &n_tests) {
 	if ((uint32_t)lane < n) {
-		const uint32_t e = S.queue[lo + lane];
+		const uint32_t e = queue[lo + lane];
 		const uint32_t slot = e >> kIndexBits;
 		const RayC r = slot_ray(S, slot);
 		const float4 *p = a.tri4 + 3 * (size_t)(e & kIndexMask);
@@ -123,11 +126,65 @@ __device__ __forceinline__ void test_queued(const TravArgs &a, WarpSmem &S, uint
 	}
 }
 
+// Child `k` of `node`: slab test and what it refers to.
+template <int FMT>
+__device__ __forceinline__ void test_child(const TravArgs &a, const RayC &r, uint32_t node,
+                                           int k, bool &hit, bool &inner, uint32_t &child,
+                                           uint32_t &leaf_n) {
+	hit = false;
+	inner = false;
+	child = 0;
+	leaf_n = 0;
+	if (FMT == PRT_NODES_FP32) {
+		const float4 *cp =
+		    reinterpret_cast<const float4 *>(&(static_cast<const Node8 *>(a.nodes) + node)->c[k]);
+		const float4 lo = __ldg(cp), hi = __ldg(cp + 1);
+		const uint32_t ref = __float_as_uint(lo.w);
+		if (ref != kNone) {
+			inner = !ref_is_leaf(ref);
+			hit = box_test(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+			child = inner ? ref : leaf_first(ref);
+			leaf_n = inner ? 0u : leaf_count(ref);
+		}
+	} else {
+		const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
+		const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
+		const uint2 w1 = __ldg(reinterpret_cast<const uint2 *>(cn) + 2);
+		const uint2 ck = __ldg(reinterpret_cast<const uint2 *>(&cn->c[k]));
+		const uint32_t imask = byte_of(w0.w, 3);
+		const uint32_t m = byte_of(ck.y, 2);
+		inner = (imask >> k) & 1u;
+		if (inner || m) {
+			const float sx = cscale((uint8_t)byte_of(w0.w, 0));
+			const float sy = cscale((uint8_t)byte_of(w0.w, 1));
+			const float sz = cscale((uint8_t)byte_of(w0.w, 2));
+			const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
+			            oz = __uint_as_float(w0.z);
+			const float lx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 0), sx));
+			const float hx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 1), sx));
+			const float ly = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 2), sy));
+			const float hy = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 3), sy));
+			const float lz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 0), sz));
+			const float hz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 1), sz));
+			hit = box_test(r, lx, hx, ly, hy, lz, hz);
+			if (inner) {
+				child = w1.x + __popc(imask & ((1u << k) - 1u));
+			} else {
+				child = w1.y + byte_of(ck.y, 3);
+				leaf_n = m;
+			}
+		}
+	}
+}
+
 template <int FMT, bool COUNT>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
-	WarpSmem &S = reinterpret_cast<WarpSmem *>(smem_raw)[threadIdx.x >> 5];
-	const int lane = threadIdx.x & 31, g = lane >> 3, c = lane & 7;
+	unsigned char *wbase = smem_raw + (size_t)(threadIdx.x >> 5) * a.warp_bytes;
+	WarpFixed &S = *reinterpret_cast<WarpFixed *>(wbase);
+	uint32_t *queue = reinterpret_cast<uint32_t *>(wbase + sizeof(WarpFixed));
+	uint32_t *pool = queue + a.queue_cap; // also the staging area of the output records
+	const int lane = threadIdx.x & 31, g = lane / kLanesPerNode, s = lane % kLanesPerNode;
 	const uint32_t lt = lanemask_lt();
 	uint32_t n_visits = 0, n_tests = 0;
 	// A tree is visited at most once per ray; more steps than this means a malformed
@@ -145,7 +202,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 
 		if ((uint32_t)lane < nb) {
 			const float2 *rp = reinterpret_cast<const float2 *>(a.rays + 6 * (size_t)(base + lane));
-			const float2 p0 = __ldg(rp), p1 = __ldg(rp + 1), p2 = __ldg(rp + 2);
+			const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
 			const RayC r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
 			float *sr = S.ray[lane];
 			sr[0] = r.ox; sr[1] = r.oy; sr[2] = r.oz;
@@ -162,11 +219,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 			uint32_t next = 0; // next slot whose root is not yet in the pool
 			uint64_t steps = 0;
 			for (;;) {
-				// Admit new rays while fewer than 4 items are pending.
-				if (top < 4u && next < nb) {
-					const uint32_t add = min(4u - top, nb - next);
+				// Admit new rays while fewer than K items are pending.
+				if (top < (uint32_t)kItems && next < nb) {
+					const uint32_t add = min((uint32_t)kItems - top, nb - next);
 					if ((uint32_t)lane < add)
-						S.pool[top + lane] = (next + lane) << kIndexBits; // root = node 0
+						pool[top + lane] = (next + lane) << kIndexBits; // root = node 0
 					top += add;
 					next += add;
 					__syncwarp();
@@ -178,117 +235,112 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 						atomicOr(a.err, kErrStack);
 					break;
 				}
-				const uint32_t take = min(top, 4u);
+				const uint32_t take = min(top, (uint32_t)kItems);
 				top -= take;
 				const bool work = (uint32_t)g < take;
-				const uint32_t item = work ? S.pool[top + g] : 0u;
+				const uint32_t item = work ? pool[top + g] : 0u;
 				__syncwarp(); // the pops above are read before the pushes below overwrite them
 				const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
 				RayC r;
 				if (work)
 					r = slot_ray(S, slot);
-				if (COUNT && work && c == 0)
+				if (COUNT && work && s == 0)
 					++n_visits;
 
-				// Lane c tests child c of `node`.
-				bool hit = false, inner = false;
-				uint32_t child = 0, leaf_n = 0;
-				if (work) {
-					if (FMT == PRT_NODES_FP32) {
-						const float4 *cp = reinterpret_cast<const float4 *>(
-						    &(static_cast<const Node8 *>(a.nodes) + node)->c[c]);
-						const float4 lo = __ldg(cp), hi = __ldg(cp + 1);
-						const uint32_t ref = __float_as_uint(lo.w);
-						if (ref != kNone) {
-							inner = !ref_is_leaf(ref);
-							hit = box_test(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-							child = inner ? ref : leaf_first(ref);
-							leaf_n = inner ? 0u : leaf_count(ref);
-						}
-					} else {
-						const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
-						const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
-						const uint2 w1 = __ldg(reinterpret_cast<const uint2 *>(cn) + 2);
-						const uint2 ck = __ldg(reinterpret_cast<const uint2 *>(&cn->c[c]));
-						const uint32_t imask = byte_of(w0.w, 3);
-						const uint32_t m = byte_of(ck.y, 2);
-						inner = (imask >> c) & 1u;
-						if (inner || m) {
-							const float sx = cscale((uint8_t)byte_of(w0.w, 0));
-							const float sy = cscale((uint8_t)byte_of(w0.w, 1));
-							const float sz = cscale((uint8_t)byte_of(w0.w, 2));
-							const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
-							            oz = __uint_as_float(w0.z);
-							const float lx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 0), sx));
-							const float hx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 1), sx));
-							const float ly = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 2), sy));
-							const float hy = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 3), sy));
-							const float lz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 0), sz));
-							const float hz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 1), sz));
-							hit = box_test(r, lx, hx, ly, hy, lz, hz);
-							if (inner) {
-								child = w1.x + __popc(imask & ((1u << c) - 1u));
-							} else {
-								child = w1.y + byte_of(ck.y, 3);
-								leaf_n = m;
-							}
-						}
-					}
+				bool hit[kChildPerLane], inner[kChildPerLane];
+				uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j) {
+					hit[j] = false;
+					inner[j] = false;
+					child[j] = 0;
+					leaf_n[j] = 0;
+					if (work)
+						test_child<FMT>(a, r, node, s * kChildPerLane + j, hit[j], inner[j],
+						                child[j], leaf_n[j]);
 				}
 
-				// Push the hit inner children as new items.
-				const bool push = hit && inner;
-				const uint32_t bp = __ballot_sync(0xFFFFFFFFu, push);
-				const uint32_t n_push = __popc(bp);
-				if (top + n_push > (uint32_t)kPoolCap) {
+				// Push the hit inner children as new items (lane order, then child order).
+				uint32_t n_push = 0, before = 0;
+				bool push[kChildPerLane];
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j) {
+					push[j] = hit[j] && inner[j];
+					const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
+					n_push += __popc(b);
+					before += __popc(b & lt);
+				}
+				if (top + n_push > a.pool_cap) {
 					if (lane == 0)
 						atomicOr(a.err, kErrStack);
 				} else {
-					if (push)
-						S.pool[top + __popc(bp & lt)] = (slot << kIndexBits) | child;
+					uint32_t pos = top + before;
+#pragma unroll
+					for (int j = 0; j < kChildPerLane; ++j)
+						if (push[j])
+							pool[pos++] = (slot << kIndexBits) | child[j];
 					top += n_push;
 				}
 
 				// Queue the triangles of the hit leaf children.
-				const uint32_t cnt = (hit && !inner) ? leaf_n : 0u;
-				const uint32_t bl = __ballot_sync(0xFFFFFFFFu, cnt != 0u);
-				if (__all_sync(0xFFFFFFFFu, cnt <= 1u)) {
-					if (cnt)
-						S.queue[q + __popc(bl & lt)] = (slot << kIndexBits) | child;
-					q += __popc(bl);
+				uint32_t cnt[kChildPerLane], all_cnt = 0;
+				bool single = true;
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j) {
+					cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
+					all_cnt += cnt[j];
+					single = single && cnt[j] <= 1u;
+				}
+				if (__all_sync(0xFFFFFFFFu, single)) {
+					uint32_t n_add = 0, pre = 0;
+#pragma unroll
+					for (int j = 0; j < kChildPerLane; ++j) {
+						const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
+						n_add += __popc(b);
+						pre += __popc(b & lt);
+					}
+					uint32_t pos = q + pre;
+#pragma unroll
+					for (int j = 0; j < kChildPerLane; ++j)
+						if (cnt[j])
+							queue[pos++] = (slot << kIndexBits) | child[j];
+					q += n_add;
 				} else {
-					uint32_t incl = cnt;
+					uint32_t incl = all_cnt;
 #pragma unroll
 					for (int o = 1; o < 32; o <<= 1) {
 						const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
 						if (lane >= o)
 							incl += y;
 					}
-					const uint32_t pos = q + incl - cnt;
-					for (uint32_t k = 0; k < cnt; ++k)
-						S.queue[pos + k] = (slot << kIndexBits) | (child + k);
+					uint32_t pos = q + incl - all_cnt;
+#pragma unroll
+					for (int j = 0; j < kChildPerLane; ++j)
+						for (uint32_t k = 0; k < cnt[j]; ++k)
+							queue[pos++] = (slot << kIndexBits) | (child[j] + k);
 					q += __shfl_sync(0xFFFFFFFFu, incl, 31);
 				}
 				__syncwarp();
 				while (q >= 32u) {
 					q -= 32u;
-					test_queued<COUNT>(a, S, q, 32u, lane, n_tests);
+					test_queued<COUNT>(a, S, queue, q, 32u, lane, n_tests);
 					__syncwarp();
 				}
 			}
 			while (q > 0u) {
 				const uint32_t n = min(q, 32u);
 				q -= n;
-				test_queued<COUNT>(a, S, q, n, lane, n_tests);
+				test_queued<COUNT>(a, S, queue, q, n, lane, n_tests);
 				__syncwarp();
 			}
 		}
 		__syncwarp();
 
 		// Finalise: recompute the winning triangle of each slot and stage the record.
+		uint32_t *stage = pool;
 		const uint32_t rw = a.rec_size >> 2;
 		for (uint32_t w = 0; w < rw; ++w)
-			S.stage[lane * rw + w] = 0u;
+			stage[lane * rw + w] = 0u;
 		__syncwarp();
 		if ((uint32_t)lane < nb) {
 			const RayC r = slot_ray(S, lane);
@@ -306,7 +358,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 					best.pid = pid;
 				}
 			}
-			uint8_t *rb = reinterpret_cast<uint8_t *>(S.stage) + lane * a.rec_size;
+			uint8_t *rb = reinterpret_cast<uint8_t *>(stage) + lane * a.rec_size;
 			if (a.mask & PRT_FIELD_UV) {
 				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_U]) = best.u;
 				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_V]) = best.v;
@@ -332,15 +384,15 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 		const uint32_t bytes = nb * a.rec_size;
 		if (a.store_mode == 0 && nb == 32u) {
 			uint4 *d4 = reinterpret_cast<uint4 *>(dst);
-			const uint4 *s4 = reinterpret_cast<const uint4 *>(S.stage);
+			const uint4 *s4 = reinterpret_cast<const uint4 *>(stage);
 			for (uint32_t k = lane; k < bytes / 16u; k += 32u)
-				d4[k] = s4[k];
+				__stcs(d4 + k, s4[k]);
 		} else if (a.store_mode <= 1) {
 			uint32_t *d1 = reinterpret_cast<uint32_t *>(dst);
 			for (uint32_t k = lane; k < bytes / 4u; k += 32u)
-				d1[k] = S.stage[k];
+				d1[k] = stage[k];
 		} else {
-			const uint8_t *sb = reinterpret_cast<const uint8_t *>(S.stage);
+			const uint8_t *sb = reinterpret_cast<const uint8_t *>(stage);
 			for (uint32_t k = lane; k < bytes; k += 32u)
 				dst[k] = sb[k];
 		}
@@ -359,27 +411,31 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 	}
 }
 
-// Resident blocks per SM for a block of `warps` warps (cached per block size).
-template <int FMT, bool COUNT> int blocks_per_sm(int warps) {
-	static int cached[kWarpsPerBlock + 1] = {0};
-	if (!cached[warps]) {
-		const size_t smem = sizeof(WarpSmem) * warps;
+// Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each.
+template <int FMT, bool COUNT> int blocks_per_sm(int warps, uint32_t warp_bytes) {
+	static int cached_warps = -1;
+	static uint32_t cached_bytes = 0;
+	static int cached = 0;
+	if (cached_warps != warps || cached_bytes != warp_bytes) {
+		const size_t smem = (size_t)warp_bytes * warps;
 		cudaFuncSetAttribute(k_trace8<FMT, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                     (int)(sizeof(WarpSmem) * kWarpsPerBlock));
+		                     (int)smem);
 		int b = 0;
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT>, 32 * warps, smem);
-		cached[warps] = b > 0 ? b : 1;
+		cached = b > 0 ? b : 1;
+		cached_warps = warps;
+		cached_bytes = warp_bytes;
 	}
-	return cached[warps];
+	return cached;
 }
 
 template <int FMT, bool COUNT>
 void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	const int bps = blocks_per_sm<FMT, COUNT>(warps);
+	const int bps = blocks_per_sm<FMT, COUNT>(warps, a.warp_bytes);
 	const uint64_t warps_needed = (a.n_rays + 31ull) / 32ull;
 	const uint64_t need = (warps_needed + warps - 1) / warps;
 	const uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
-	k_trace8<FMT, COUNT><<<(unsigned)grid, 32 * warps, sizeof(WarpSmem) * warps, st>>>(a);
+	k_trace8<FMT, COUNT><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(a);
 }
 
 } // namespace
@@ -396,6 +452,10 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 	const int warps = (cfg.block >= 32 && cfg.block <= 32 * kWarpsPerBlock && cfg.block % 32 == 0)
 	                      ? cfg.block / 32
 	                      : kWarpsPerBlock;
+	const uint32_t depth = std::max<uint32_t>(sc.depth, 1u);
+	const uint32_t pool_cap =
+	    std::max<uint32_t>(256u, 7u * kItems * (depth - 1u) + 2u * kItems);
+	const uint32_t queue_cap = 32u + (uint32_t)kItems * 8u * (uint32_t)std::max(sc.leaf_size, 1);
 	for (uint64_t s = 0; s < n; s += chunk) {
 		const uint64_t m = std::min(chunk, n - s);
 		TravArgs a;
@@ -413,6 +473,9 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 			a.off[k] = lay.off[k];
 		const uintptr_t addr = reinterpret_cast<uintptr_t>(a.out);
 		a.store_mode = (addr % 16 == 0) ? 0u : ((addr % 4 == 0) ? 1u : 2u);
+		a.pool_cap = pool_cap;
+		a.queue_cap = queue_cap;
+		a.warp_bytes = (warp_smem_bytes(pool_cap, queue_cap) + 15u) & ~15u;
 		a.counter = d_work;
 		a.err = d_err;
 		a.visits = d_visits;
