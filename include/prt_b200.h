@@ -103,6 +103,22 @@ int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t 
 /* Waits for the context's queued work and reports errors the kernels flagged. */
 int prt_b200_sync(prt_b200_ctx *ctx);
 
+/* No counterpart in the reference.  prt_b200_nearest_hits for programs that must not
+ * allocate device memory once running (for example a renderer that reserves its memory
+ * at start-up and forbids allocation in its frame loop: cudaMalloc can synchronise the
+ * device and can fail under a fixed budget).  Same arguments and results as
+ * prt_b200_nearest_hits, but the call allocates nothing: rays, records, the ray counter
+ * and the error word are staged in one fixed device array of the library (3.5 MiB on
+ * each device that loads it, kept until the process exits).  At most 65536 rays per
+ * call; more returns PRT_ERR_LIMIT.  The first call on a device looks the array's
+ * address up (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array: they are synchronous and serialised by a process-wide
+ * lock; GPU work of two calls that overlapped would race.  The context and the scene
+ * must already exist (prt_b200_create, prt_b200_set_tris allocate). */
+int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *rays6, uint64_t n,
+                                  uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                                  void *out_host);
+
 /* Tuning and statistics.  Options (take effect at the next set_tris unless noted):
  *   "leaf_size"    1..8  most triangles per leaf of the 8-wide tree (default 1)
  *   "node_format"  PRT_NODES_FP32 or PRT_NODES_COMPRESSED (default FP32; applies to the

@@ -17,7 +17,7 @@ EXPORTS = (
     "prt_b200_available", "prt_b200_create", "prt_b200_destroy", "prt_b200_last_error",
     "prt_b200_device_name", "prt_b200_set_tris", "prt_b200_set_tris_dev",
     "prt_b200_nearest_hits", "prt_b200_nearest_hits_dev", "prt_b200_sync",
-    "prt_b200_set_option", "prt_b200_get_stat",
+    "prt_b200_set_option", "prt_b200_get_stat", "prt_b200_nearest_hits_noalloc",
 )
 
 PRT_OK = 0
@@ -58,6 +58,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_nearest_hits_dev.argtypes = [vp, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp, vp]
     L.prt_b200_sync.restype = c_int
     L.prt_b200_sync.argtypes = [vp]
+    L.prt_b200_nearest_hits_noalloc.restype = c_int
+    L.prt_b200_nearest_hits_noalloc.argtypes = [vp, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp]
     L.prt_b200_set_option.restype = c_int
     L.prt_b200_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
     L.prt_b200_get_stat.restype = c_int

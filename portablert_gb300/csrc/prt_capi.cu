@@ -416,3 +416,112 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
 }
 
 } // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Nearest hits without any device allocation.
+//
+// Who needs it: programs that must not allocate device memory once they are running,
+// e.g. a renderer that reserves its whole memory budget at start-up and forbids
+// allocation inside its frame loop, because cudaMalloc can synchronise the device and
+// can fail when the budget is fixed.  prt_b200_nearest_hits grows its device buffers on
+// demand; this variant instead stages rays and records, and keeps the traversal's ray
+// counter and error word, in one file-scope device array of fixed size, so a call never
+// allocates.  The context and the scene are still created and built beforehand (at
+// start-up, where allocation is allowed).
+//
+// The array is kNoallocBytes (3.5 MiB) on every device that loads the library, held
+// until the process exits, and limits one call to kNoallocMaxRays rays.  Every call
+// shares it and it keeps the last call's contents: each call clears the counter, the
+// error word and the visit counters it uses.  Calls whose GPU work overlaps would race
+// on the array; calls are synchronous and serialised by a process-wide mutex, so this
+// only matters if the array is reached some other way.
+// ---------------------------------------------------------------------------------------
+namespace {
+
+constexpr uint64_t kNoallocMaxRays = 65536;
+constexpr size_t kNoallocWork = 256;                      // counter, error word, visits
+constexpr size_t kNoallocRayBytes = 24 * kNoallocMaxRays; // 6 floats per ray
+constexpr size_t kNoallocRecBytes = 32 * kNoallocMaxRays; // largest HitReg<Tags...>
+constexpr size_t kNoallocBytes = kNoallocWork + kNoallocRayBytes + kNoallocRecBytes;
+constexpr int kNoallocMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocBytes];
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[kNoallocMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `device` (which must be current).  In host code
+// the array's name is only a host-side stand-in, so its device address is looked up
+// once per device with cudaGetSymbolAddress.  Caller holds g_noalloc_mu.
+int noalloc_scratch(prt_b200_ctx *ctx, int device, unsigned char **out) {
+	if (device < 0 || device >= kNoallocMaxDevices)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: device index out of range");
+	if (!g_noalloc_ptr[device]) {
+		void *p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if (e != cudaSuccess || !p)
+			return cuda_fail(ctx, e, "nearest_hits_noalloc: cudaGetSymbolAddress");
+		g_noalloc_ptr[device] = p;
+	}
+	*out = static_cast<unsigned char *>(g_noalloc_ptr[device]);
+	return PRT_OK;
+}
+
+} // namespace
+
+extern "C" int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *rays6, uint64_t n,
+                                             uint32_t field_mask, uint32_t rec_size,
+                                             const uint8_t offs[8], void *out_host) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!layout_ok(field_mask, rec_size, offs, why))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: " + why);
+	if (n > kNoallocMaxRays)
+		return fail(ctx, PRT_ERR_LIMIT,
+		            "nearest_hits_noalloc: at most 65536 rays per call (" + std::to_string(n) +
+		                " given); split the batch or use prt_b200_nearest_hits");
+	if (n && (!rays6 || !out_host))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: null buffer");
+	std::lock_guard<std::mutex> glk(g_noalloc_mu);
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	if (!ctx->scene_set)
+		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits_noalloc: set_tris has not succeeded");
+	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: compressed nodes were not built");
+	if (n == 0)
+		return PRT_OK;
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	unsigned char *scratch = nullptr;
+	int rc = noalloc_scratch(ctx, ctx->device, &scratch);
+	if (rc != PRT_OK)
+		return rc;
+	uint32_t *d_work = reinterpret_cast<uint32_t *>(scratch);
+	uint32_t *d_err = d_work + 1;
+	unsigned long long *d_visits = reinterpret_cast<unsigned long long *>(scratch + 16);
+	float *d_rays = reinterpret_cast<float *>(scratch + kNoallocWork);
+	void *d_out = scratch + kNoallocWork + kNoallocRayBytes;
+	cudaStream_t st = ctx->stream;
+	CAPI_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoallocWork, st));
+	CAPI_TRY(ctx, cudaMemcpyAsync(d_rays, rays6, 24ull * n, cudaMemcpyHostToDevice, st));
+	prt::OutLayout lay;
+	lay.mask = field_mask;
+	lay.rec_size = rec_size;
+	std::memcpy(lay.off, offs, 8);
+	prt::TravConfig cfg;
+	cfg.format = ctx->node_format;
+	cfg.block = ctx->block;
+	cfg.count = ctx->count;
+	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays, n, lay, d_out, cfg, d_work,
+	                                       d_visits, d_err, st, ctx->sms));
+	CAPI_TRY(ctx, cudaMemcpyAsync(out_host, d_out, (uint64_t)rec_size * n, cudaMemcpyDeviceToHost,
+	                              st));
+	uint32_t err_word = 0;
+	CAPI_TRY(ctx, cudaMemcpyAsync(&err_word, d_err, 4, cudaMemcpyDeviceToHost, st));
+	CAPI_TRY(ctx, cudaStreamSynchronize(st));
+	if (ctx->count)
+		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, d_visits, 16, cudaMemcpyDeviceToHost));
+	if (err_word)
+		return fail(ctx, PRT_ERR_DEVICE, "nearest_hits_noalloc: kernel reported an error");
+	return PRT_OK;
+}
