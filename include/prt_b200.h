@@ -119,6 +119,54 @@ int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *rays6, uint64_
                                   uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
                                   void *out_host);
 
+/* ---- Batches: many scenes on the device at once --------------------------------------
+ * No counterpart in the reference, which holds one scene per backend (Backend::set_tris,
+ * backend.hpp:19).  A batch builds S scenes in one pass and answers any number of
+ * queries against them with one persistent launch; each answer equals what
+ * nearest_hits<Tags...> gives for that scene alone.  A batch uses its context's device,
+ * options and scratch; calls on it are serialised with the context's. */
+typedef struct prt_b200_batch prt_b200_batch;
+
+/* One query: rays of one scene of the batch and where their records go (device memory,
+ * layout as in prt_b200_nearest_hits). */
+typedef struct {
+	uint32_t scene;      /* index of the scene in the batch */
+	uint32_t field_mask; /* PRT_FIELD_* */
+	const float *rays;   /* n_rays x 6 floats, device memory, 8-byte aligned */
+	uint64_t n_rays;
+	void *out;           /* n_rays records of rec_size bytes, device memory */
+	uint32_t rec_size;
+	uint8_t offs[8];     /* PRT_OFF_* */
+} prt_b200_query;
+
+int prt_b200_batch_create(prt_b200_ctx *ctx, prt_b200_batch **out);
+void prt_b200_batch_destroy(prt_b200_batch *batch);
+
+/* Builds every scene: scene s is d_tris[tri_off[s] .. tri_off[s+1]) (triangles of 9
+ * floats in device memory; tri_off is host memory with n_scenes + 1 entries, starting at
+ * 0).  Primitive ids are per scene, from 0.  Synchronous. */
+int prt_b200_batch_set_tris_dev(prt_b200_batch *batch, const float *d_tris,
+                                const uint64_t *tri_off, uint32_t n_scenes);
+
+/* Answers all queries with one launch queued on `stream` (NULL = the context's).  Up to
+ * 8 launches per batch may be in flight; prt_b200_batch_sync waits for them. */
+int prt_b200_batch_query_dev(prt_b200_batch *batch, const prt_b200_query *queries,
+                             uint32_t n_queries, void *stream);
+
+/* Build + query as one CUDA graph: the first call with these arguments (device pointers,
+ * offsets, queries and the context's options) captures the whole build and the query
+ * launch and instantiates the graph; later calls with the same arguments replay it on
+ * `stream`.  Inputs are read when the graph runs. */
+int prt_b200_batch_run_graph(prt_b200_batch *batch, const float *d_tris,
+                             const uint64_t *tri_off, uint32_t n_scenes,
+                             const prt_b200_query *queries, uint32_t n_queries, void *stream);
+
+/* Waits for the batch's launches and reports kernel-side errors. */
+int prt_b200_batch_sync(prt_b200_batch *batch);
+
+/* "n_scenes", "n_tris", "n_nodes", "depth", "build_ms", "visits_nodes", "visits_tris". */
+int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
+
 /* Tuning and statistics.  Options (take effect at the next set_tris unless noted):
  *   "leaf_size"    1..8  most triangles per leaf of the 8-wide tree (default 1)
  *   "node_format"  PRT_NODES_FP32 or PRT_NODES_COMPRESSED (default FP32; applies to the

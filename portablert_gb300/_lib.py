@@ -18,7 +18,18 @@ EXPORTS = (
     "prt_b200_device_name", "prt_b200_set_tris", "prt_b200_set_tris_dev",
     "prt_b200_nearest_hits", "prt_b200_nearest_hits_dev", "prt_b200_sync",
     "prt_b200_set_option", "prt_b200_get_stat", "prt_b200_nearest_hits_noalloc",
+    "prt_b200_batch_create", "prt_b200_batch_destroy", "prt_b200_batch_set_tris_dev",
+    "prt_b200_batch_query_dev", "prt_b200_batch_run_graph", "prt_b200_batch_sync",
+    "prt_b200_batch_stat",
 )
+
+
+class Query(ctypes.Structure):
+    """prt_b200_query (include/prt_b200.h)."""
+    _fields_ = [("scene", ctypes.c_uint32), ("field_mask", ctypes.c_uint32),
+                ("rays", ctypes.c_void_p), ("n_rays", ctypes.c_uint64),
+                ("out", ctypes.c_void_p), ("rec_size", ctypes.c_uint32),
+                ("offs", ctypes.c_uint8 * 8)]
 
 PRT_OK = 0
 ERRORS = {1: "PRT_ERR_ARG", 2: "PRT_ERR_CUDA", 3: "PRT_ERR_NO_DEVICE", 4: "PRT_ERR_NO_SCENE",
@@ -60,6 +71,21 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_sync.argtypes = [vp]
     L.prt_b200_nearest_hits_noalloc.restype = c_int
     L.prt_b200_nearest_hits_noalloc.argtypes = [vp, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp]
+    qp = ctypes.POINTER(Query)
+    L.prt_b200_batch_create.restype = c_int
+    L.prt_b200_batch_create.argtypes = [vp, ctypes.POINTER(vp)]
+    L.prt_b200_batch_destroy.restype = None
+    L.prt_b200_batch_destroy.argtypes = [vp]
+    L.prt_b200_batch_set_tris_dev.restype = c_int
+    L.prt_b200_batch_set_tris_dev.argtypes = [vp, vp, ctypes.POINTER(c_u64), c_u32]
+    L.prt_b200_batch_query_dev.restype = c_int
+    L.prt_b200_batch_query_dev.argtypes = [vp, qp, c_u32, vp]
+    L.prt_b200_batch_run_graph.restype = c_int
+    L.prt_b200_batch_run_graph.argtypes = [vp, vp, ctypes.POINTER(c_u64), c_u32, qp, c_u32, vp]
+    L.prt_b200_batch_sync.restype = c_int
+    L.prt_b200_batch_sync.argtypes = [vp]
+    L.prt_b200_batch_stat.restype = c_int
+    L.prt_b200_batch_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.prt_b200_set_option.restype = c_int
     L.prt_b200_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
     L.prt_b200_get_stat.restype = c_int

@@ -1,16 +1,19 @@
-// prt_build.cu - LBVH build of the 8-wide tree on the GPU.
+// prt_build.cu - LBVH build of 8-wide trees on the GPU, for one scene or many at once.
 //
 // Replaces the single-threaded binned-SAH build of portableRT (bvh.hpp:58-193).  The
 // tree's shape does not affect the answers (every triangle whose own box passes the
 // reference slab test is examined; see prt_traverse.cu), so a fast parallel build is
-// used instead:
-//   1. centroid bounds            (k_centroid_bounds)
+// used instead.  Several scenes are built in the same launches: scene s owns the input
+// triangles [tri_off[s], tri_off[s+1]), its sort key carries the scene index above the
+// Morton code, its binary nodes are the range [int_off[s], int_off[s+1]) and its 8-wide
+// root is node s.
+//   1. centroid bounds per scene  (k_centroid_bounds; warp reduce + ordered-int atomics)
 //   2. 30-bit Morton codes        (k_morton; 10 bits per axis, centroids normalised)
-//   3. onesweep radix sort        (prt_sort.cu; 4 digit passes, stable)
-//   4. Karras hierarchy           (k_karras; Karras 2012, ties broken by index)
+//   3. onesweep radix sort        (prt_sort.cu; 4 digit passes, +1 or 2 for the scene)
+//   4. Karras hierarchy           (k_karras; Karras 2012 within each scene's range)
 //   5. bottom-up refit            (k_leaf_boxes + k_refit; atomic arrival counters)
-//   6. collapse to 8-wide nodes   (k_collapse, one launch per level; the child of
-//                                  largest surface area is opened until 8 children)
+//   6. collapse to 8-wide nodes   (k_collapse, one launch per level, per-level counters,
+//                                  so the host checks progress only every few levels)
 //   7. triangle re-layout         (k_relayout; each node's leaf triangles contiguous)
 //   8. optional 8-bit encoding    (k_compress; outward-rounded child boxes)
 // A triangle with a non-finite vertex gets the box [-FLT_MAX, FLT_MAX]^3 in the tree,
@@ -26,10 +29,10 @@
 namespace prt {
 
 void BuildScratch::release() {
-	DevBuf *all[] = {&keys,       &vals,       &keys2,  &vals2,       &left,       &right,
-	                 &parent_int, &parent_leaf, &rfirst, &rlast,       &ibox,       &lbox,
-	                 &flags,      &items_a,    &items_b, &counters,   &perm,       &sort_hist,
-	                 &sort_tiles, &sort_status, &bounds};
+	DevBuf *all[] = {&keys,        &vals,     &keys2,      &vals2,    &scene_of,   &int_off,
+	                 &left,        &right,    &parent_int, &parent_leaf, &rfirst,  &rlast,
+	                 &ibox,        &lbox,     &flags,      &items_a,  &items_b,    &counters,
+	                 &perm,        &sort_hist, &sort_tiles, &sort_status, &bounds};
 	for (DevBuf *b : all)
 		b->release();
 	if (h_counters)
@@ -39,8 +42,15 @@ void BuildScratch::release() {
 
 namespace {
 
+constexpr int kMaxLevels = 32;       // 8-wide levels (the traversal's depth limit)
+constexpr int kLevelsPerCheck = 4;   // collapse launches between host checks
+// counters layout: [0, kMaxLevels] frontier size per level, then nodes used, triangles placed
+constexpr int kCtrNodes = kMaxLevels + 1;
+constexpr int kCtrTris = kMaxLevels + 2;
+constexpr int kCtrWords = kMaxLevels + 3;
+
 struct Item {
-	uint32_t ref;  // binary-tree reference (bit 31 = leaf)
+	uint32_t ref;  // binary-tree reference (bit 31 = leaf); kNone = empty scene
 	uint32_t slot; // index of the 8-wide node it becomes
 };
 
@@ -52,31 +62,69 @@ __device__ __forceinline__ bool tri_finite(const float *t) {
 	return ok;
 }
 
-__global__ void k_centroid_bounds(const float *__restrict__ tris, uint32_t n, uint32_t *gb) {
-	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
-	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const float *t = tris + 9 * (size_t)i;
-		if (!tri_finite(t))
-			continue;
+__device__ __forceinline__ float centroid(const float *t, int k) {
+	return t[k] * (1.0f / 3.0f) + t[k + 3] * (1.0f / 3.0f) + t[k + 6] * (1.0f / 3.0f);
+}
+
+__device__ __forceinline__ uint32_t scene_at(const uint32_t *scene_of, uint32_t i) {
+	return scene_of ? scene_of[i] : 0u;
+}
+
+// scene_of[i] = s for every triangle of scene s (one block per scene, grid-stride).
+__global__ void k_scene_of(const uint32_t *tri_off, uint32_t n_scenes, uint32_t *scene_of) {
+	for (uint32_t s = blockIdx.x; s < n_scenes; s += gridDim.x)
+		for (uint32_t i = tri_off[s] + threadIdx.x; i < tri_off[s + 1]; i += blockDim.x)
+			scene_of[i] = s;
+}
+
+__global__ void k_bounds_init(uint32_t *gb, uint32_t n_scenes) {
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < 6 * n_scenes;
+	     i += gridDim.x * blockDim.x)
+		gb[i] = (i % 6) < 3 ? 0xFFFFFFFFu : 0u;
+}
+
+// Per-scene centroid bounds as ordered words: a warp whose triangles all belong to one
+// scene reduces first; otherwise each lane updates its own scene.
+__global__ void k_centroid_bounds(const float *__restrict__ tris, uint32_t n,
+                                  const uint32_t *__restrict__ scene_of, uint32_t *gb) {
+	const int lane = threadIdx.x & 31;
+	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+		const uint32_t i = base + threadIdx.x;
+		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+		uint32_t s = 0;
+		if (i < n) {
+			const float *t = tris + 9 * (size_t)i;
+			s = scene_at(scene_of, i);
+			if (tri_finite(t)) {
 #pragma unroll
-		for (int k = 0; k < 3; ++k) {
-			float c = t[k] * (1.0f / 3.0f) + t[k + 3] * (1.0f / 3.0f) + t[k + 6] * (1.0f / 3.0f);
-			mn[k] = fminf(mn[k], c);
-			mx[k] = fmaxf(mx[k], c);
+				for (int k = 0; k < 3; ++k)
+					mn[k] = mx[k] = centroid(t, k);
+			}
 		}
-	}
+		// Lanes past the end hold empty bounds, so they never change a reduction.
+		const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, s, 0);
+		const bool same = __all_sync(0xFFFFFFFFu, s == s0 || i >= n);
+		if (same) {
 #pragma unroll
-	for (int k = 0; k < 3; ++k) {
-		for (int o = 16; o > 0; o >>= 1) {
-			mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
-			mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
-		}
-	}
-	if ((threadIdx.x & 31) == 0 && mn[0] <= mx[0]) {
+			for (int k = 0; k < 3; ++k) {
+				for (int o = 16; o > 0; o >>= 1) {
+					mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+					mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
+				}
+			}
+			if (lane == 0 && mn[0] <= mx[0]) {
 #pragma unroll
-		for (int k = 0; k < 3; ++k) {
-			atomicMin(&gb[k], f2ord(mn[k]));
-			atomicMax(&gb[3 + k], f2ord(mx[k]));
+				for (int k = 0; k < 3; ++k) {
+					atomicMin(&gb[6 * s0 + k], f2ord(mn[k]));
+					atomicMax(&gb[6 * s0 + 3 + k], f2ord(mx[k]));
+				}
+			}
+		} else if (i < n && mn[0] <= mx[0]) {
+#pragma unroll
+			for (int k = 0; k < 3; ++k) {
+				atomicMin(&gb[6 * s + k], f2ord(mn[k]));
+				atomicMax(&gb[6 * s + 3 + k], f2ord(mx[k]));
+			}
 		}
 	}
 }
@@ -90,83 +138,110 @@ __device__ __forceinline__ uint32_t spread10(uint32_t x) {
 	return x;
 }
 
-__global__ void k_morton(const float *__restrict__ tris, uint32_t n, const uint32_t *gb,
-                         uint32_t *keys, uint32_t *vals) {
+// Key = Morton code of the centroid in its scene's centroid box; with several scenes
+// (64-bit keys) the scene index sits above it.
+template <typename K>
+__global__ void k_morton(const float *__restrict__ tris, uint32_t n,
+                         const uint32_t *__restrict__ scene_of, const uint32_t *gb, K *keys,
+                         uint32_t *vals) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n)
 		return;
 	const float *t = tris + 9 * (size_t)i;
+	const uint32_t s = scene_at(scene_of, i);
+	const uint32_t *b = gb + 6 * s;
 	uint32_t code = 0;
-	float lo0 = ord2f(gb[0]), hi0 = ord2f(gb[3]);
-	if (tri_finite(t) && lo0 <= hi0) {
+	if (tri_finite(t) && ord2f(b[0]) <= ord2f(b[3])) {
 		uint32_t q[3];
 #pragma unroll
 		for (int k = 0; k < 3; ++k) {
-			float lo = ord2f(gb[k]), hi = ord2f(gb[3 + k]);
-			float ext = hi - lo;
-			float s = ext > 0.0f ? 1024.0f / ext : 0.0f;
-			float c = t[k] * (1.0f / 3.0f) + t[k + 3] * (1.0f / 3.0f) + t[k + 6] * (1.0f / 3.0f);
-			float qf = fminf(fmaxf((c - lo) * s, 0.0f), 1023.0f);
+			const float lo = ord2f(b[k]), hi = ord2f(b[3 + k]);
+			const float ext = hi - lo;
+			const float sc = ext > 0.0f ? 1024.0f / ext : 0.0f;
+			const float qf = fminf(fmaxf((centroid(t, k) - lo) * sc, 0.0f), 1023.0f);
 			q[k] = (uint32_t)qf;
 		}
 		code = (spread10(q[0]) << 2) | (spread10(q[1]) << 1) | spread10(q[2]);
 	}
-	keys[i] = code;
+	if (sizeof(K) == 8)
+		keys[i] = (K)(((uint64_t)s << 32) | code);
+	else
+		keys[i] = (K)code;
 	vals[i] = i;
 }
 
-// Length of the common prefix of keys i and j, with the index appended to break ties
-// between equal keys; -1 outside [0, n).
-__device__ __forceinline__ int kdelta(const uint32_t *__restrict__ k, int n, int i, int j) {
+// Common-prefix length of the Morton codes of leaves i and j of one scene, with the
+// index appended to break ties between equal codes; -1 outside [0, n).
+template <typename K>
+__device__ __forceinline__ int kdelta(const K *__restrict__ k, int n, int i, int j) {
 	if (j < 0 || j >= n)
 		return -1;
-	uint32_t a = k[i], b = k[j];
+	const uint32_t a = (uint32_t)k[i], b = (uint32_t)k[j];
 	return (a != b) ? __clz(a ^ b) : 32 + __clz((uint32_t)i ^ (uint32_t)j);
 }
 
-__global__ void k_karras(const uint32_t *__restrict__ keys, int n, uint32_t *left,
+// Binary node gi: find its scene (int_off is non-decreasing), then Karras's
+// construction on that scene's sorted leaves.  References are global: leaf positions
+// are tri_off[s] + local, binary nodes int_off[s] + local.
+template <typename K>
+__global__ void k_karras(const K *__restrict__ keys, uint32_t n_int, const uint32_t *tri_off,
+                         const uint32_t *int_off, uint32_t n_scenes, uint32_t *left,
                          uint32_t *right, uint32_t *parent_int, uint32_t *parent_leaf,
                          uint32_t *rfirst, uint32_t *rlast) {
-	int i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n - 1)
+	const uint32_t gi = blockIdx.x * blockDim.x + threadIdx.x;
+	if (gi >= n_int)
 		return;
-	const int d = kdelta(keys, n, i, i + 1) > kdelta(keys, n, i, i - 1) ? 1 : -1;
-	const int dmin = kdelta(keys, n, i, i - d);
+	uint32_t lo_s = 0, hi_s = n_scenes; // last s with int_off[s] <= gi
+	while (hi_s - lo_s > 1) {
+		const uint32_t mid = (lo_s + hi_s) >> 1;
+		if (int_off[mid] <= gi)
+			lo_s = mid;
+		else
+			hi_s = mid;
+	}
+	const uint32_t s = lo_s;
+	const uint32_t first = tri_off[s], ibase = int_off[s];
+	const int n = (int)(tri_off[s + 1] - first);
+	const int i = (int)(gi - ibase);
+	const K *k = keys + first;
+	const int d = kdelta(k, n, i, i + 1) > kdelta(k, n, i, i - 1) ? 1 : -1;
+	const int dmin = kdelta(k, n, i, i - d);
 	int lmax = 2;
-	while (kdelta(keys, n, i, i + lmax * d) > dmin)
+	while (kdelta(k, n, i, i + lmax * d) > dmin)
 		lmax <<= 1;
 	int l = 0;
 	for (int t = lmax >> 1; t >= 1; t >>= 1)
-		if (kdelta(keys, n, i, i + (l + t) * d) > dmin)
+		if (kdelta(k, n, i, i + (l + t) * d) > dmin)
 			l += t;
 	const int j = i + l * d;
-	const int dnode = kdelta(keys, n, i, j);
-	int s = 0;
+	const int dnode = kdelta(k, n, i, j);
+	int sp = 0;
 	for (int div = 2;; div <<= 1) {
-		int t = (l + div - 1) / div;
-		if (kdelta(keys, n, i, i + (s + t) * d) > dnode)
-			s += t;
+		const int t = (l + div - 1) / div;
+		if (kdelta(k, n, i, i + (sp + t) * d) > dnode)
+			sp += t;
 		if (t <= 1)
 			break;
 	}
-	const int gamma = i + s * d + min(d, 0);
+	const int gamma = i + sp * d + min(d, 0);
 	const int lo = min(i, j), hi = max(i, j);
-	uint32_t lc = (lo == gamma) ? (kLeafBit | (uint32_t)gamma) : (uint32_t)gamma;
-	uint32_t rc = (hi == gamma + 1) ? (kLeafBit | (uint32_t)(gamma + 1)) : (uint32_t)(gamma + 1);
-	left[i] = lc;
-	right[i] = rc;
-	if (lc & kLeafBit)
-		parent_leaf[gamma] = i;
+	const bool lleaf = lo == gamma, rleaf = hi == gamma + 1;
+	const uint32_t lc = lleaf ? (kLeafBit | (first + gamma)) : (ibase + gamma);
+	const uint32_t rc = rleaf ? (kLeafBit | (first + gamma + 1)) : (ibase + gamma + 1);
+	left[gi] = lc;
+	right[gi] = rc;
+	if (lleaf)
+		parent_leaf[first + gamma] = gi;
 	else
-		parent_int[gamma] = i;
-	if (rc & kLeafBit)
-		parent_leaf[gamma + 1] = i;
+		parent_int[ibase + gamma] = gi;
+	if (rleaf)
+		parent_leaf[first + gamma + 1] = gi;
 	else
-		parent_int[gamma + 1] = i;
-	rfirst[i] = lo;
-	rlast[i] = hi;
+		parent_int[ibase + gamma + 1] = gi;
+	rfirst[gi] = first + lo;
+	rlast[gi] = first + hi;
 	if (i == 0)
-		parent_int[0] = kNone;
+		parent_int[gi] = kNone;
 }
 
 __global__ void k_leaf_boxes(const float *__restrict__ tris, const uint32_t *__restrict__ vals,
@@ -201,15 +276,16 @@ __device__ __forceinline__ void child_box(uint32_t ref, const float4 *ibox, cons
 	}
 }
 
-// One thread per leaf walks towards the root; at each binary node the first thread to
-// arrive stops and the second, which then sees both children's boxes, writes the
-// union and continues.  No thread waits on another.
+// One thread per leaf walks towards its scene's root; at each binary node the first
+// thread to arrive stops and the second, which then sees both children's boxes, writes
+// the union and continues.  No thread waits on another.  A scene of one triangle has
+// no binary node (parent_leaf stays kNone).
 __global__ void k_refit(uint32_t n, const uint32_t *__restrict__ parent_leaf,
                         const uint32_t *__restrict__ parent_int, const uint32_t *__restrict__ left,
                         const uint32_t *__restrict__ right, const float4 *lbox, float4 *ibox,
                         uint32_t *flags) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n || n < 2)
+	if (i >= n)
 		return;
 	uint32_t p = parent_leaf[i];
 	while (p != kNone) {
@@ -228,6 +304,22 @@ __global__ void k_refit(uint32_t n, const uint32_t *__restrict__ parent_leaf,
 	}
 }
 
+// Level-0 frontier: the root of every scene becomes 8-wide node s; the node counter
+// starts after the roots.
+__global__ void k_collapse_roots(const uint32_t *tri_off, const uint32_t *int_off,
+                                 uint32_t n_scenes, Item *items, uint32_t *ctr) {
+	const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+	if (s == 0) {
+		ctr[0] = n_scenes;
+		ctr[kCtrNodes] = n_scenes;
+	}
+	if (s >= n_scenes)
+		return;
+	const uint32_t n = tri_off[s + 1] - tri_off[s];
+	const uint32_t ref = n == 0 ? kNone : (n == 1 ? (kLeafBit | tri_off[s]) : int_off[s]);
+	items[s] = Item{ref, s};
+}
+
 __device__ __forceinline__ uint32_t bcount(uint32_t ref, const uint32_t *rfirst,
                                            const uint32_t *rlast) {
 	return (ref & kLeafBit) ? 1u : (rlast[ref] - rfirst[ref] + 1u);
@@ -243,6 +335,7 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 	return isfinite(a) ? a : FLT_MAX;
 }
 
+// One level: each frontier item becomes an 8-wide node.
 __global__ void __launch_bounds__(128)
     k_collapse(const Item *__restrict__ in, const uint32_t *in_count, Item *out,
                uint32_t *out_count, uint32_t *node_counter, uint32_t node_cap,
@@ -255,6 +348,18 @@ __global__ void __launch_bounds__(128)
 	for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_in;
 	     w += gridDim.x * blockDim.x) {
 		const Item it = in[w];
+		Node8 *nd = nodes + it.slot;
+		if (it.ref == kNone) { // empty scene: a node without children
+			for (int c = 0; c < 8; ++c) {
+				Child8 ch;
+				ch.lo_x = ch.lo_y = ch.lo_z = 0.0f;
+				ch.hi_x = ch.hi_y = ch.hi_z = 0.0f;
+				ch.ref = kNone;
+				ch.pad = 0u;
+				nd->c[c] = ch;
+			}
+			continue;
+		}
 		uint32_t C[8];
 		int nc = 1;
 		C[0] = it.ref;
@@ -310,7 +415,6 @@ __global__ void __launch_bounds__(128)
 			atomicOr(err, kErrCollapse);
 			continue;
 		}
-		Node8 *nd = nodes + it.slot;
 		uint32_t k_inner = 0, toff = 0;
 		for (int c = 0; c < 8; ++c) {
 			float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
@@ -352,15 +456,19 @@ __global__ void __launch_bounds__(128)
 	}
 }
 
+// Triangle records in leaf order; tri4.w holds the per-scene primitive id and inv maps
+// a global input index to its leaf-order position.
 __global__ void k_relayout(const float *__restrict__ tris, const uint32_t *__restrict__ vals,
-                           const uint32_t *__restrict__ perm, uint32_t n, float4 *tri4,
+                           const uint32_t *__restrict__ perm, const uint32_t *__restrict__ scene_of,
+                           const uint32_t *__restrict__ tri_off, uint32_t n, float4 *tri4,
                            uint32_t *inv) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n)
 		return;
-	uint32_t pid = vals[perm[i]];
-	inv[pid] = i;
-	const float *t = tris + 9 * (size_t)pid;
+	const uint32_t g = vals[perm[i]];
+	const uint32_t pid = g - tri_off[scene_at(scene_of, g)];
+	inv[g] = i;
+	const float *t = tris + 9 * (size_t)g;
 	tri4[3 * (size_t)i] = make_float4(t[0], t[1], t[2], __uint_as_float(pid));
 	tri4[3 * (size_t)i + 1] = make_float4(t[3], t[4], t[5], 0.0f);
 	tri4[3 * (size_t)i + 2] = make_float4(t[6], t[7], t[8], 0.0f);
@@ -394,9 +502,12 @@ __device__ uint32_t quant_hi(float o, float s, float v) {
 	return q;
 }
 
-__global__ void k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes, CNode8 *cn) {
+// n_nodes_dev (when not null) holds the node count on the device: a build queued
+// without host round-trips launches this kernel over the node capacity.
+__global__ void k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes,
+                           const uint32_t *n_nodes_dev, CNode8 *cn) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= n_nodes)
+	if (i >= (n_nodes_dev ? *n_nodes_dev : n_nodes))
 		return;
 	const Node8 &nd = nodes[i];
 	float lo[3][8], hi[3][8];
@@ -491,128 +602,244 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 
 } // namespace
 
-int build_scene(const float *d_tris, uint64_t n64, int leaf_size, bool compressed, SceneGPU &sc,
-                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg) {
-	if (n64 > kMaxTris) {
-		msg = "set_tris: at most 134217727 triangles per scene";
-		return PRT_ERR_LIMIT;
-	}
+int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compressed,
+               SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
+               std::string &msg) {
 	if (leaf_size < 1 || leaf_size > kMaxLeaf) {
 		msg = "leaf_size must be in [1, 8]";
 		return PRT_ERR_ARG;
 	}
-	const uint32_t n = (uint32_t)n64;
+	if (S == 0 || !tri_off64 || tri_off64[0] != 0) {
+		msg = "build: at least one scene, offsets starting at 0";
+		return PRT_ERR_ARG;
+	}
+	for (uint32_t s = 0; s < S; ++s) {
+		if (tri_off64[s + 1] < tri_off64[s]) {
+			msg = "build: triangle offsets must not decrease";
+			return PRT_ERR_ARG;
+		}
+	}
+	const uint64_t n64 = tri_off64[S];
+	if (n64 > kMaxTris) {
+		msg = "set_tris: at most 134217727 triangles per scene";
+		return PRT_ERR_LIMIT;
+	}
+	plan.S = S;
+	plan.n = (uint32_t)n64;
+	plan.leaf_size = leaf_size;
+	plan.compressed = compressed;
+	plan.multi = S > 1;
+	plan.toff.resize(S + 1);
+	plan.ioff.resize(S + 1);
+	plan.n_int = 0;
+	for (uint32_t s = 0; s <= S; ++s) {
+		plan.toff[s] = (uint32_t)tri_off64[s];
+		plan.ioff[s] = plan.n_int;
+		if (s < S)
+			plan.n_int += plan.toff[s + 1] - plan.toff[s] > 1 ? plan.toff[s + 1] - plan.toff[s] - 1 : 0;
+	}
+	plan.scene_digits = 0;
+	for (uint32_t v = S - 1; v; v >>= 8)
+		++plan.scene_digits;
+	const uint32_t n = plan.n;
+	plan.node_cap = n + S;
+
+	sc.n_scenes = S;
 	sc.n_tris = n;
 	sc.leaf_size = leaf_size;
 	sc.n_nodes = 0;
 	sc.depth = 0;
 	sc.has_cnodes = false;
-	if (n == 0)
-		return PRT_OK;
+	sc.h_tri_off.assign(tri_off64, tri_off64 + S + 1);
 
-	const size_t ni = std::max<uint32_t>(n - 1, 1);
-	const uint32_t node_cap = n;
-	BUILD_TRY(ws.keys.reserve(4ull * n));
-	BUILD_TRY(ws.vals.reserve(4ull * n));
-	BUILD_TRY(ws.keys2.reserve(4ull * n));
-	BUILD_TRY(ws.vals2.reserve(4ull * n));
+	const size_t key_bytes = plan.multi ? 8 : 4;
+	const size_t ni = std::max<uint32_t>(plan.n_int, 1);
+	const size_t nn = std::max<uint32_t>(n, 1);
+	BUILD_TRY(sc.tri_off.reserve(4ull * (S + 1)));
+	BUILD_TRY(ws.keys.reserve(key_bytes * nn));
+	BUILD_TRY(ws.keys2.reserve(key_bytes * nn));
+	BUILD_TRY(ws.vals.reserve(4 * nn));
+	BUILD_TRY(ws.vals2.reserve(4 * nn));
+	if (plan.multi)
+		BUILD_TRY(ws.scene_of.reserve(4 * nn));
+	BUILD_TRY(ws.int_off.reserve(4ull * (S + 1)));
 	BUILD_TRY(ws.left.reserve(4 * ni));
 	BUILD_TRY(ws.right.reserve(4 * ni));
 	BUILD_TRY(ws.parent_int.reserve(4 * ni));
-	BUILD_TRY(ws.parent_leaf.reserve(4ull * n));
+	BUILD_TRY(ws.parent_leaf.reserve(4 * nn));
 	BUILD_TRY(ws.rfirst.reserve(4 * ni));
 	BUILD_TRY(ws.rlast.reserve(4 * ni));
 	BUILD_TRY(ws.flags.reserve(4 * ni));
 	BUILD_TRY(ws.ibox.reserve(32 * ni));
-	BUILD_TRY(ws.lbox.reserve(32ull * n));
-	BUILD_TRY(ws.items_a.reserve(8ull * n));
-	BUILD_TRY(ws.items_b.reserve(8ull * n));
-	BUILD_TRY(ws.counters.reserve(64));
-	BUILD_TRY(ws.perm.reserve(4ull * n));
+	BUILD_TRY(ws.lbox.reserve(32 * nn));
+	BUILD_TRY(ws.items_a.reserve(8ull * plan.node_cap));
+	BUILD_TRY(ws.items_b.reserve(8ull * plan.node_cap));
+	BUILD_TRY(ws.counters.reserve(4 * kCtrWords));
+	BUILD_TRY(ws.perm.reserve(4 * nn));
 	BUILD_TRY(ws.sort_hist.reserve(8 * 256 * 4));
 	BUILD_TRY(ws.sort_tiles.reserve(8 * 4));
 	BUILD_TRY(ws.sort_status.reserve(4 * sort_status_words(n)));
-	BUILD_TRY(ws.bounds.reserve(32));
-	BUILD_TRY(sc.tri4.reserve(48ull * n));
-	BUILD_TRY(sc.inv.reserve(4ull * n));
-	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)node_cap));
+	BUILD_TRY(ws.bounds.reserve(24ull * S));
+	BUILD_TRY(sc.tri4.reserve(48 * nn));
+	BUILD_TRY(sc.inv.reserve(4 * nn));
+	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)plan.node_cap));
+	if (compressed)
+		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * (size_t)plan.node_cap));
 	if (!ws.h_counters)
-		BUILD_TRY(cudaMallocHost(&ws.h_counters, 64));
+		BUILD_TRY(cudaMallocHost(&ws.h_counters, 4 * kCtrWords));
+	BUILD_TRY(cudaMemcpyAsync(sc.tri_off.p, plan.toff.data(), 4ull * (S + 1),
+	                          cudaMemcpyHostToDevice, st));
+	BUILD_TRY(cudaMemcpyAsync(ws.int_off.p, plan.ioff.data(), 4ull * (S + 1),
+	                          cudaMemcpyHostToDevice, st));
+	return PRT_OK;
+}
 
+int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
+                  cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg) {
+	const uint32_t S = plan.S, n = plan.n, n_int = plan.n_int;
+	const size_t ni = std::max<uint32_t>(n_int, 1);
+	const size_t nn = std::max<uint32_t>(n, 1);
+	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
+	uint32_t *d_ioff = ws.int_off.as<uint32_t>();
+	uint32_t *scene_of = plan.multi ? ws.scene_of.as<uint32_t>() : nullptr;
+	if (plan.multi)
+		k_scene_of<<<std::min(S, 4096u), 256, 0, st>>>(d_toff, S, scene_of);
 	uint32_t *gb = ws.bounds.as<uint32_t>();
-	BUILD_TRY(cudaMemsetAsync(gb, 0xFF, 12, st));
-	BUILD_TRY(cudaMemsetAsync(gb + 3, 0x00, 12, st));
-	k_centroid_bounds<<<std::min(blocks_for(n, 256), 1024u), 256, 0, st>>>(d_tris, n, gb);
-	k_morton<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, gb, ws.keys.as<uint32_t>(),
-	                                             ws.vals.as<uint32_t>());
+	k_bounds_init<<<blocks_for(6ull * S, 256), 256, 0, st>>>(gb, S);
+	if (n)
+		k_centroid_bounds<<<std::min(blocks_for(n, 256), 2048u), 256, 0, st>>>(d_tris, n, scene_of,
+		                                                                        gb);
 	SortScratch ss{ws.sort_hist.as<uint32_t>(), ws.sort_tiles.as<uint32_t>(),
 	               ws.sort_status.as<uint32_t>()};
-	int where = sort_pairs_u32(ws.keys.as<uint32_t>(), ws.vals.as<uint32_t>(),
-	                           ws.keys2.as<uint32_t>(), ws.vals2.as<uint32_t>(), n, 4, ss, st, d_err);
-	const uint32_t *skeys = where ? ws.keys2.as<uint32_t>() : ws.keys.as<uint32_t>();
-	const uint32_t *svals = where ? ws.vals2.as<uint32_t>() : ws.vals.as<uint32_t>();
+	const uint32_t *svals = ws.vals.as<uint32_t>();
+	const void *skeys = ws.keys.p;
+	if (n && !plan.multi) {
+		k_morton<uint32_t><<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, nullptr, gb,
+		                                                       ws.keys.as<uint32_t>(),
+		                                                       ws.vals.as<uint32_t>());
+		int where = sort_pairs_u32(ws.keys.as<uint32_t>(), ws.vals.as<uint32_t>(),
+		                           ws.keys2.as<uint32_t>(), ws.vals2.as<uint32_t>(), n, 4, ss, st,
+		                           d_err);
+		skeys = where ? ws.keys2.p : ws.keys.p;
+		svals = where ? ws.vals2.as<uint32_t>() : ws.vals.as<uint32_t>();
+	} else if (n) {
+		k_morton<uint64_t><<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, scene_of, gb,
+		                                                       ws.keys.as<uint64_t>(),
+		                                                       ws.vals.as<uint32_t>());
+		int where = sort_pairs_u64(ws.keys.as<uint64_t>(), ws.vals.as<uint32_t>(),
+		                           ws.keys2.as<uint64_t>(), ws.vals2.as<uint32_t>(), n,
+		                           4 + plan.scene_digits, ss, st, d_err);
+		skeys = where ? ws.keys2.p : ws.keys.p;
+		svals = where ? ws.vals2.as<uint32_t>() : ws.vals.as<uint32_t>();
+	}
 
-	if (n >= 2) {
-		k_karras<<<blocks_for(n - 1, 256), 256, 0, st>>>(
-		    skeys, (int)n, ws.left.as<uint32_t>(), ws.right.as<uint32_t>(),
-		    ws.parent_int.as<uint32_t>(), ws.parent_leaf.as<uint32_t>(), ws.rfirst.as<uint32_t>(),
-		    ws.rlast.as<uint32_t>());
+	BUILD_TRY(cudaMemsetAsync(ws.parent_leaf.p, 0xFF, 4 * nn, st));
+	if (n_int) {
+		if (plan.multi)
+			k_karras<uint64_t><<<blocks_for(n_int, 256), 256, 0, st>>>(
+			    static_cast<const uint64_t *>(skeys), n_int, d_toff, d_ioff, S,
+			    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
+			    ws.parent_leaf.as<uint32_t>(), ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>());
+		else
+			k_karras<uint32_t><<<blocks_for(n_int, 256), 256, 0, st>>>(
+			    static_cast<const uint32_t *>(skeys), n_int, d_toff, d_ioff, S,
+			    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
+			    ws.parent_leaf.as<uint32_t>(), ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>());
 		BUILD_TRY(cudaMemsetAsync(ws.flags.p, 0, 4 * ni, st));
 	}
-	k_leaf_boxes<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, n, ws.lbox.as<float4>());
-	if (n >= 2)
-		k_refit<<<blocks_for(n, 256), 256, 0, st>>>(
-		    n, ws.parent_leaf.as<uint32_t>(), ws.parent_int.as<uint32_t>(), ws.left.as<uint32_t>(),
-		    ws.right.as<uint32_t>(), ws.lbox.as<float4>(), ws.ibox.as<float4>(),
-		    ws.flags.as<uint32_t>());
+	if (n) {
+		k_leaf_boxes<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, n, ws.lbox.as<float4>());
+		if (n_int)
+			k_refit<<<blocks_for(n, 256), 256, 0, st>>>(
+			    n, ws.parent_leaf.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
+			    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.lbox.as<float4>(),
+			    ws.ibox.as<float4>(), ws.flags.as<uint32_t>());
+	}
 
-	// counters: [0], [1] frontier sizes, [2] nodes used, [3] triangles placed
-	uint32_t init[4] = {1u, 0u, 1u, 0u};
 	uint32_t *ctr = ws.counters.as<uint32_t>();
-	BUILD_TRY(cudaMemcpyAsync(ctr, init, sizeof init, cudaMemcpyHostToDevice, st));
-	Item root{n == 1 ? (kLeafBit | 0u) : 0u, 0u};
-	BUILD_TRY(cudaMemcpyAsync(ws.items_a.p, &root, sizeof root, cudaMemcpyHostToDevice, st));
-	Item *cur = ws.items_a.as<Item>(), *nxt = ws.items_b.as<Item>();
-	int ci = 0;
-	uint32_t level = 0;
+	BUILD_TRY(cudaMemsetAsync(ctr, 0, 4 * kCtrWords, st));
+	Item *items[2] = {ws.items_a.as<Item>(), ws.items_b.as<Item>()};
+	k_collapse_roots<<<blocks_for(S, 128), 128, 0, st>>>(d_toff, d_ioff, S, items[0], ctr);
+	int level = 0;
 	for (;;) {
-		BUILD_TRY(cudaMemsetAsync(ctr + (ci ^ 1), 0, 4, st));
-		k_collapse<<<1216, 128, 0, st>>>(cur, ctr + ci, nxt, ctr + (ci ^ 1), ctr + 2, node_cap,
-		                                 ctr + 3, sc.nodes.as<Node8>(), ws.perm.as<uint32_t>(),
-		                                 ws.left.as<uint32_t>(), ws.right.as<uint32_t>(),
-		                                 ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>(),
-		                                 ws.ibox.as<float4>(), ws.lbox.as<float4>(),
-		                                 (uint32_t)leaf_size, n, d_err);
-		++level;
-		BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ctr, 16, cudaMemcpyDeviceToHost, st));
-		BUILD_TRY(cudaStreamSynchronize(st));
-		if (ws.h_counters[ci ^ 1] == 0)
+		for (int k = 0; (host_checks ? k < kLevelsPerCheck : true) && level < kMaxLevels;
+		     ++k, ++level)
+			k_collapse<<<1216, 128, 0, st>>>(
+			    items[level & 1], ctr + level, items[(level + 1) & 1], ctr + level + 1,
+			    ctr + kCtrNodes, plan.node_cap, ctr + kCtrTris, sc.nodes.as<Node8>(),
+			    ws.perm.as<uint32_t>(), ws.left.as<uint32_t>(), ws.right.as<uint32_t>(),
+			    ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>(), ws.ibox.as<float4>(),
+			    ws.lbox.as<float4>(), (uint32_t)plan.leaf_size, n, d_err);
+		if (!host_checks)
 			break;
-		std::swap(cur, nxt);
-		ci ^= 1;
-		if (level > 4096) {
-			msg = "collapse did not terminate";
-			return PRT_ERR_DEVICE;
+		BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ctr, 4 * kCtrWords, cudaMemcpyDeviceToHost, st));
+		BUILD_TRY(cudaStreamSynchronize(st));
+		if (ws.h_counters[level] == 0)
+			break;
+		if (level >= kMaxLevels) {
+			msg = "tree deeper than " + std::to_string(kMaxLevels) + " levels";
+			return PRT_ERR_LIMIT;
 		}
 	}
-	sc.n_nodes = ws.h_counters[2];
-	sc.depth = level;
-	if (ws.h_counters[3] != n) {
-		msg = "collapse placed " + std::to_string(ws.h_counters[3]) + " of " + std::to_string(n) +
-		      " triangles";
-		return PRT_ERR_DEVICE;
+	if (n)
+		k_relayout<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, ws.perm.as<uint32_t>(),
+		                                               scene_of, d_toff, n, sc.tri4.as<float4>(),
+		                                               sc.inv.as<uint32_t>());
+	if (host_checks) {
+		int rc = build_finish(sc, ws, st, msg);
+		if (rc != PRT_OK)
+			return rc;
 	}
-	k_relayout<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, ws.perm.as<uint32_t>(), n,
-	                                               sc.tri4.as<float4>(), sc.inv.as<uint32_t>());
-	if (compressed) {
-		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * (size_t)sc.n_nodes));
-		k_compress<<<blocks_for(sc.n_nodes, 128), 128, 0, st>>>(sc.nodes.as<Node8>(), sc.n_nodes,
-		                                                        sc.cnodes.as<CNode8>());
+	if (plan.compressed) {
+		if (host_checks)
+			k_compress<<<blocks_for(sc.n_nodes, 128), 128, 0, st>>>(
+			    sc.nodes.as<Node8>(), sc.n_nodes, nullptr, sc.cnodes.as<CNode8>());
+		else
+			k_compress<<<blocks_for(plan.node_cap, 128), 128, 0, st>>>(
+			    sc.nodes.as<Node8>(), plan.node_cap, ctr + kCtrNodes, sc.cnodes.as<CNode8>());
 		sc.has_cnodes = true;
 	}
 	BUILD_TRY(cudaGetLastError());
-	BUILD_TRY(cudaStreamSynchronize(st));
+	if (host_checks)
+		BUILD_TRY(cudaStreamSynchronize(st));
 	return PRT_OK;
+}
+
+int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg) {
+	BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ws.counters.p, 4 * kCtrWords, cudaMemcpyDeviceToHost,
+	                          st));
+	BUILD_TRY(cudaStreamSynchronize(st));
+	uint32_t depth = 0;
+	while (depth < (uint32_t)kMaxLevels && ws.h_counters[depth])
+		++depth;
+	if (depth == (uint32_t)kMaxLevels && ws.h_counters[kMaxLevels]) {
+		msg = "tree deeper than " + std::to_string(kMaxLevels) + " levels";
+		return PRT_ERR_LIMIT;
+	}
+	sc.n_nodes = ws.h_counters[kCtrNodes];
+	sc.depth = depth;
+	if (ws.h_counters[kCtrTris] != sc.n_tris) {
+		msg = "collapse placed " + std::to_string(ws.h_counters[kCtrTris]) + " of " +
+		      std::to_string(sc.n_tris) + " triangles";
+		return PRT_ERR_DEVICE;
+	}
+	return PRT_OK;
+}
+
+int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
+                 bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
+                 uint32_t *d_err, std::string &msg) {
+	BuildPlan plan;
+	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg);
+	if (rc != PRT_OK)
+		return rc;
+	return build_enqueue(d_tris, plan, sc, ws, st, d_err, true, msg);
+}
+
+int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
+                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg) {
+	const uint64_t off[2] = {0, n};
+	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg);
 }
 
 } // namespace prt

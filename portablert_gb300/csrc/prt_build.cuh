@@ -1,10 +1,11 @@
-// prt_build.cuh - device scene and the LBVH build pipeline (prt_build.cu).
+// prt_build.cuh - device scenes and the LBVH build pipeline (prt_build.cu).
 #pragma once
 
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "prt_internal.cuh"
 #include "prt_sort.cuh"
@@ -36,21 +37,31 @@ struct DevBuf {
 	template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
+// One or more scenes built together into shared arrays ("arena").  Scene s owns the
+// triangles [tri_off[s], tri_off[s+1]) of the input, its root is node s, its triangle
+// records sit anywhere in tri4, and inv + tri_off[s] maps its primitive ids (0-based,
+// per scene, as in the reference) to positions in tri4.
 struct SceneGPU {
-	uint64_t n_tris = 0;
+	uint32_t n_scenes = 0;
+	uint64_t n_tris = 0; // all scenes
 	uint32_t n_nodes = 0;
-	uint32_t depth = 0;
-	int leaf_size = 4;
+	uint32_t depth = 0;  // levels of the deepest tree
+	int leaf_size = 1;
 	bool has_cnodes = false;
-	DevBuf tri4;   // float4[3 n]
-	DevBuf inv;    // uint32[n]: primitive id -> position in tri4
-	DevBuf nodes;  // Node8[n_nodes]
-	DevBuf cnodes; // CNode8[n_nodes]
+	DevBuf tri4;         // float4[3 n]
+	DevBuf inv;          // uint32[n]
+	DevBuf nodes;        // Node8[n_nodes]
+	DevBuf cnodes;       // CNode8[n_nodes]
+	DevBuf tri_off;      // uint32[n_scenes + 1] (device copy)
+	std::vector<uint64_t> h_tri_off;
 	void release() {
 		tri4.release();
 		inv.release();
 		nodes.release();
 		cnodes.release();
+		tri_off.release();
+		h_tri_off.clear();
+		n_scenes = 0;
 		n_tris = 0;
 		n_nodes = 0;
 		depth = 0;
@@ -60,24 +71,57 @@ struct SceneGPU {
 
 // Scratch reused across builds (grow-only).
 struct BuildScratch {
-	DevBuf keys, vals, keys2, vals2;  // Morton codes and triangle indices (sort ping-pong)
-	DevBuf left, right;               // children of the n-1 binary nodes (bit 31 = leaf)
+	DevBuf keys, vals, keys2, vals2;  // Morton keys (u32 or u64) and triangle indices
+	DevBuf scene_of;                  // scene of each input triangle (several scenes)
+	DevBuf int_off;                   // first binary node of each scene
+	DevBuf left, right;               // children of the binary nodes (bit 31 = leaf)
 	DevBuf parent_int, parent_leaf;   // parents of binary nodes and of leaves
 	DevBuf rfirst, rlast;             // leaf range of each binary node
 	DevBuf ibox, lbox;                // boxes of binary nodes and of leaves (2 float4 each)
 	DevBuf flags;                     // refit arrival counters
 	DevBuf items_a, items_b;          // collapse frontiers
-	DevBuf counters;                  // small device counters
+	DevBuf counters;                  // per-level frontier sizes, node / triangle counters
 	DevBuf perm;                      // leaf-order slot -> sorted index
 	DevBuf sort_hist, sort_tiles, sort_status;
-	DevBuf bounds;                    // centroid bounds (6 ordered words)
+	DevBuf bounds;                    // centroid bounds, 6 ordered words per scene
 	uint32_t *h_counters = nullptr;   // pinned mirror of `counters`
 	void release();
 };
 
-// Builds the 8-wide tree for n triangles at d_tris (n x 9 floats, device memory) into
-// `sc`.  compressed: also encode CNode8.  Synchronises `st`.  Returns PRT_* status;
-// on error `msg` says why.
+// Host-side tables of one build (kept alive until its uploads have been queued).
+struct BuildPlan {
+	uint32_t S = 0, n = 0, n_int = 0, node_cap = 0;
+	int leaf_size = 1, scene_digits = 0;
+	bool compressed = false, multi = false;
+	std::vector<uint32_t> toff, ioff; // triangle and binary-node offsets per scene
+};
+
+// Validates the offsets, reserves every buffer of the build and queues the uploads of
+// the offset tables on `st`.  Nothing after it allocates.
+int build_plan(const uint64_t *tri_off, uint32_t n_scenes, int leaf_size, bool compressed,
+               SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
+               std::string &msg);
+
+// Queues the build kernels.  host_checks: read the level counters every few levels and
+// finish with build_finish (synchronises).  Without host checks nothing synchronises:
+// all 32 collapse levels are queued (empty ones return at once) and the compression
+// kernel reads the node count on the device, so the whole build can be captured in a
+// CUDA graph; call build_finish after it ran to learn the node count and depth.
+int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
+                  cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg);
+
+// Reads the build's counters (synchronises `st`): node count, depth, placement check.
+int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg);
+
+// Builds the 8-wide trees of the scenes [tri_off[s], tri_off[s+1]) of the triangles at
+// d_tris (n x 9 floats, device memory) into `sc`.  tri_off is host memory with
+// n_scenes + 1 entries (tri_off[0] = 0).  compressed: also encode CNode8.
+// Synchronises `st` (a few times, never per tree level).  Returns PRT_* status.
+int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
+                 bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
+                 uint32_t *d_err, std::string &msg);
+
+// One scene: build_scenes with tri_off = {0, n}.
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
                 BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg);
 

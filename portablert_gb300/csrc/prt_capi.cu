@@ -15,39 +15,14 @@
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
+#include "prt_ctx.cuh"
 #include "prt_traverse.cuh"
-
-struct prt_b200_ctx {
-	int device = 0;
-	int sms = 0;
-	cudaStream_t stream = nullptr;
-	std::mutex mu;
-	std::string err;
-	prt::SceneGPU scene;
-	bool scene_set = false;
-	prt::BuildScratch ws;
-	prt::DevBuf tris_in;
-	prt::DevBuf rays_buf, out_buf;
-	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters
-	uint32_t *h_err = nullptr;
-	int leaf_size = 1;
-	int node_format = PRT_NODES_FP32;
-	int block = 128;
-	bool count = false;
-	bool build_compressed = true;
-	double build_ms = 0.0;
-	unsigned long long visits[2] = {0, 0};
-
-	uint32_t *d_work() { return work.as<uint32_t>(); }
-	uint32_t *d_err() { return work.as<uint32_t>() + 1; }
-	unsigned long long *d_visits() {
-		return reinterpret_cast<unsigned long long *>(work.as<uint8_t>() + 16);
-	}
-};
 
 namespace {
 
 thread_local std::string g_create_error;
+
+using prt::layout_ok;
 
 int fail(prt_b200_ctx *ctx, int code, const std::string &msg) {
 	if (ctx)
@@ -74,40 +49,6 @@ bool cc_ok(int dev) {
 	if (cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev) != cudaSuccess)
 		return false;
 	return major == 10 && minor == 3;
-}
-
-// Validates a HitReg layout descriptor.
-bool layout_ok(uint32_t mask, uint32_t rec, const uint8_t *off, std::string &why) {
-	if (mask == 0 || mask > 31u) {
-		why = "field_mask must be a non-empty subset of PRT_FIELD_*";
-		return false;
-	}
-	if (rec < 4 || rec > 32 || rec % 4 != 0) {
-		why = "rec_size must be a multiple of 4 in [4, 32]";
-		return false;
-	}
-	if (!off) {
-		why = "offsets pointer is null";
-		return false;
-	}
-	struct F {
-		uint32_t bit;
-		int idx;
-		uint32_t size;
-	} fields[] = {{PRT_FIELD_UV, PRT_OFF_U, 4},      {PRT_FIELD_UV, PRT_OFF_V, 4},
-	              {PRT_FIELD_T, PRT_OFF_T, 4},       {PRT_FIELD_PRIMITIVE_ID, PRT_OFF_PID, 4},
-	              {PRT_FIELD_VALID, PRT_OFF_VALID, 1}, {PRT_FIELD_P, PRT_OFF_PX, 4},
-	              {PRT_FIELD_P, PRT_OFF_PY, 4},      {PRT_FIELD_P, PRT_OFF_PZ, 4}};
-	for (const F &f : fields) {
-		if (!(mask & f.bit))
-			continue;
-		uint32_t o = off[f.idx];
-		if (o + f.size > rec || (f.size == 4 && o % 4 != 0)) {
-			why = "field offset out of range or misaligned";
-			return false;
-		}
-	}
-	return true;
 }
 
 int check_device_errors(prt_b200_ctx *ctx) {

@@ -47,21 +47,16 @@ constexpr int kChildPerLane = 8 / kLanesPerNode;
 constexpr int kMaxDepth = 32;
 
 struct TravArgs {
-	const float4 *tri4;
-	const uint32_t *inv;
-	const void *nodes;
-	const float *rays;
-	uint8_t *out;
-	uint32_t n_tris;
-	uint32_t n_nodes;
-	uint32_t n_rays;
-	uint32_t rec_size;
-	uint32_t mask;
-	uint32_t off[8];
-	uint32_t store_mode; // 0: 16-B stores, 1: 4-B stores, 2: byte stores
-	uint32_t pool_cap;   // entries of the pool (>= 256, it also holds the staged records)
-	uint32_t queue_cap;  // entries of the triangle queue
-	uint32_t warp_bytes; // shared memory per warp
+	const SceneDesc *scenes; // scene table (n_segs > 0)
+	const SegDesc *segs;     // segment table sorted by vbegin (n_segs > 0)
+	uint32_t n_segs;         // 0: one run, described by seg0 / scene0
+	uint32_t n_virtual;      // padded ray count
+	SceneDesc scene0;
+	SegDesc seg0;
+	uint32_t n_nodes;        // largest node array (bounds the steps of a batch)
+	uint32_t pool_cap;       // entries of the pool (>= 256, it also holds the staged records)
+	uint32_t queue_cap;      // entries of the triangle queue
+	uint32_t warp_bytes;     // shared memory per warp
 	uint32_t *counter;
 	uint32_t *err;
 	unsigned long long *visits;
@@ -72,6 +67,7 @@ struct WarpFixed {
 	unsigned long long key[32]; // best (t, primitive id) per slot
 	float ray[32][9];           // origin, direction, reciprocal per slot
 	int kind[32];
+	SegDesc seg;                // the run the current 32 rays belong to
 };
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t pool_cap, uint32_t queue_cap) {
@@ -109,14 +105,14 @@ __device__ __forceinline__ RayC slot_ray(const WarpFixed &S, uint32_t s) {
 
 // Tests queue entries [lo, lo + n) (n <= 32), one per lane.
 template <bool COUNT>
-__device__ __forceinline__ void test_queued(const TravArgs &a, WarpFixed &S,
+__device__ __forceinline__ void test_queued(const float4 *__restrict__ tri4, WarpFixed &S,
                                             const uint32_t *queue, uint32_t lo, uint32_t n,
                                             int lane, uint32_t &n_tests) {
 	if ((uint32_t)lane < n) {
 		const uint32_t e = queue[lo + lane];
 		const uint32_t slot = e >> kIndexBits;
 		const RayC r = slot_ray(S, slot);
-		const float4 *p = a.tri4 + 3 * (size_t)(e & kIndexMask);
+		const float4 *p = tri4 + 3 * (size_t)(e & kIndexMask);
 		const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
 		float t, u, v;
 		if (tri_test(r, A, B, C, t, u, v) && t < INFINITY)
@@ -128,16 +124,16 @@ __device__ __forceinline__ void test_queued(const TravArgs &a, WarpFixed &S,
 
 // Child `k` of `node`: slab test and what it refers to.
 template <int FMT>
-__device__ __forceinline__ void test_child(const TravArgs &a, const RayC &r, uint32_t node,
-                                           int k, bool &hit, bool &inner, uint32_t &child,
-                                           uint32_t &leaf_n) {
+__device__ __forceinline__ void test_child(const void *__restrict__ nodes, const RayC &r,
+                                           uint32_t node, int k, bool &hit, bool &inner,
+                                           uint32_t &child, uint32_t &leaf_n) {
 	hit = false;
 	inner = false;
 	child = 0;
 	leaf_n = 0;
 	if (FMT == PRT_NODES_FP32) {
 		const float4 *cp =
-		    reinterpret_cast<const float4 *>(&(static_cast<const Node8 *>(a.nodes) + node)->c[k]);
+		    reinterpret_cast<const float4 *>(&(static_cast<const Node8 *>(nodes) + node)->c[k]);
 		const float4 lo = __ldg(cp), hi = __ldg(cp + 1);
 		const uint32_t ref = __float_as_uint(lo.w);
 		if (ref != kNone) {
@@ -147,7 +143,7 @@ __device__ __forceinline__ void test_child(const TravArgs &a, const RayC &r, uin
 			leaf_n = inner ? 0u : leaf_count(ref);
 		}
 	} else {
-		const CNode8 *cn = static_cast<const CNode8 *>(a.nodes) + node;
+		const CNode8 *cn = static_cast<const CNode8 *>(nodes) + node;
 		const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
 		const uint2 w1 = __ldg(reinterpret_cast<const uint2 *>(cn) + 2);
 		const uint2 ck = __ldg(reinterpret_cast<const uint2 *>(&cn->c[k]));
@@ -178,7 +174,7 @@ __device__ __forceinline__ void test_child(const TravArgs &a, const RayC &r, uin
 }
 
 template <int FMT, bool COUNT>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_trace8(TravArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	unsigned char *wbase = smem_raw + (size_t)(threadIdx.x >> 5) * a.warp_bytes;
 	WarpFixed &S = *reinterpret_cast<WarpFixed *>(wbase);
@@ -196,12 +192,38 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 		if (lane == 0)
 			base = atomicAdd(a.counter, 32u);
 		base = __shfl_sync(0xFFFFFFFFu, base, 0);
-		if (base >= a.n_rays)
+		if (base >= a.n_virtual)
 			break;
-		const uint32_t nb = min(32u, a.n_rays - base);
+		// The run these 32 rays belong to (runs are padded to whole warps).
+		uint32_t si = 0;
+		if (a.n_segs) {
+			if (lane == 0) {
+				uint32_t lo_s = 0, hi_s = a.n_segs;
+				while (hi_s - lo_s > 1) {
+					const uint32_t mid = (lo_s + hi_s) >> 1;
+					if (a.segs[mid].vbegin <= base)
+						lo_s = mid;
+					else
+						hi_s = mid;
+				}
+				si = lo_s;
+			}
+			si = __shfl_sync(0xFFFFFFFFu, si, 0);
+		}
+		if (lane == 0)
+			S.seg = a.n_segs ? a.segs[si] : a.seg0;
+		__syncwarp();
+		const uint32_t local = base - (uint32_t)S.seg.vbegin;
+		const uint32_t run_rays = S.seg.n_rays;
+		if (local >= run_rays)
+			continue; // padding of the run
+		const uint32_t nb = min(32u, run_rays - local);
+		const SceneDesc sd = a.n_segs ? a.scenes[S.seg.scene] : a.scene0;
+		const float4 *__restrict__ tri4 = sd.tri4;
+		const void *__restrict__ nodes = sd.nodes;
 
 		if ((uint32_t)lane < nb) {
-			const float2 *rp = reinterpret_cast<const float2 *>(a.rays + 6 * (size_t)(base + lane));
+			const float2 *rp = reinterpret_cast<const float2 *>(S.seg.rays + 6 * (size_t)(local + lane));
 			const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
 			const RayC r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
 			float *sr = S.ray[lane];
@@ -213,7 +235,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 		S.key[lane] = kNoHit;
 		__syncwarp();
 
-		if (a.n_tris) {
+		if (sd.n_tris) {
 			uint32_t top = 0;  // items in the pool (warp-uniform)
 			uint32_t q = 0;    // queued triangles (warp-uniform)
 			uint32_t next = 0; // next slot whose root is not yet in the pool
@@ -223,7 +245,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 				if (top < (uint32_t)kItems && next < nb) {
 					const uint32_t add = min((uint32_t)kItems - top, nb - next);
 					if ((uint32_t)lane < add)
-						pool[top + lane] = (next + lane) << kIndexBits; // root = node 0
+						pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
 					top += add;
 					next += add;
 					__syncwarp();
@@ -256,7 +278,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 					child[j] = 0;
 					leaf_n[j] = 0;
 					if (work)
-						test_child<FMT>(a, r, node, s * kChildPerLane + j, hit[j], inner[j],
+						test_child<FMT>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
 						                child[j], leaf_n[j]);
 				}
 
@@ -323,22 +345,24 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 				__syncwarp();
 				while (q >= 32u) {
 					q -= 32u;
-					test_queued<COUNT>(a, S, queue, q, 32u, lane, n_tests);
+					test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
 					__syncwarp();
 				}
 			}
 			while (q > 0u) {
 				const uint32_t n = min(q, 32u);
 				q -= n;
-				test_queued<COUNT>(a, S, queue, q, n, lane, n_tests);
+				test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
 				__syncwarp();
 			}
 		}
 		__syncwarp();
 
-		// Finalise: recompute the winning triangle of each slot and stage the record.
+		// Finalise: recompute the winning triangle of each slot and stage the record in
+		// the run's HitReg<Tags...> layout.
 		uint32_t *stage = pool;
-		const uint32_t rw = a.rec_size >> 2;
+		const uint32_t rec = S.seg.rec_size, fmask = S.seg.mask;
+		const uint32_t rw = rec >> 2;
 		for (uint32_t w = 0; w < rw; ++w)
 			stage[lane * rw + w] = 0u;
 		__syncwarp();
@@ -349,7 +373,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 			const unsigned long long key = S.key[lane];
 			if (key != kNoHit) {
 				const uint32_t pid = (uint32_t)key;
-				const float4 *p = a.tri4 + 3 * (size_t)__ldg(&a.inv[pid]);
+				const float4 *p = tri4 + 3 * (size_t)__ldg(&sd.inv[pid]);
 				float t, u, v;
 				if (tri_test(r, __ldg(p), __ldg(p + 1), __ldg(p + 2), t, u, v)) {
 					best.t = t;
@@ -358,36 +382,38 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock) k_trace8(TravArgs a) {
 					best.pid = pid;
 				}
 			}
-			uint8_t *rb = reinterpret_cast<uint8_t *>(stage) + lane * a.rec_size;
-			if (a.mask & PRT_FIELD_UV) {
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_U]) = best.u;
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_V]) = best.v;
+			const uint8_t *off = S.seg.off;
+			uint8_t *rb = reinterpret_cast<uint8_t *>(stage) + lane * rec;
+			if (fmask & PRT_FIELD_UV) {
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_U]) = best.u;
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_V]) = best.v;
 			}
-			if (a.mask & PRT_FIELD_T)
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_T]) = best.t;
-			if (a.mask & PRT_FIELD_PRIMITIVE_ID)
-				*reinterpret_cast<uint32_t *>(rb + a.off[PRT_OFF_PID]) = best.pid;
-			if (a.mask & PRT_FIELD_VALID)
-				rb[a.off[PRT_OFF_VALID]] = best.t < INFINITY ? 1 : 0;
-			if (a.mask & PRT_FIELD_P) {
+			if (fmask & PRT_FIELD_T)
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_T]) = best.t;
+			if (fmask & PRT_FIELD_PRIMITIVE_ID)
+				*reinterpret_cast<uint32_t *>(rb + off[PRT_OFF_PID]) = best.pid;
+			if (fmask & PRT_FIELD_VALID)
+				rb[off[PRT_OFF_VALID]] = best.t < INFINITY ? 1 : 0;
+			if (fmask & PRT_FIELD_P) {
 				// bvh.hpp:261-263: p = origin + t * direction, per component.
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_PX]) =
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_PX]) =
 				    __fadd_rn(r.ox, __fmul_rn(best.t, r.dx));
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_PY]) =
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_PY]) =
 				    __fadd_rn(r.oy, __fmul_rn(best.t, r.dy));
-				*reinterpret_cast<float *>(rb + a.off[PRT_OFF_PZ]) =
+				*reinterpret_cast<float *>(rb + off[PRT_OFF_PZ]) =
 				    __fadd_rn(r.oz, __fmul_rn(best.t, r.dz));
 			}
 		}
 		__syncwarp();
-		uint8_t *dst = a.out + (size_t)base * a.rec_size;
-		const uint32_t bytes = nb * a.rec_size;
-		if (a.store_mode == 0 && nb == 32u) {
+		uint8_t *dst = S.seg.out + (size_t)local * rec;
+		const uint32_t bytes = nb * rec;
+		const uint32_t mode = S.seg.store_mode;
+		if (mode == 0 && nb == 32u) {
 			uint4 *d4 = reinterpret_cast<uint4 *>(dst);
 			const uint4 *s4 = reinterpret_cast<const uint4 *>(stage);
 			for (uint32_t k = lane; k < bytes / 16u; k += 32u)
 				__stcs(d4 + k, s4[k]);
-		} else if (a.store_mode <= 1) {
+		} else if (mode <= 1) {
 			uint32_t *d1 = reinterpret_cast<uint32_t *>(dst);
 			for (uint32_t k = lane; k < bytes / 4u; k += 32u)
 				d1[k] = stage[k];
@@ -432,10 +458,42 @@ template <int FMT, bool COUNT> int blocks_per_sm(int warps, uint32_t warp_bytes)
 template <int FMT, bool COUNT>
 void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
 	const int bps = blocks_per_sm<FMT, COUNT>(warps, a.warp_bytes);
-	const uint64_t warps_needed = (a.n_rays + 31ull) / 32ull;
+	const uint64_t warps_needed = (a.n_virtual + 31ull) / 32ull;
 	const uint64_t need = (warps_needed + warps - 1) / warps;
 	const uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
 	k_trace8<FMT, COUNT><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(a);
+}
+
+void size_smem(TravArgs &a, uint32_t depth, int leaf_size) {
+	depth = std::max<uint32_t>(depth, 1u);
+	a.pool_cap = std::max<uint32_t>(256u, 7u * kItems * (depth - 1u) + 2u * kItems);
+	a.queue_cap = 32u + (uint32_t)kItems * 8u * (uint32_t)std::max(leaf_size, 1);
+	a.warp_bytes = (warp_smem_bytes(a.pool_cap, a.queue_cap) + 15u) & ~15u;
+}
+
+int warps_for(const TravConfig &cfg) {
+	return (cfg.block >= 32 && cfg.block <= 32 * kWarpsPerBlock && cfg.block % 32 == 0)
+	           ? cfg.block / 32
+	           : kWarpsPerBlock;
+}
+
+cudaError_t dispatch(const TravArgs &a, const TravConfig &cfg, int sm_count, cudaStream_t st) {
+	cudaError_t e = cudaMemsetAsync(a.counter, 0, 4, st);
+	if (e != cudaSuccess)
+		return e;
+	const int warps = warps_for(cfg);
+	if (cfg.format == PRT_NODES_COMPRESSED) {
+		if (cfg.count)
+			launch<PRT_NODES_COMPRESSED, true>(a, warps, sm_count, st);
+		else
+			launch<PRT_NODES_COMPRESSED, false>(a, warps, sm_count, st);
+	} else {
+		if (cfg.count)
+			launch<PRT_NODES_FP32, true>(a, warps, sm_count, st);
+		else
+			launch<PRT_NODES_FP32, false>(a, warps, sm_count, st);
+	}
+	return cudaGetLastError();
 }
 
 } // namespace
@@ -449,55 +507,65 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 	if (cfg.count)
 		cudaMemsetAsync(d_visits, 0, 2 * sizeof(unsigned long long), st);
 	const uint64_t chunk = 1ull << 31;
-	const int warps = (cfg.block >= 32 && cfg.block <= 32 * kWarpsPerBlock && cfg.block % 32 == 0)
-	                      ? cfg.block / 32
-	                      : kWarpsPerBlock;
-	const uint32_t depth = std::max<uint32_t>(sc.depth, 1u);
-	const uint32_t pool_cap =
-	    std::max<uint32_t>(256u, 7u * kItems * (depth - 1u) + 2u * kItems);
-	const uint32_t queue_cap = 32u + (uint32_t)kItems * 8u * (uint32_t)std::max(sc.leaf_size, 1);
 	for (uint64_t s = 0; s < n; s += chunk) {
 		const uint64_t m = std::min(chunk, n - s);
 		TravArgs a;
-		a.tri4 = sc.tri4.as<float4>();
-		a.inv = sc.inv.as<uint32_t>();
-		a.nodes = cfg.format == PRT_NODES_COMPRESSED ? sc.cnodes.p : sc.nodes.p;
-		a.rays = d_rays + 6 * s;
-		a.out = static_cast<uint8_t *>(d_out) + s * lay.rec_size;
-		a.n_tris = (uint32_t)sc.n_tris;
-		a.n_nodes = sc.n_nodes;
-		a.n_rays = (uint32_t)m;
-		a.rec_size = lay.rec_size;
-		a.mask = lay.mask;
+		a.scenes = nullptr;
+		a.segs = nullptr;
+		a.n_segs = 0;
+		a.n_virtual = (uint32_t)m;
+		a.scene0.tri4 = sc.tri4.as<float4>();
+		a.scene0.inv = sc.inv.as<uint32_t>();
+		a.scene0.nodes = cfg.format == PRT_NODES_COMPRESSED ? sc.cnodes.p : sc.nodes.p;
+		a.scene0.root = 0;
+		a.scene0.n_tris = (uint32_t)sc.n_tris;
+		a.seg0.vbegin = 0;
+		a.seg0.rays = d_rays + 6 * s;
+		a.seg0.out = static_cast<uint8_t *>(d_out) + s * lay.rec_size;
+		a.seg0.n_rays = (uint32_t)m;
+		a.seg0.scene = 0;
+		a.seg0.mask = lay.mask;
+		a.seg0.rec_size = lay.rec_size;
 		for (int k = 0; k < 8; ++k)
-			a.off[k] = lay.off[k];
-		const uintptr_t addr = reinterpret_cast<uintptr_t>(a.out);
-		a.store_mode = (addr % 16 == 0) ? 0u : ((addr % 4 == 0) ? 1u : 2u);
-		a.pool_cap = pool_cap;
-		a.queue_cap = queue_cap;
-		a.warp_bytes = (warp_smem_bytes(pool_cap, queue_cap) + 15u) & ~15u;
+			a.seg0.off[k] = lay.off[k];
+		a.seg0.store_mode = store_mode_for(a.seg0.out);
+		a.seg0.pad = 0;
+		a.n_nodes = sc.n_nodes;
+		size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : sc.depth, sc.leaf_size);
 		a.counter = d_work;
 		a.err = d_err;
 		a.visits = d_visits;
-		cudaError_t e = cudaMemsetAsync(d_work, 0, 4, st);
-		if (e != cudaSuccess)
-			return e;
-		if (cfg.format == PRT_NODES_COMPRESSED) {
-			if (cfg.count)
-				launch<PRT_NODES_COMPRESSED, true>(a, warps, sm_count, st);
-			else
-				launch<PRT_NODES_COMPRESSED, false>(a, warps, sm_count, st);
-		} else {
-			if (cfg.count)
-				launch<PRT_NODES_FP32, true>(a, warps, sm_count, st);
-			else
-				launch<PRT_NODES_FP32, false>(a, warps, sm_count, st);
-		}
-		e = cudaGetLastError();
+		cudaError_t e = dispatch(a, cfg, sm_count, st);
 		if (e != cudaSuccess)
 			return e;
 	}
 	return cudaSuccess;
+}
+
+cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDesc *d_segs,
+                                         uint32_t n_segs, unsigned long long n_virtual,
+                                         uint32_t depth, int leaf_size, uint32_t n_nodes,
+                                         const TravConfig &cfg, uint32_t *d_work,
+                                         unsigned long long *d_visits, uint32_t *d_err,
+                                         cudaStream_t st, int sm_count) {
+	if (cfg.count)
+		cudaMemsetAsync(d_visits, 0, 2 * sizeof(unsigned long long), st);
+	if (n_segs == 0 || n_virtual == 0)
+		return cudaSuccess;
+	if (n_virtual > (1ull << 31))
+		return cudaErrorInvalidValue;
+	TravArgs a;
+	memset(&a, 0, sizeof a);
+	a.scenes = d_scenes;
+	a.segs = d_segs;
+	a.n_segs = n_segs;
+	a.n_virtual = (uint32_t)n_virtual;
+	a.n_nodes = n_nodes;
+	size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : depth, leaf_size);
+	a.counter = d_work;
+	a.err = d_err;
+	a.visits = d_visits;
+	return dispatch(a, cfg, sm_count, st);
 }
 
 } // namespace prt

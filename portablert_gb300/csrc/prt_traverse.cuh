@@ -10,7 +10,7 @@ namespace prt {
 
 struct OutLayout {
 	uint32_t mask;      // PRT_FIELD_* bits
-	uint32_t rec_size;  // bytes per record, 1..32
+	uint32_t rec_size;  // bytes per record, 4..32
 	uint8_t off[8];     // u, v, t, primitive_id, valid, px, py, pz
 };
 
@@ -18,17 +18,61 @@ struct TravConfig {
 	int format = 0;       // PRT_NODES_FP32 / PRT_NODES_COMPRESSED
 	int block = 128;      // threads per block
 	bool count = false;   // accumulate visit counters into d_visits[0..1]
+	int pool_depth = 0;   // size the pool for this depth instead of the scene's (0 = scene)
 };
 
-// Levels of the 8-wide tree the traversal stack can hold.
+// One scene as the traversal sees it: its arrays, root node and triangle count.
+struct SceneDesc {
+	const float4 *tri4;
+	const uint32_t *inv; // primitive id -> tri4 position for this scene
+	const void *nodes;   // Node8 or CNode8 array holding the scene's tree
+	uint32_t root;
+	uint32_t n_tris;
+};
+
+// A run of rays of one scene and where their records go.  vbegin (a multiple of 32) is
+// the first index of the run in the launch's "virtual" ray numbering, in which every
+// run is padded to whole warps, so a warp's 32 rays never mix runs.
+struct SegDesc {
+	unsigned long long vbegin;
+	const float *rays;   // n_rays x 6 floats, device memory
+	uint8_t *out;        // n_rays records of rec_size bytes, device memory
+	uint32_t n_rays;
+	uint32_t scene;      // index into the scene table
+	uint32_t mask;
+	uint32_t rec_size;
+	uint8_t off[8];
+	uint32_t store_mode; // 0: 16-B stores, 1: 4-B stores, 2: byte stores
+	uint32_t pad;
+};
+
+// Levels of the 8-wide tree the traversal can walk.
 int traversal_stack_depth();
 
-// Queues one nearest-hit pass over n rays (device memory, 6 floats each) on `st`.
-// d_work: 16 bytes of device scratch (ray counter); d_visits: 2 uint64 counters
-// (node visits, triangle tests), used when cfg.count.
+// Queues one nearest-hit pass over n rays of one scene (device memory, 6 floats each)
+// on `st`.  d_work: device scratch (ray counter); d_visits: 2 uint64 counters (node
+// visits, triangle tests), used when cfg.count.
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
                                 uint32_t *d_work, unsigned long long *d_visits, uint32_t *d_err,
                                 cudaStream_t st, int sm_count);
+
+// One persistent launch over several runs of rays, each against its own scene and with
+// its own output layout.  d_scenes / d_segs: device copies of the tables (segments
+// sorted by vbegin); n_virtual: the padded ray count (end of the last run).  depth and
+// leaf_size: the largest over the scenes (they size the shared-memory pool and queue);
+// n_nodes: the largest node array (bounds the steps of a batch).
+cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDesc *d_segs,
+                                         uint32_t n_segs, unsigned long long n_virtual,
+                                         uint32_t depth, int leaf_size, uint32_t n_nodes,
+                                         const TravConfig &cfg, uint32_t *d_work,
+                                         unsigned long long *d_visits, uint32_t *d_err,
+                                         cudaStream_t st, int sm_count);
+
+// Store mode for an output pointer (16-byte, 4-byte or byte stores).
+inline uint32_t store_mode_for(const void *p) {
+	const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+	return (a % 16 == 0) ? 0u : ((a % 4 == 0) ? 1u : 2u);
+}
 
 } // namespace prt

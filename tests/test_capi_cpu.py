@@ -61,6 +61,24 @@ def test_null_context_is_an_argument_error(lib):
     assert lib.prt_b200_set_option(None, b"leaf_size", 4) == 1
 
 
+def test_query_struct_layout_matches_header(tmp_path):
+    src = tmp_path / "q.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "prt_b200.h"\n'
+        'int main(void) { printf("%zu %zu %zu %zu %zu %zu\\n", sizeof(prt_b200_query),'
+        ' offsetof(prt_b200_query, rays), offsetof(prt_b200_query, n_rays),'
+        ' offsetof(prt_b200_query, out), offsetof(prt_b200_query, rec_size),'
+        ' offsetof(prt_b200_query, offs)); return 0; }\n')
+    exe = tmp_path / "q"
+    subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)],
+                   check=True)
+    c_side = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True,
+                                             check=True).stdout.split()]
+    Q = _lib.Query
+    assert c_side == [ctypes.sizeof(Q), Q.rays.offset, Q.n_rays.offset, Q.out.offset,
+                      Q.rec_size.offset, Q.offs.offset]
+
+
 def test_cpp_api_compiles_and_links():
     exe = build.build_cpp_test()
     assert os.path.exists(exe)
