@@ -631,12 +631,19 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	plan.multi = S > 1;
 	plan.toff.resize(S + 1);
 	plan.ioff.resize(S + 1);
+	for (uint32_t s = 0; s <= S; ++s)
+		plan.toff[s] = (uint32_t)tri_off64[s];
 	plan.n_int = 0;
 	for (uint32_t s = 0; s <= S; ++s) {
-		plan.toff[s] = (uint32_t)tri_off64[s];
 		plan.ioff[s] = plan.n_int;
-		if (s < S)
-			plan.n_int += plan.toff[s + 1] - plan.toff[s] > 1 ? plan.toff[s + 1] - plan.toff[s] - 1 : 0;
+		if (s < S) {
+			const uint32_t ns = plan.toff[s + 1] - plan.toff[s];
+			plan.n_int += ns > 1 ? ns - 1 : 0;
+		}
+	}
+	if (plan.n_int >= std::max<uint32_t>(plan.toff[S], 1u)) {
+		msg = "build: inconsistent scene offsets";
+		return PRT_ERR_ARG;
 	}
 	plan.scene_digits = 0;
 	for (uint32_t v = S - 1; v; v >>= 8)

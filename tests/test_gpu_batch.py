@@ -18,6 +18,13 @@ def _torch():
     return torch
 
 
+def _dev(torch, a):
+    """Device copy of a numpy array, finished before the library's stream reads it."""
+    t = torch.from_numpy(a).cuda()
+    torch.cuda.synchronize()
+    return t
+
+
 def _scenes(seed, sizes, n_rays):
     tris = [workloads.soup_tris(seed + s, n) for s, n in enumerate(sizes)]
     rays = [workloads.soup_rays(seed + s, m) for s, m in enumerate(n_rays)]
@@ -31,10 +38,11 @@ def _queries(torch, rays, tagsets):
     for s, r in enumerate(rays):
         tags = tagsets[s % len(tagsets)]
         lay = hitreg.layout(tags)
-        d_r = torch.from_numpy(r).cuda()
+        d_r = _dev(torch, r)
         d_o = torch.zeros(max(len(r), 1) * lay.size, dtype=torch.uint8, device="cuda")
         qs.append(make_query(s, d_r.data_ptr(), len(r), d_o.data_ptr(), tags))
         keep.append((d_r, d_o, tags, lay))
+    torch.cuda.synchronize()
     return qs, keep
 
 
@@ -58,7 +66,7 @@ def test_batch_matches_each_scene_alone(gpu_backend):
     n_rays = [50, 100, 1000, 31, 32, 33, 5000, 64, 2048, 999]
     tris, rays = _scenes(100, sizes, n_rays)
     off = np.cumsum([0] + sizes)
-    d_tris = torch.from_numpy(np.concatenate(tris)).cuda()
+    d_tris = _dev(torch, np.concatenate(tris))
     b = Batch(gpu_backend)
     try:
         b.set_tris_dev(d_tris.data_ptr(), off)
@@ -81,7 +89,7 @@ def test_batch_graph_replay_matches(gpu_backend, fmt):
     n_rays = list(workloads.batch_sizes(40, seed=9, tri_range=(16, 4000), ray_range=(64, 3000))[1])
     tris, rays = _scenes(300, sizes, n_rays)
     off = np.cumsum([0] + sizes)
-    d_tris = torch.from_numpy(np.concatenate(tris)).cuda()
+    d_tris = _dev(torch, np.concatenate(tris))
     gpu_backend.set_option("node_format", fmt)
     b = Batch(gpu_backend)
     try:
@@ -89,6 +97,7 @@ def test_batch_graph_replay_matches(gpu_backend, fmt):
         for _ in range(2):  # capture + launch, then replay
             for _, d_o, _, _ in keep:
                 d_o.zero_()
+            torch.cuda.synchronize()
             b.run_graph(d_tris.data_ptr(), off, qs)
             b.sync()
             torch.cuda.synchronize()
@@ -97,6 +106,7 @@ def test_batch_graph_replay_matches(gpu_backend, fmt):
         # the graph-built arena answers direct queries too
         for _, d_o, _, _ in keep:
             d_o.zero_()
+        torch.cuda.synchronize()
         b.query_dev(qs)
         b.sync()
         torch.cuda.synchronize()
@@ -114,12 +124,13 @@ def test_batch_of_many_small_scenes_vs_oracle(gpu_backend, oracle_lib):
     tris = [workloads.soup_tris(1000 + s, int(n)) for s, n in enumerate(tri_n)]
     rays = [workloads.soup_rays(1000 + s, int(m)) for s, m in enumerate(ray_n)]
     off = np.cumsum([0] + [len(t) for t in tris])
-    d_tris = torch.from_numpy(np.concatenate(tris)).cuda()
+    d_tris = _dev(torch, np.concatenate(tris))
     all_rays = np.concatenate(rays)
-    d_rays = torch.from_numpy(all_rays).cuda()
+    d_rays = _dev(torch, all_rays)
     roff = np.cumsum([0] + [len(r) for r in rays])
     lay = hitreg.layout(hitreg.TAGS)
     d_out = torch.zeros(len(all_rays) * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
     qs = [make_query(s, d_rays.data_ptr() + 24 * int(roff[s]), len(rays[s]),
                      d_out.data_ptr() + lay.size * int(roff[s]), hitreg.TAGS)
           for s in range(len(tris))]
