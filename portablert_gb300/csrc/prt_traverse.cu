@@ -63,12 +63,15 @@ struct TravArgs {
 };
 
 // Per-warp shared memory: fixed part, then the queue and the pool (sizes per launch).
-struct WarpFixed {
+// alignas(16): the queue follows this part and the pool after it doubles as the staging
+// area of the output records, which is read with 16-byte vector loads.
+struct alignas(16) WarpFixed {
 	unsigned long long key[32]; // best (t, primitive id) per slot
 	float ray[32][9];           // origin, direction, reciprocal per slot
 	int kind[32];
 	SegDesc seg;                // the run the current 32 rays belong to
 };
+static_assert(sizeof(WarpFixed) % 16 == 0, "queue and pool must start 16-byte aligned");
 
 __host__ __device__ inline uint32_t warp_smem_bytes(uint32_t pool_cap, uint32_t queue_cap) {
 	return (uint32_t)sizeof(WarpFixed) + 4u * (queue_cap + pool_cap);
