@@ -53,6 +53,9 @@ int bcuda(prt_b200_ctx *ctx, cudaError_t e, const char *what) {
 struct prt_b200_batch {
 	prt_b200_ctx *ctx = nullptr;
 	prt::SceneGPU arena;
+	// The batch's own build scratch: a captured graph reads tables uploaded before the
+	// capture, so nothing outside the batch may overwrite them between replays.
+	prt::BuildScratch ws;
 	bool built = false;
 	prt::DevBuf scenes_fp32, scenes_comp; // SceneDesc[S] for each node format
 	Slot slots[kSlots];
@@ -253,6 +256,7 @@ void prt_b200_batch_destroy(prt_b200_batch *b) {
 				cudaEventDestroy(b->slots[i].done);
 		}
 		b->arena.release();
+		b->ws.release();
 		b->scenes_fp32.release();
 		b->scenes_comp.release();
 		if (b->h_words)
@@ -283,7 +287,7 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 	cudaEventRecord(e0, ctx->stream);
 	std::string msg;
 	int rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-	                           b->arena, ctx->ws, ctx->stream, ctx->d_err(), msg);
+	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg);
 	cudaEventRecord(e1, ctx->stream);
 	cudaEventSynchronize(e1);
 	float ms = 0.0f;
@@ -362,7 +366,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 		std::string msg;
 		// Plan: reserve everything and upload the offset tables outside the graph.
 		rc = prt::build_plan(tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed, b->arena,
-		                     ctx->ws, ctx->stream, b->gplan, msg);
+		                     b->ws, ctx->stream, b->gplan, msg);
 		if (rc != PRT_OK)
 			return bfail(ctx, rc, msg);
 		b->arena.has_cnodes = ctx->build_compressed;
@@ -383,7 +387,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 		B_TRY(ctx, cudaStreamSynchronize(ctx->stream));
 		// Capture: the whole build (no host round-trips) and the query launch.
 		B_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-		rc = prt::build_enqueue(d_tris, b->gplan, b->arena, ctx->ws, ctx->stream, ctx->d_err(),
+		rc = prt::build_enqueue(d_tris, b->gplan, b->arena, b->ws, ctx->stream, ctx->d_err(),
 		                        false, msg);
 		if (rc == PRT_OK && !segs.empty())
 			rc = launch_query(b, b->gslot, segs, n_virtual, prt::traversal_stack_depth(),
@@ -433,7 +437,7 @@ int prt_b200_batch_sync(prt_b200_batch *b) {
 		return rc;
 	if (b->graph_dirty) {
 		std::string msg;
-		rc = prt::build_finish(b->arena, ctx->ws, ctx->stream, msg);
+		rc = prt::build_finish(b->arena, b->ws, ctx->stream, msg);
 		if (rc != PRT_OK)
 			return bfail(ctx, rc, msg);
 		uint32_t err_word = 0;

@@ -280,15 +280,21 @@ __device__ __forceinline__ void child_box(uint32_t ref, const float4 *ibox, cons
 // thread to arrive stops and the second, which then sees both children's boxes, writes
 // the union and continues.  No thread waits on another.  A scene of one triangle has
 // no binary node (parent_leaf stays kNone).
-__global__ void k_refit(uint32_t n, const uint32_t *__restrict__ parent_leaf,
+__global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__ parent_leaf,
                         const uint32_t *__restrict__ parent_int, const uint32_t *__restrict__ left,
                         const uint32_t *__restrict__ right, const float4 *lbox, float4 *ibox,
-                        uint32_t *flags) {
+                        uint32_t *flags, uint32_t *err) {
 	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n)
 		return;
 	uint32_t p = parent_leaf[i];
-	while (p != kNone) {
+	// A path to the root passes each binary node once; a longer walk (or an index out
+	// of range) means corrupt parents, reported instead of followed.
+	for (uint32_t steps = 0; p != kNone; ++steps) {
+		if (p >= n_int || steps >= n_int) {
+			atomicOr(err, kErrCollapse);
+			return;
+		}
 		__threadfence();
 		if (atomicAdd(&flags[p], 1u) == 0u)
 			return;
@@ -758,9 +764,9 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 		k_leaf_boxes<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, svals, n, ws.lbox.as<float4>());
 		if (n_int)
 			k_refit<<<blocks_for(n, 256), 256, 0, st>>>(
-			    n, ws.parent_leaf.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
+			    n, n_int, ws.parent_leaf.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
 			    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.lbox.as<float4>(),
-			    ws.ibox.as<float4>(), ws.flags.as<uint32_t>());
+			    ws.ibox.as<float4>(), ws.flags.as<uint32_t>(), d_err);
 	}
 
 	uint32_t *ctr = ws.counters.as<uint32_t>();
