@@ -197,6 +197,154 @@ def run_reference(args, world, rank):
     print(json.dumps(out), flush=True)
 
 
+# --------------------------------------------------------------------------- other configs
+
+C0_TAGS = ("uv", "t", "primitive_id", "valid")
+
+
+def _events(torch, stream, fn, reps):
+    ms = []
+    for _ in range(reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    return ms
+
+
+def leg_batch(b, stream, steps, n_scenes=4096, log=None):
+    """4,096 soup scenes (triangles log-uniform in [16, 65536], rays log-uniform in
+    [64, 262144], seeds 1000+s, tags uv/t/primitive_id/valid) built and queried as one
+    CUDA graph with the autotuned knobs and compressed nodes, beside the same batch
+    with FP32 nodes and the plain per-scene path (set_tris + nearest_hits per scene,
+    FP32).  Inputs (1.2 GB triangles, 3.2 GB rays) exceed L2, so no flush is needed."""
+    import torch
+
+    from portablert_gb300 import autotune, _lib
+    from portablert_gb300.batch import Batch, make_query
+
+    tri_n, ray_n = workloads.batch_sizes(n_scenes, seed=3)
+    toff = np.concatenate([[0], np.cumsum(tri_n)]).astype(np.uint64)
+    roff = np.concatenate([[0], np.cumsum(ray_n)]).astype(np.int64)
+    T, R = int(toff[-1]), int(roff[-1])
+    lay = hitreg.layout(C0_TAGS)
+    d_tris = torch.empty(T * 9, dtype=torch.float32, device="cuda")
+    d_rays = torch.empty(R * 6, dtype=torch.float32, device="cuda")
+    d_out = torch.zeros(R * lay.size, dtype=torch.uint8, device="cuda")
+    d_plain = torch.zeros(R * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    tp, rp, op = d_tris.data_ptr(), d_rays.data_ptr(), d_out.data_ptr()
+    for s in range(n_scenes):
+        workloads.generate_dev(b, workloads.GEN_SOUP_TRIS, 1000 + s, int(tri_n[s]),
+                               tp + 36 * int(toff[s]))
+        workloads.generate_dev(b, workloads.GEN_SOUP_RAYS, 1000 + s, int(ray_n[s]),
+                               rp + 24 * int(roff[s]))
+    b.sync()
+    qs = [make_query(s, rp + 24 * int(roff[s]), int(ray_n[s]), op + lay.size * int(roff[s]),
+                     C0_TAGS) for s in range(n_scenes)]
+    qarr = (_lib.Query * n_scenes)(*qs)
+    res = {"workload": f"{n_scenes} soup scenes, {T:,} tris, {R:,} rays (log-uniform sizes); "
+                       "tags uv, t, primitive_id, valid (20 B records)",
+           "n_scenes": n_scenes, "n_tris": T, "n_rays": R}
+    out = {}
+    for name, fmts in (("compressed", (1,)), ("fp32", (0,))):
+        tuned = autotune.tune_batch(b, tp, toff, qarr, stream=stream, formats=fmts, reps=2,
+                                    log=log)
+        bt = Batch(b)
+        try:
+            graph_ms = autotune.time_graph(bt, b, tp, toff, qarr, stream, max(3, steps))
+            q_ms = _events(torch, stream, lambda: bt.query_dev(qarr, stream.cuda_stream),
+                           max(3, steps))
+            bt.sync()
+            depth, nodes = bt.stat("depth"), bt.stat("n_nodes")
+        finally:
+            bt.close()
+        g, q = float(np.median(graph_ms)), float(np.median(q_ms))
+        out[name] = {"graph_ms": g, "query_ms": q, "build_ms": g - q,
+                     "mrays_s_graph": R / g / 1e3, "mrays_s_query": R / q / 1e3,
+                     "mtris_s_build": T / max(g - q, 1e-6) / 1e3, "depth": depth,
+                     "nodes": nodes, "autotuned": tuned["config"],
+                     "autotune_cached": tuned["cached"],
+                     "autotune_tried": len(tuned.get("tried", []))}
+        if name == "compressed":
+            torch.cuda.synchronize()
+            batched = d_out.clone()
+    # The plain path: one scene at a time through set_tris_dev + nearest_hits_dev (FP32,
+    # default options), timed on the host clock around the whole loop.
+    autotune.apply(b, {"node_format": 0, "leaf_size": 1, "block": 128, "pool_depth": 0})
+    b.set_option("build_compressed", 1)
+    pp = d_plain.data_ptr()
+    t0 = time.perf_counter()
+    for s in range(n_scenes):
+        b.set_tris_dev(tp + 36 * int(toff[s]), int(tri_n[s]))
+        b.nearest_hits_dev(rp + 24 * int(roff[s]), int(ray_n[s]), pp + lay.size * int(roff[s]),
+                           C0_TAGS, stream.cuda_stream)
+    b.sync()
+    torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    out["plain_per_scene"] = {"ms": 1e3 * plain_s, "mrays_s": R / plain_s / 1e6,
+                              "mtris_s_with_queries": T / plain_s / 1e6}
+    res.update(out)
+    # Records of the compressed graph and of the FP32 graph against the plain path's.
+    res["identical"] = {"compressed_graph_vs_plain": bool(torch.equal(batched, d_plain)),
+                        "fp32_graph_vs_plain": bool(torch.equal(d_out, d_plain))}
+    res["speedup_vs_plain_per_scene"] = (out["compressed"]["mrays_s_graph"] /
+                                         out["plain_per_scene"]["mrays_s"])
+    res["speedup_vs_fp32_batched"] = (out["compressed"]["mrays_s_graph"] /
+                                      out["fp32"]["mrays_s_graph"])
+    del d_tris, d_rays, d_out, d_plain, batched
+    torch.cuda.empty_cache()
+    return res
+
+
+def leg_precision(b, stream, steps):
+    """The clustered soup: 8,388,608 tris in 256 Gaussian clusters, 16,777,216 random
+    rays, tags uv/t/primitive_id/valid; FP32 against compressed nodes (records must be
+    byte-identical) and the FP64 t error of the answers."""
+    import torch
+
+    n_t, n_r = 8_388_608, 16_777_216
+    lay = hitreg.layout(C0_TAGS)
+    d_t = torch.empty(n_t * 9, dtype=torch.float32, device="cuda")
+    d_r = torch.empty(n_r * 6, dtype=torch.float32, device="cuda")
+    outs = [torch.zeros(n_r * lay.size, dtype=torch.uint8, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    workloads.generate_dev(b, workloads.GEN_CLUSTER_TRIS, 2, n_t, d_t.data_ptr(), 256)
+    workloads.generate_dev(b, workloads.GEN_RANDOM_RAYS, 2, n_r, d_r.data_ptr(), 12.0)
+    b.sync()
+    bms = []
+    for _ in range(3):
+        b.set_tris_dev(d_t.data_ptr(), n_t)
+        bms.append(b.stat("build_ms"))
+    res = {"workload": f"clustered soup {n_t:,} tris (256 clusters), {n_r:,} random rays; "
+                       "tags uv, t, primitive_id, valid", "n_tris": n_t, "n_rays": n_r,
+           "build_ms": float(np.median(bms)),
+           "build_mtris_s": n_t / float(np.median(bms)) / 1e3}
+    for fmt, name in ((0, "fp32"), (1, "compressed")):
+        b.set_option("node_format", fmt)
+        o = outs[fmt]
+        step = lambda: b.nearest_hits_dev(d_r.data_ptr(), n_r, o.data_ptr(), C0_TAGS,
+                                          stream.cuda_stream)
+        for _ in range(2):
+            step()
+        b.sync()
+        ms = _events(torch, stream, step, max(3, steps))
+        b.sync()
+        res[name] = {"mrays_s": n_r / float(np.median(ms)) / 1e3, "ms": float(np.median(ms)),
+                     "node_bytes": b.stat("node_size")}
+    b.set_option("node_format", 0)
+    res["identical"] = bool(torch.equal(outs[0], outs[1]))
+    sc = b.t_error(d_t.data_ptr(), n_t, d_r.data_ptr(), n_r, outs[0].data_ptr(), C0_TAGS)
+    res["t_error_vs_fp64"] = sc
+    res["compressed_over_fp32"] = res["compressed"]["mrays_s"] / res["fp32"]["mrays_s"]
+    del d_t, d_r, outs
+    torch.cuda.empty_cache()
+    return res
+
+
 # --------------------------------------------------------------------------- GPU side
 
 def run_gpu(args, world, rank):
@@ -342,6 +490,14 @@ def run_gpu(args, world, rank):
            "compressed": {"value": world * n * args.steps / (comp_ms / 1e3) / 1e6,
                           "unit": "Mrays/s", "node_bytes": comp_node_size},
            "clocks": clk}
+    del d_rays, d_out, flush
+    torch.cuda.empty_cache()
+    legs = set(args.legs.split(",")) if args.legs else set()
+    log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
+    if "precision" in legs:
+        out["precision"] = leg_precision(b, stream, min(args.steps, 10))
+    if "batch" in legs:
+        out["batch"] = leg_batch(b, stream, min(args.steps, 10), log=log)
     if rank == 0 and not args.no_cpu:
         _, cb = cpu_baseline(tris, rays, sample_rays=131_072)
         out["cpu_baseline"] = cb
@@ -357,6 +513,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="b200", choices=["b200", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--legs", default="precision,batch",
+                    help="other configurations to measure: precision, batch (comma list)")
+    ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -56,7 +56,7 @@ enum {
 
 /* Acceleration-structure node formats (option "node_format"). */
 #define PRT_NODES_FP32 0       /* 8-wide nodes, FP32 child boxes (224 B) */
-#define PRT_NODES_COMPRESSED 1 /* 8-wide nodes, 8-bit child boxes rounded outward (80 B) */
+#define PRT_NODES_COMPRESSED 1 /* 8-wide nodes, 8-bit child boxes rounded outward (96 B) */
 
 /* Replaces CPUBackend::is_available (portableRT src/intersect_cpu.cpp:9) for this
  * backend: 1 when a device of compute capability 10.3 is visible.  Cheap, no context. */
@@ -173,10 +173,40 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  next nearest_hits when both formats have been built)
  *   "block"        threads per block of the traversal kernel (default 128)
  *   "count_visits" 1 = the traversal also accumulates node / triangle visit counts
+ *   "pool_depth"   0..32: tree depth the traversal's shared-memory pool is sized for in
+ *                  a batch graph, where the depth is not known when the graph is
+ *                  captured (0 = 32, always enough; a smaller value raises occupancy,
+ *                  and a tree it does not fit makes the query fail with
+ *                  PRT_ERR_DEVICE, never a wrong answer)
+ *   "build_compressed" 1 = set_tris also builds the compressed nodes (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
+
+/* Seeded synthetic workloads written straight into device memory (no counterpart in
+ * portableRT, whose examples read meshes from files).  SplitMix64 streams; the same
+ * generators as portablert_gb300/workloads.py (values that pass through log/cos may
+ * differ from the host's in the last bit).  n items of 9 floats (triangles) or 6 floats
+ * (rays) are written to d_out on `stream` (NULL = the context's). */
+#define PRT_GEN_SOUP_TRIS 0    /* centres in [-1,1]^3, vertex offsets in [-0.05,0.05]^3 */
+#define PRT_GEN_SOUP_RAYS 1    /* origins on the radius-3 sphere, aimed into [-0.5,0.5]^3 */
+#define PRT_GEN_CLUSTER_TRIS 2 /* param = cluster count: Gaussian clusters in [-10,10]^3 */
+#define PRT_GEN_RANDOM_RAYS 3  /* param = extent e: origins in [-e,e]^3, uniform directions */
+int prt_b200_generate(prt_b200_ctx *ctx, int kind, uint64_t seed, uint64_t n, double param,
+                      void *d_out, void *stream);
+
+/* FP64 scorer of t (no counterpart in portableRT; measurement only).  For every valid
+ * record of a nearest_hits result (device buffers; the records need t, primitive_id and
+ * valid), recomputes t by the Möller-Trumbore formula of core.hpp:27-65 in double on the
+ * triangle the record names (d_tris9, the AoS array set_tris was given) and reports
+ * result[0] max |t - t64|, [1] max |t - t64| / |t64|, [2] mean |t - t64|, [3] records
+ * scored, [4] records whose t equals t64 rounded to FP32, [5] valid records that could
+ * not be scored (primitive id out of range, t64 not finite).  Synchronous. */
+int prt_b200_t_error(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n_tris,
+                     const float *d_rays6, uint64_t n_rays, const void *d_records,
+                     uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                     double result[6]);
 
 #ifdef __cplusplus
 }

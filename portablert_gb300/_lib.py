@@ -20,7 +20,7 @@ EXPORTS = (
     "prt_b200_set_option", "prt_b200_get_stat", "prt_b200_nearest_hits_noalloc",
     "prt_b200_batch_create", "prt_b200_batch_destroy", "prt_b200_batch_set_tris_dev",
     "prt_b200_batch_query_dev", "prt_b200_batch_run_graph", "prt_b200_batch_sync",
-    "prt_b200_batch_stat",
+    "prt_b200_batch_stat", "prt_b200_generate", "prt_b200_t_error",
 )
 
 
@@ -86,6 +86,11 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_batch_sync.argtypes = [vp]
     L.prt_b200_batch_stat.restype = c_int
     L.prt_b200_batch_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+    L.prt_b200_generate.restype = c_int
+    L.prt_b200_generate.argtypes = [vp, c_int, c_u64, c_u64, ctypes.c_double, vp, vp]
+    L.prt_b200_t_error.restype = c_int
+    L.prt_b200_t_error.argtypes = [vp, vp, c_u64, vp, c_u64, vp, c_u32, c_u32, ctypes.c_char_p,
+                                   ctypes.POINTER(ctypes.c_double)]
     L.prt_b200_set_option.restype = c_int
     L.prt_b200_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
     L.prt_b200_get_stat.restype = c_int

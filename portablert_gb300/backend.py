@@ -95,6 +95,17 @@ class B200Backend:
         self._need()
         self._check(self._L.prt_b200_sync(self.ctx))
 
+    def t_error(self, tris_ptr: int, n_tris: int, rays_ptr: int, n_rays: int, out_ptr: int,
+                tags) -> dict:
+        """FP64 score of the t values in a device record buffer (prt_b200_t_error)."""
+        self._need()
+        lay = hitreg.layout(tags)
+        r = (ctypes.c_double * 6)()
+        self._check(self._L.prt_b200_t_error(self.ctx, tris_ptr, n_tris, rays_ptr, n_rays,
+                                             out_ptr, lay.mask, lay.size, lay.offsets8(), r))
+        return {"max_abs": r[0], "max_rel": r[1], "mean_abs": r[2], "scored": int(r[3]),
+                "exact": int(r[4]), "unscored": int(r[5])}
+
     # -- tuning and statistics ----------------------------------------------------------
     def set_option(self, key: str, value: int) -> None:
         self._need()

@@ -61,12 +61,12 @@ class Batch:
         self._check(self._L.prt_b200_batch_set_tris_dev(self.h, tris_ptr, p, s))
 
     def query_dev(self, queries, stream: int = 0) -> None:
-        arr = (_lib.Query * len(queries))(*queries)
+        arr = queries if isinstance(queries, ctypes.Array) else (_lib.Query * len(queries))(*queries)
         self._check(self._L.prt_b200_batch_query_dev(self.h, arr, len(queries), stream or None))
 
     def run_graph(self, tris_ptr: int, tri_off, queries, stream: int = 0) -> None:
         off, p, s = self._offsets(tri_off)
-        arr = (_lib.Query * len(queries))(*queries)
+        arr = queries if isinstance(queries, ctypes.Array) else (_lib.Query * len(queries))(*queries)
         self._check(self._L.prt_b200_batch_run_graph(self.h, tris_ptr, p, s, arr, len(queries),
                                                      stream or None))
 

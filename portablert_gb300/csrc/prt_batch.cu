@@ -182,7 +182,8 @@ size_t graph_key(const float *d_tris, const uint64_t *tri_off, uint32_t S,
 	std::string k(reinterpret_cast<const char *>(&d_tris), sizeof d_tris);
 	k.append(reinterpret_cast<const char *>(tri_off), sizeof(uint64_t) * (S + 1));
 	k.append(reinterpret_cast<const char *>(q), sizeof(prt_b200_query) * nq);
-	const int opts[4] = {ctx->leaf_size, ctx->node_format, ctx->block, (int)ctx->count};
+	const int opts[6] = {ctx->leaf_size,      ctx->node_format,       ctx->block,
+	                     (int)ctx->count,     ctx->pool_depth,        (int)ctx->build_compressed};
 	k.append(reinterpret_cast<const char *>(opts), sizeof opts);
 	return h(k);
 }
@@ -390,7 +391,8 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 		rc = prt::build_enqueue(d_tris, b->gplan, b->arena, b->ws, ctx->stream, ctx->d_err(),
 		                        false, msg);
 		if (rc == PRT_OK && !segs.empty())
-			rc = launch_query(b, b->gslot, segs, n_virtual, prt::traversal_stack_depth(),
+			rc = launch_query(b, b->gslot, segs, n_virtual,
+			                  ctx->pool_depth ? ctx->pool_depth : prt::traversal_stack_depth(),
 			                  b->gplan.node_cap, ctx->stream);
 		cudaGraph_t g = nullptr;
 		cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);

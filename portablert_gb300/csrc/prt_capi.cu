@@ -143,6 +143,14 @@ int prt_b200_create(int device, prt_b200_ctx **out) {
 		e = cudaMallocHost(&ctx->h_err, 16);
 	if (e == cudaSuccess)
 		e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+	for (cudaStream_t *s : {&ctx->s_in, &ctx->s_out, &ctx->s_k2})
+		if (e == cudaSuccess)
+			e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+	for (int i = 0; i < prt_b200_ctx::kPipe && e == cudaSuccess; ++i) {
+		e = cudaEventCreateWithFlags(&ctx->ev_in[i], cudaEventDisableTiming);
+		if (e == cudaSuccess)
+			e = cudaEventCreateWithFlags(&ctx->ev_k[i], cudaEventDisableTiming);
+	}
 	if (e != cudaSuccess) {
 		g_create_error = std::string("create: ") + cudaGetErrorString(e);
 		prt_b200_destroy(ctx);
@@ -156,8 +164,9 @@ void prt_b200_destroy(prt_b200_ctx *ctx) {
 	if (!ctx)
 		return;
 	cudaSetDevice(ctx->device);
-	if (ctx->stream)
-		cudaStreamSynchronize(ctx->stream);
+	for (cudaStream_t s : {ctx->stream, ctx->s_in, ctx->s_out, ctx->s_k2})
+		if (s)
+			cudaStreamSynchronize(s);
 	ctx->scene.release();
 	ctx->ws.release();
 	ctx->tris_in.release();
@@ -166,8 +175,17 @@ void prt_b200_destroy(prt_b200_ctx *ctx) {
 	ctx->work.release();
 	if (ctx->h_err)
 		cudaFreeHost(ctx->h_err);
-	if (ctx->stream)
-		cudaStreamDestroy(ctx->stream);
+	for (int i = 0; i < prt_b200_ctx::kPipe; ++i) {
+		if (ctx->ev_in[i])
+			cudaEventDestroy(ctx->ev_in[i]);
+		if (ctx->ev_k[i])
+			cudaEventDestroy(ctx->ev_k[i]);
+	}
+	for (cudaStream_t s : {ctx->s_in, ctx->s_out, ctx->s_k2, ctx->stream})
+		if (s) {
+			cudaStreamSynchronize(s);
+			cudaStreamDestroy(s);
+		}
 	delete ctx;
 }
 
@@ -269,26 +287,70 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
 	if (n && (!rays6 || !out_host))
 		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
-	{
-		std::lock_guard<std::mutex> lk(ctx->mu);
-		if (!ctx->scene_set)
-			return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
-		if (n == 0)
-			return PRT_OK;
-		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-		CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
-		CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
-		CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.p, rays6, 24ull * n, cudaMemcpyHostToDevice,
-		                              ctx->stream));
-	}
-	int rc = prt_b200_nearest_hits_dev(ctx, ctx->rays_buf.as<float>(), n, field_mask, rec_size,
-	                                   offs, ctx->out_buf.p, nullptr);
-	if (rc != PRT_OK)
-		return rc;
 	std::lock_guard<std::mutex> lk(ctx->mu);
-	CAPI_TRY(ctx, cudaMemcpyAsync(out_host, ctx->out_buf.p, (uint64_t)rec_size * n,
-	                              cudaMemcpyDeviceToHost, ctx->stream));
-	CAPI_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+	if (!ctx->scene_set)
+		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
+	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: compressed nodes were not built");
+	if (n == 0)
+		return PRT_OK;
+	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+	CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
+	CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
+	prt::OutLayout lay;
+	lay.mask = field_mask;
+	lay.rec_size = rec_size;
+	std::memcpy(lay.off, offs, 8);
+	prt::TravConfig cfg;
+	cfg.format = ctx->node_format;
+	cfg.block = ctx->block;
+	cfg.count = ctx->count;
+	// Chunks: about kPipe of them, at least 2^18 rays each (whole warps), one when the
+	// visit counters are on (each launch would reset them).  Chunk c is copied in on s_in,
+	// traversed on stream c % 2 (so a chunk's last blocks overlap the next chunk's first)
+	// and copied out on s_out.  Every chunk has its own rays, records and events; the two
+	// compute streams have their own ray counters.
+	const uint64_t per = (n + prt_b200_ctx::kPipe - 1) / prt_b200_ctx::kPipe;
+	const uint64_t chunk = ctx->count ? n : std::max<uint64_t>(1ull << 18, (per + 31) & ~31ull);
+	const int nc = (int)((n + chunk - 1) / chunk);
+	cudaStream_t ks[2] = {ctx->stream, ctx->s_k2};
+	uint32_t *ctr[2] = {ctx->d_work(), ctx->d_work() + 8};
+	// Earlier work of the context's stream (a _dev call) finishes before the chunks start.
+	CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[0], ctx->stream));
+	for (cudaStream_t st : {ctx->s_in, ctx->s_out, ctx->s_k2})
+		CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_k[0], 0));
+	const uint8_t *rin = reinterpret_cast<const uint8_t *>(rays6);
+	uint8_t *rout = static_cast<uint8_t *>(out_host);
+	for (int c = 0; c <= nc; ++c) {
+		if (c < nc) {
+			const uint64_t b = (uint64_t)c * chunk, m = std::min(chunk, n - b);
+			CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.as<uint8_t>() + 24 * b, rin + 24 * b,
+			                              24 * m, cudaMemcpyHostToDevice, ctx->s_in));
+			CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[c], ctx->s_in));
+			cudaStream_t st = ks[c & 1];
+			CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_in[c], 0));
+			CAPI_TRY(ctx, prt::launch_nearest_hits(
+			                  ctx->scene, ctx->rays_buf.as<float>() + 6 * b, m, lay,
+			                  ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b, cfg, ctr[c & 1],
+			                  ctx->d_visits(), ctx->d_err(), st, ctx->sms));
+			CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[c], st));
+		}
+		// The copy-out of the chunk before is queued after this chunk's copy-in, so that
+		// with pageable host memory (where the copy calls return only when done) the
+		// copy-in still overlaps the traversal.
+		if (c > 0) {
+			const uint64_t b = (uint64_t)(c - 1) * chunk, m = std::min(chunk, n - b);
+			CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->s_out, ctx->ev_k[c - 1], 0));
+			CAPI_TRY(ctx, cudaMemcpyAsync(rout + (uint64_t)rec_size * b,
+			                              ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b,
+			                              (uint64_t)rec_size * m, cudaMemcpyDeviceToHost,
+			                              ctx->s_out));
+		}
+	}
+	// s_out waited for every chunk's traversal; the context's stream waits for s_out.
+	CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[0], ctx->s_out));
+	CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[0], 0));
+	CAPI_TRY(ctx, cudaStreamSynchronize(ctx->s_out));
 	if (ctx->count)
 		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
 	return check_device_errors(ctx);
@@ -311,6 +373,10 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		if (v < 32 || v > 128 || v % 32)
 			return fail(ctx, PRT_ERR_ARG, "block must be 32, 64, 96 or 128");
 		ctx->block = (int)v;
+	} else if (k == "pool_depth") {
+		if (v < 0 || v > prt::traversal_stack_depth())
+			return fail(ctx, PRT_ERR_ARG, "pool_depth must be in [0, 32]");
+		ctx->pool_depth = (int)v;
 	} else if (k == "count_visits") {
 		ctx->count = v != 0;
 	} else if (k == "build_compressed") {

@@ -21,11 +21,18 @@ struct prt_b200_ctx {
 	prt::BuildScratch ws;
 	prt::DevBuf tris_in;
 	prt::DevBuf rays_buf, out_buf;
-	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters
+	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters,
+	                  // [32..35] ray counter of the second compute stream
+	// The host-buffer call splits large batches into chunks and overlaps the copy-in of a
+	// chunk, the traversal of the one before and the copy-out of the one before that.
+	static constexpr int kPipe = 8;
+	cudaStream_t s_in = nullptr, s_out = nullptr, s_k2 = nullptr;
+	cudaEvent_t ev_in[kPipe] = {}, ev_k[kPipe] = {};
 	uint32_t *h_err = nullptr;
 	int leaf_size = 1;
 	int node_format = PRT_NODES_FP32;
 	int block = 128;
+	int pool_depth = 0; // tree depth a batch graph's traversal pool is sized for (0 = 32)
 	bool count = false;
 	bool build_compressed = true;
 	double build_ms = 0.0;

@@ -246,3 +246,21 @@ def batch_sizes(n_scenes: int = 4096, seed: int = 3, tri_range=(16, 65_536),
     s = Stream(seed, 7)
     return (log_uniform_int(s, tri_range[0], tri_range[1], n_scenes),
             log_uniform_int(s, ray_range[0], ray_range[1], n_scenes))
+
+
+# ---------------------------------------------------------------- device generation
+
+GEN_SOUP_TRIS, GEN_SOUP_RAYS, GEN_CLUSTER_TRIS, GEN_RANDOM_RAYS = 0, 1, 2, 3
+
+
+def generate_dev(backend, kind: int, seed: int, n: int, out_ptr: int, param: float = 0.0,
+                 stream: int | None = None) -> None:
+    """Writes the generator `kind` (GEN_*) for `seed` straight into device memory at
+    out_ptr (prt_b200_generate): n x 9 floats for triangles, n x 6 for rays.  Queued on
+    `stream` (None = the backend context's stream)."""
+    import ctypes
+
+    backend._need()
+    backend._check(backend._L.prt_b200_generate(backend.ctx, int(kind), int(seed), int(n),
+                                                float(param), ctypes.c_void_p(out_ptr),
+                                                ctypes.c_void_p(stream) if stream else None))

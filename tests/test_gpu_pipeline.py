@@ -1,0 +1,73 @@
+"""The host-buffer call (prt_b200_nearest_hits) splits large batches into chunks whose
+copies and traversals overlap on several streams.  Its records must be byte-identical
+to one device-buffer launch over the same rays, for pageable and pinned host memory,
+chunk counts from one to eight, ragged last chunks and every node format."""
+import numpy as np
+import pytest
+
+from portablert_gb300 import hitreg, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_records(torch, backend, rays, tags):
+    lay = hitreg.layout(tags)
+    d_r = torch.from_numpy(rays).cuda()
+    d_o = torch.zeros(len(rays) * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    backend.nearest_hits_dev(d_r.data_ptr(), len(rays), d_o.data_ptr(), tags)
+    backend.sync()
+    return d_o.cpu().numpy()
+
+
+@pytest.mark.parametrize("n_rays", [(1 << 18) - 1, (1 << 18) + 1, 5 * (1 << 18) + 77, 2_500_001])
+@pytest.mark.parametrize("fmt", [0, 1])
+def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt):
+    import torch
+
+    tris = workloads.soup_tris(41, 20_000)
+    rays = workloads.soup_rays(42, n_rays)
+    gpu_backend.set_option("node_format", fmt)
+    try:
+        gpu_backend.set_tris(tris)
+        for tags in [hitreg.TAGS, ("t", "primitive_id", "valid"), ("valid",)]:
+            want = _device_records(torch, gpu_backend, rays, tags)
+            got = gpu_backend.nearest_hits(rays, tags).view(np.uint8).reshape(-1)
+            assert np.array_equal(got, want), tags
+    finally:
+        gpu_backend.set_option("node_format", 0)
+
+
+def test_chunked_host_call_pinned_buffers(gpu_backend):
+    import ctypes
+
+    import torch
+
+    tris = workloads.soup_tris(43, 5_000)
+    rays = workloads.soup_rays(44, 3 * (1 << 18) + 5)
+    gpu_backend.set_tris(tris)
+    lay = hitreg.layout(hitreg.TAGS)
+    h_r = torch.from_numpy(rays).pin_memory()
+    h_o = torch.zeros(len(rays) * lay.size, dtype=torch.uint8).pin_memory()
+    L = gpu_backend._L
+    gpu_backend._check(L.prt_b200_nearest_hits(gpu_backend.ctx, ctypes.c_void_p(h_r.data_ptr()),
+                                               len(rays), lay.mask, lay.size, lay.offsets8(),
+                                               ctypes.c_void_p(h_o.data_ptr())))
+    want = _device_records(torch, gpu_backend, rays, hitreg.TAGS)
+    assert np.array_equal(h_o.numpy(), want)
+
+
+def test_counting_run_is_one_chunk_and_equal(gpu_backend):
+    import torch
+
+    tris = workloads.soup_tris(45, 3_000)
+    rays = workloads.soup_rays(46, 3 * (1 << 18))
+    gpu_backend.set_tris(tris)
+    want = _device_records(torch, gpu_backend, rays, hitreg.TAGS)
+    gpu_backend.set_option("count_visits", 1)
+    try:
+        got = gpu_backend.nearest_hits(rays, hitreg.TAGS).view(np.uint8).reshape(-1)
+        assert np.array_equal(got, want)
+        assert gpu_backend.stat("visits_nodes") >= len(rays)
+    finally:
+        gpu_backend.set_option("count_visits", 0)
