@@ -71,7 +71,30 @@ int check_device_errors(prt_b200_ctx *ctx) {
 	return PRT_OK;
 }
 
+// The bookkeeping of a caller's stream (created at its first query).
+int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out) {
+	for (auto &q : ctx->query_streams)
+		if (q.st == st) {
+			*out = &q;
+			return PRT_OK;
+		}
+	prt_b200_ctx::QueryStream q{st, nullptr, nullptr};
+	CAPI_TRY(ctx, cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming));
+	cudaError_t e = cudaMalloc(&q.counter, 64);
+	if (e != cudaSuccess) {
+		cudaEventDestroy(q.ev);
+		return cuda_fail(ctx, e, "nearest_hits_dev: stream counter");
+	}
+	ctx->query_streams.push_back(q);
+	*out = &ctx->query_streams.back();
+	return PRT_OK;
+}
+
 int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
+	// Queries still reading the old scene on callers' streams finish before the
+	// rebuild overwrites its arrays.
+	for (auto &q : ctx->query_streams)
+		CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->stream, q.ev, 0));
 	cudaEvent_t e0, e1;
 	CAPI_TRY(ctx, cudaEventCreate(&e0));
 	CAPI_TRY(ctx, cudaEventCreate(&e1));
@@ -167,6 +190,8 @@ void prt_b200_destroy(prt_b200_ctx *ctx) {
 	for (cudaStream_t s : {ctx->stream, ctx->s_in, ctx->s_out, ctx->s_k2})
 		if (s)
 			cudaStreamSynchronize(s);
+	for (auto &q : ctx->query_streams)
+		cudaEventSynchronize(q.ev);
 	ctx->scene.release();
 	ctx->ws.release();
 	ctx->tris_in.release();
@@ -175,6 +200,10 @@ void prt_b200_destroy(prt_b200_ctx *ctx) {
 	ctx->work.release();
 	if (ctx->h_err)
 		cudaFreeHost(ctx->h_err);
+	for (auto &q : ctx->query_streams) {
+		cudaEventDestroy(q.ev);
+		cudaFree(q.counter);
+	}
 	for (int i = 0; i < prt_b200_ctx::kPipe; ++i) {
 		if (ctx->ev_in[i])
 			cudaEventDestroy(ctx->ev_in[i]);
@@ -260,9 +289,17 @@ int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t 
 	cfg.block = ctx->block;
 	cfg.count = ctx->count;
 	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	prt_b200_ctx::QueryStream *qs = nullptr;
+	if (st != ctx->stream) {
+		int rc = query_stream(ctx, st, &qs);
+		if (rc != PRT_OK)
+			return rc;
+	}
 	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays6, n, lay, d_out, cfg,
-	                                       ctx->d_work(), ctx->d_visits(), ctx->d_err(), st,
-	                                       ctx->sms));
+	                                       qs ? qs->counter : ctx->d_work(), ctx->d_visits(),
+	                                       ctx->d_err(), st, ctx->sms));
+	if (qs)
+		CAPI_TRY(ctx, cudaEventRecord(qs->ev, st));
 	return PRT_OK;
 }
 

@@ -6,6 +6,8 @@
 
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
@@ -28,6 +30,15 @@ struct prt_b200_ctx {
 	static constexpr int kPipe = 8;
 	cudaStream_t s_in = nullptr, s_out = nullptr, s_k2 = nullptr;
 	cudaEvent_t ev_in[kPipe] = {}, ev_k[kPipe] = {};
+	// Callers' streams that nearest_hits_dev has queued queries on.  Each has its own
+	// ray counter (so queries on different streams may run at once) and an event
+	// recorded after its last query, which set_tris waits for before it rebuilds.
+	struct QueryStream {
+		cudaStream_t st;
+		cudaEvent_t ev;
+		uint32_t *counter;
+	};
+	std::vector<QueryStream> query_streams;
 	uint32_t *h_err = nullptr;
 	int leaf_size = 1;
 	int node_format = PRT_NODES_FP32;

@@ -71,3 +71,55 @@ def test_counting_run_is_one_chunk_and_equal(gpu_backend):
         assert gpu_backend.stat("visits_nodes") >= len(rays)
     finally:
         gpu_backend.set_option("count_visits", 0)
+
+
+def test_rebuild_waits_for_queries_on_caller_streams(gpu_backend):
+    """set_tris_dev right after nearest_hits_dev on a caller's stream (no sync between):
+    the rebuild must not overwrite the scene the queued query is reading."""
+    import torch
+
+    scenes = [workloads.soup_tris(60 + s, 20_000 + 3_000 * s) for s in range(6)]
+    rays = [workloads.soup_rays(70 + s, 400_000) for s in range(6)]
+    want = []
+    for t, r in zip(scenes, rays):
+        gpu_backend.set_tris(t)
+        want.append(gpu_backend.nearest_hits(r, hitreg.TAGS).view(np.uint8).reshape(-1))
+    lay = hitreg.layout(hitreg.TAGS)
+    d_t = [torch.from_numpy(t).cuda() for t in scenes]
+    d_r = [torch.from_numpy(r).cuda() for r in rays]
+    d_o = [torch.zeros(len(r) * lay.size, dtype=torch.uint8, device="cuda") for r in rays]
+    torch.cuda.synchronize()
+    st = torch.cuda.Stream()
+    for s in range(len(scenes)):
+        gpu_backend.set_tris_dev(d_t[s].data_ptr(), len(scenes[s]))
+        gpu_backend.nearest_hits_dev(d_r[s].data_ptr(), len(rays[s]), d_o[s].data_ptr(),
+                                     hitreg.TAGS, st.cuda_stream)
+    gpu_backend.sync()
+    for s in range(len(scenes)):
+        assert np.array_equal(d_o[s].cpu().numpy(), want[s]), s
+
+
+def test_queries_on_two_streams_at_once(gpu_backend):
+    """Queries queued on two callers' streams may run at the same time: each stream has
+    its own ray counter."""
+    import torch
+
+    tris = workloads.soup_tris(80, 30_000)
+    gpu_backend.set_tris(tris)
+    ra, rb = workloads.soup_rays(81, 1_500_000), workloads.soup_rays(82, 900_000)
+    wa = gpu_backend.nearest_hits(ra, hitreg.TAGS).view(np.uint8).reshape(-1)
+    wb = gpu_backend.nearest_hits(rb, hitreg.TAGS).view(np.uint8).reshape(-1)
+    lay = hitreg.layout(hitreg.TAGS)
+    da, db = torch.from_numpy(ra).cuda(), torch.from_numpy(rb).cuda()
+    oa = torch.zeros(len(ra) * lay.size, dtype=torch.uint8, device="cuda")
+    ob = torch.zeros(len(rb) * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for _ in range(3):
+        gpu_backend.nearest_hits_dev(da.data_ptr(), len(ra), oa.data_ptr(), hitreg.TAGS,
+                                     s1.cuda_stream)
+        gpu_backend.nearest_hits_dev(db.data_ptr(), len(rb), ob.data_ptr(), hitreg.TAGS,
+                                     s2.cuda_stream)
+    gpu_backend.sync()
+    assert np.array_equal(oa.cpu().numpy(), wa)
+    assert np.array_equal(ob.cpu().numpy(), wb)
