@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstddef>
 #include <cstring>
 
 #include "../../include/prt_b200.h"
@@ -88,6 +89,50 @@ __global__ void k_bounds_init(uint32_t *gb, uint32_t n_scenes) {
 __global__ void k_centroid_bounds(const float *__restrict__ tris, uint32_t n,
                                   const uint32_t *__restrict__ scene_of, uint32_t *gb) {
 	const int lane = threadIdx.x & 31;
+	if (!scene_of) {
+		// One scene: each thread folds its grid-stride share, then the block reduces and
+		// one thread updates the six words (so the same-address atomics stay few).
+		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+		for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n;
+		     i += gridDim.x * blockDim.x) {
+			const float *t = tris + 9 * (size_t)i;
+			if (tri_finite(t)) {
+#pragma unroll
+				for (int k = 0; k < 3; ++k) {
+					const float c = centroid(t, k);
+					mn[k] = fminf(mn[k], c);
+					mx[k] = fmaxf(mx[k], c);
+				}
+			}
+		}
+		__shared__ float red[32][6];
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			for (int o = 16; o > 0; o >>= 1) {
+				mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+				mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
+			}
+		const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+		if (lane == 0)
+			for (int k = 0; k < 3; ++k) {
+				red[w][k] = mn[k];
+				red[w][3 + k] = mx[k];
+			}
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			for (int v = 1; v < nw; ++v)
+				for (int k = 0; k < 3; ++k) {
+					mn[k] = fminf(mn[k], red[v][k]);
+					mx[k] = fmaxf(mx[k], red[v][3 + k]);
+				}
+			if (mn[0] <= mx[0])
+				for (int k = 0; k < 3; ++k) {
+					atomicMin(&gb[k], f2ord(mn[k]));
+					atomicMax(&gb[3 + k], f2ord(mx[k]));
+				}
+		}
+		return;
+	}
 	for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
 		const uint32_t i = base + threadIdx.x;
 		float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
@@ -341,7 +386,23 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 	return isfinite(a) ? a : FLT_MAX;
 }
 
-// One level: each frontier item becomes an 8-wide node.
+__device__ __forceinline__ float open_area(uint32_t r, const float4 *__restrict__ ibox) {
+	return (r & kLeafBit) ? -1.0f : half_area(ibox[2 * r], ibox[2 * r + 1]);
+}
+
+// Compare-exchange of two children by first leaf (registers only).
+__device__ __forceinline__ void cx(uint32_t &ca, uint32_t &fa, uint32_t &na, uint32_t &cb,
+                                   uint32_t &fb, uint32_t &nb) {
+	if (fa > fb) {
+		uint32_t t = ca; ca = cb; cb = t;
+		t = fa; fa = fb; fb = t;
+		t = na; na = nb; nb = t;
+	}
+}
+
+// One level: each frontier item becomes an 8-wide node.  A warp takes 32 items; the
+// node slots, triangle ranges and next-level items it needs are reserved with one
+// atomic per counter per warp.
 __global__ void __launch_bounds__(128)
     k_collapse(const Item *__restrict__ in, const uint32_t *in_count, Item *out,
                uint32_t *out_count, uint32_t *node_counter, uint32_t node_cap,
@@ -351,11 +412,128 @@ __global__ void __launch_bounds__(128)
                const float4 *__restrict__ ibox, const float4 *__restrict__ lbox,
                uint32_t leaf_size, uint32_t n_tris, uint32_t *err) {
 	const uint32_t n_in = *in_count;
-	for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < n_in;
-	     w += gridDim.x * blockDim.x) {
-		const Item it = in[w];
+	const uint32_t lane = threadIdx.x & 31u;
+	for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n_in;
+	     w0 += gridDim.x * blockDim.x) {
+		const uint32_t w = w0 + lane;
+		const bool live = w < n_in;
+		const Item it = live ? in[w] : Item{kNone, 0u};
+		const bool empty_scene = live && it.ref == kNone;
+		// Open the binary child of largest surface area until 8 children: any binary
+		// node can be opened, so nodes fill up and small subtrees end as single
+		// triangles (whose box is then tested exactly like the reference's leaf box).
+		uint32_t C[8], F[8], N[8];
+		float A[8];
+#pragma unroll
+		for (int c = 0; c < 8; ++c) {
+			C[c] = kNone;
+			A[c] = -1.0f;
+		}
+		int nc = 0;
+		if (live && !empty_scene) {
+			C[0] = it.ref;
+			A[0] = open_area(it.ref, ibox);
+			nc = 1;
+			while (nc < 8) {
+				int best = -1;
+				float best_area = -1.0f;
+#pragma unroll
+				for (int c = 0; c < 8; ++c)
+					if (c < nc && A[c] > best_area) {
+						best_area = A[c];
+						best = c;
+					}
+				if (best < 0)
+					break;
+				uint32_t x = 0;
+#pragma unroll
+				for (int c = 0; c < 8; ++c)
+					if (c == best)
+						x = C[c];
+				const uint32_t l = left[x], r = right[x];
+				const float al = open_area(l, ibox), ar = open_area(r, ibox);
+#pragma unroll
+				for (int c = 0; c < 8; ++c) {
+					if (c == best) {
+						C[c] = l;
+						A[c] = al;
+					}
+					if (c == nc) {
+						C[c] = r;
+						A[c] = ar;
+					}
+				}
+				++nc;
+			}
+		}
+		// First leaf and triangle count of each child; unused slots sort last.  Children
+		// are ordered by first leaf, so a node's leaf triangles keep the Morton order
+		// (first leaves of distinct children differ, so the order is unique).
+		uint32_t n_inner = 0, n_leaf_tris = 0;
+#pragma unroll
+		for (int c = 0; c < 8; ++c) {
+			if (c < nc) {
+				F[c] = bfirst(C[c], rfirst);
+				N[c] = bcount(C[c], rfirst, rlast);
+				if (!(C[c] & kLeafBit) && N[c] > leaf_size)
+					++n_inner;
+				else
+					n_leaf_tris += N[c];
+			} else {
+				F[c] = 0xFFFFFFFFu;
+				N[c] = 0;
+			}
+		}
+		cx(C[0], F[0], N[0], C[2], F[2], N[2]);
+		cx(C[1], F[1], N[1], C[3], F[3], N[3]);
+		cx(C[4], F[4], N[4], C[6], F[6], N[6]);
+		cx(C[5], F[5], N[5], C[7], F[7], N[7]);
+		cx(C[0], F[0], N[0], C[4], F[4], N[4]);
+		cx(C[1], F[1], N[1], C[5], F[5], N[5]);
+		cx(C[2], F[2], N[2], C[6], F[6], N[6]);
+		cx(C[3], F[3], N[3], C[7], F[7], N[7]);
+		cx(C[0], F[0], N[0], C[1], F[1], N[1]);
+		cx(C[2], F[2], N[2], C[3], F[3], N[3]);
+		cx(C[4], F[4], N[4], C[5], F[5], N[5]);
+		cx(C[6], F[6], N[6], C[7], F[7], N[7]);
+		cx(C[2], F[2], N[2], C[4], F[4], N[4]);
+		cx(C[3], F[3], N[3], C[5], F[5], N[5]);
+		cx(C[1], F[1], N[1], C[4], F[4], N[4]);
+		cx(C[3], F[3], N[3], C[6], F[6], N[6]);
+		cx(C[1], F[1], N[1], C[2], F[2], N[2]);
+		cx(C[3], F[3], N[3], C[4], F[4], N[4]);
+		cx(C[5], F[5], N[5], C[6], F[6], N[6]);
+		// Warp-wide reservation: exclusive prefix sums of the lanes' needs.
+		uint32_t inc_i = n_inner, inc_t = n_leaf_tris;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const uint32_t vi = __shfl_up_sync(0xFFFFFFFFu, inc_i, o);
+			const uint32_t vt = __shfl_up_sync(0xFFFFFFFFu, inc_t, o);
+			if (lane >= (uint32_t)o) {
+				inc_i += vi;
+				inc_t += vt;
+			}
+		}
+		const uint32_t tot_i = __shfl_sync(0xFFFFFFFFu, inc_i, 31);
+		const uint32_t tot_t = __shfl_sync(0xFFFFFFFFu, inc_t, 31);
+		uint32_t nb = 0, tb = 0, ob = 0;
+		if (lane == 31) {
+			nb = tot_i ? atomicAdd(node_counter, tot_i) : 0u;
+			tb = tot_t ? atomicAdd(tri_counter, tot_t) : 0u;
+			ob = tot_i ? atomicAdd(out_count, tot_i) : 0u;
+		}
+		nb = __shfl_sync(0xFFFFFFFFu, nb, 31);
+		tb = __shfl_sync(0xFFFFFFFFu, tb, 31);
+		ob = __shfl_sync(0xFFFFFFFFu, ob, 31);
+		if (nb + tot_i > node_cap || tb + tot_t > n_tris) {
+			if (lane == 0)
+				atomicOr(err, kErrCollapse);
+			continue;
+		}
+		if (!live)
+			continue;
 		Node8 *nd = nodes + it.slot;
-		if (it.ref == kNone) { // empty scene: a node without children
+		if (empty_scene) { // a node without children
 			for (int c = 0; c < 8; ++c) {
 				Child8 ch;
 				ch.lo_x = ch.lo_y = ch.lo_z = 0.0f;
@@ -366,86 +544,32 @@ __global__ void __launch_bounds__(128)
 			}
 			continue;
 		}
-		uint32_t C[8];
-		int nc = 1;
-		C[0] = it.ref;
-		// Open the binary child of largest surface area until 8 children: any binary
-		// node can be opened, so nodes fill up and small subtrees end as single
-		// triangles (whose box is then tested exactly like the reference's leaf box).
-		while (nc < 8) {
-			int best = -1;
-			float best_area = -1.0f;
-			for (int c = 0; c < nc; ++c) {
-				uint32_t r = C[c];
-				if (!(r & kLeafBit)) {
-					float a = half_area(ibox[2 * r], ibox[2 * r + 1]);
-					if (a > best_area) {
-						best_area = a;
-						best = c;
-					}
-				}
-			}
-			if (best < 0)
-				break;
-			uint32_t x = C[best];
-			C[best] = left[x];
-			C[nc++] = right[x];
-		}
-		// Children in order of their first leaf, so a node's leaf triangles keep the
-		// Morton order.
-		for (int a = 1; a < nc; ++a) {
-			uint32_t v = C[a];
-			uint32_t fv = bfirst(v, rfirst);
-			int b = a - 1;
-			while (b >= 0 && bfirst(C[b], rfirst) > fv) {
-				C[b + 1] = C[b];
-				--b;
-			}
-			C[b + 1] = v;
-		}
-		uint32_t n_inner = 0, n_leaf_tris = 0;
-		for (int c = 0; c < nc; ++c) {
-			uint32_t cnt = bcount(C[c], rfirst, rlast);
-			if (!(C[c] & kLeafBit) && cnt > leaf_size)
-				++n_inner;
-			else
-				n_leaf_tris += cnt;
-		}
-		uint32_t base = n_inner ? atomicAdd(node_counter, n_inner) : 0u;
-		if (base + n_inner > node_cap) {
-			atomicOr(err, kErrCollapse);
-			continue;
-		}
-		uint32_t tbase = n_leaf_tris ? atomicAdd(tri_counter, n_leaf_tris) : 0u;
-		if (tbase + n_leaf_tris > n_tris) {
-			atomicOr(err, kErrCollapse);
-			continue;
-		}
-		uint32_t k_inner = 0, toff = 0;
+		const uint32_t base = nb + inc_i - n_inner, obase = ob + inc_i - n_inner;
+		uint32_t dst = tb + inc_t - n_leaf_tris;
+		uint32_t k_inner = 0;
+#pragma unroll
 		for (int c = 0; c < 8; ++c) {
 			float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
 			uint32_t ref = kNone;
 			if (c < nc) {
-				uint32_t r = C[c];
-				uint32_t cnt = bcount(r, rfirst, rlast);
+				const uint32_t r = C[c];
 				if (r & kLeafBit) {
-					uint32_t k = r & ~kLeafBit;
+					const uint32_t k = r & ~kLeafBit;
 					lo = lbox[2 * k];
 					hi = lbox[2 * k + 1];
 				} else {
 					lo = ibox[2 * r];
 					hi = ibox[2 * r + 1];
 				}
-				if (!(r & kLeafBit) && cnt > leaf_size) {
-					ref = base + k_inner++;
-					out[atomicAdd(out_count, 1u)] = Item{r, ref};
+				if (!(r & kLeafBit) && N[c] > leaf_size) {
+					ref = base + k_inner;
+					out[obase + k_inner] = Item{r, ref};
+					++k_inner;
 				} else {
-					uint32_t first = bfirst(r, rfirst);
-					uint32_t dst = tbase + toff;
-					toff += cnt;
-					for (uint32_t k = 0; k < cnt; ++k)
-						perm[dst + k] = first + k;
-					ref = make_leaf(dst, cnt);
+					for (uint32_t k = 0; k < N[c]; ++k)
+						perm[dst + k] = F[c] + k;
+					ref = make_leaf(dst, N[c]);
+					dst += N[c];
 				}
 			}
 			Child8 ch;
@@ -485,10 +609,12 @@ __device__ __forceinline__ float cdec(float o, uint32_t q, float s) {
 }
 
 // Largest q in [0, 255] whose decoded value is <= v (decoding is monotone in q and
-// q = 0 decodes to the origin, which is <= every child bound).
+// q = 0 decodes to the origin, which is <= every child bound).  The estimate comes from
+// a directed-rounding FP32 quotient; the loops make the answer exact, so it does not
+// depend on the estimate.
 __device__ uint32_t quant_lo(float o, float s, float v) {
-	double g = floor(((double)v - (double)o) / (double)s);
-	uint32_t q = (uint32_t)fmin(fmax(g, 0.0), 255.0);
+	const float g = floorf(__fdiv_rd(__fsub_rd(v, o), s));
+	uint32_t q = (uint32_t)fminf(fmaxf(g, 0.0f), 255.0f);
 	while (q > 0 && cdec(o, q, s) > v)
 		--q;
 	while (q < 255 && cdec(o, q + 1, s) <= v)
@@ -499,8 +625,8 @@ __device__ uint32_t quant_lo(float o, float s, float v) {
 // Smallest q in [0, 255] whose decoded value is >= v (the exponent was chosen so that
 // q = 255 qualifies).
 __device__ uint32_t quant_hi(float o, float s, float v) {
-	double g = ceil(((double)v - (double)o) / (double)s);
-	uint32_t q = (uint32_t)fmin(fmax(g, 0.0), 255.0);
+	const float g = ceilf(__fdiv_ru(__fsub_ru(v, o), s));
+	uint32_t q = (uint32_t)fminf(fmaxf(g, 0.0f), 255.0f);
 	while (q < 255 && cdec(o, q, s) < v)
 		++q;
 	while (q > 0 && cdec(o, q - 1, s) >= v)
@@ -508,92 +634,119 @@ __device__ uint32_t quant_hi(float o, float s, float v) {
 	return q;
 }
 
+// Smallest biased exponent e in [1, 254] with o + 255 * 2^(e-127) >= mx in FP32 (254
+// when none is; the traversal then still tests the children exactly at the leaves).
+// The start is at most the answer: the FP32 range rounded up, over 255 rounded up, has
+// an exponent at least that of the answer's scale less two.
+__device__ uint32_t scale_exponent(float mn, float mx) {
+	const float r = __fdiv_ru(__fsub_ru(mx, mn), 255.0f);
+	int e = 254;
+	if (isfinite(r)) {
+		const uint32_t bits = __float_as_uint(r);
+		const int e0 = (int)((bits >> 23) & 0xFFu) + ((bits & 0x7FFFFFu) ? 1 : 0);
+		e = max(1, min(254, e0 - 2));
+	}
+	while (e < 254 && cdec(mn, 255u, cscale((uint8_t)e)) < mx)
+		++e;
+	return (uint32_t)e;
+}
+
+// Eight lanes per node, lane k on child k: reads and writes are contiguous per node.
 // n_nodes_dev (when not null) holds the node count on the device: a build queued
 // without host round-trips launches this kernel over the node capacity.
-__global__ void k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes,
-                           const uint32_t *n_nodes_dev, CNode8 *cn) {
-	uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	if (i >= (n_nodes_dev ? *n_nodes_dev : n_nodes))
+__global__ void __launch_bounds__(256)
+    k_compress(const Node8 *__restrict__ nodes, uint32_t n_nodes, const uint32_t *n_nodes_dev,
+               CNode8 *cn) {
+	const uint32_t k = threadIdx.x & 7u;
+	const uint32_t i = blockIdx.x * (blockDim.x / 8u) + threadIdx.x / 8u;
+	const uint32_t n = n_nodes_dev ? *n_nodes_dev : n_nodes;
+	const bool live = i < n;
+	// Groups of 8 lanes never straddle the node range, but the warp does: every lane
+	// takes part in the shuffles, idle ones with an empty child.
+	const unsigned gmask = 0xFFu << (threadIdx.x & 24u);
+	Child8 ch;
+	if (live) {
+		const float4 *src = reinterpret_cast<const float4 *>(&nodes[i].c[k]);
+		const float4 a = __ldg(src), b = __ldg(src + 1);
+		ch.lo_x = a.x;
+		ch.lo_y = a.y;
+		ch.lo_z = a.z;
+		ch.ref = __float_as_uint(a.w);
+		ch.hi_x = b.x;
+		ch.hi_y = b.y;
+		ch.hi_z = b.z;
+	} else {
+		ch.ref = kNone;
+		ch.lo_x = ch.lo_y = ch.lo_z = ch.hi_x = ch.hi_y = ch.hi_z = 0.0f;
+	}
+	const uint32_t r = ch.ref;
+	const bool used = r != kNone;
+	const bool leaf = used && (r & kLeafBit);
+	uint32_t cb = (used && !leaf) ? r : kNone;
+	uint32_t tb = leaf ? leaf_first(r) : kNone;
+	float lo[3] = {ch.lo_x, ch.lo_y, ch.lo_z}, hi[3] = {ch.hi_x, ch.hi_y, ch.hi_z};
+	float mn[3], mx[3];
+	for (int a = 0; a < 3; ++a) {
+		mn[a] = used ? lo[a] : INFINITY;
+		mx[a] = used ? hi[a] : -INFINITY;
+	}
+	for (int o = 4; o > 0; o >>= 1) {
+		cb = min(cb, __shfl_xor_sync(gmask, cb, o, 8));
+		tb = min(tb, __shfl_xor_sync(gmask, tb, o, 8));
+		for (int a = 0; a < 3; ++a) {
+			mn[a] = fminf(mn[a], __shfl_xor_sync(gmask, mn[a], o, 8));
+			mx[a] = fmaxf(mx[a], __shfl_xor_sync(gmask, mx[a], o, 8));
+		}
+	}
+	const uint32_t imask = (__ballot_sync(gmask, used && !leaf) >> (threadIdx.x & 24u)) & 0xFFu;
+	if (!live)
 		return;
-	const Node8 &nd = nodes[i];
-	float lo[3][8], hi[3][8];
-	uint32_t ref[8];
-	for (int k = 0; k < 8; ++k) {
-		const Child8 &ch = nd.c[k];
-		lo[0][k] = ch.lo_x;
-		lo[1][k] = ch.lo_y;
-		lo[2][k] = ch.lo_z;
-		hi[0][k] = ch.hi_x;
-		hi[1][k] = ch.hi_y;
-		hi[2][k] = ch.hi_z;
-		ref[k] = ch.ref;
-	}
-	CNode8 c;
-	memset(&c, 0, sizeof c);
-	uint32_t child_base = kNone, tri_base = kNone;
-	for (int k = 0; k < 8; ++k) {
-		const uint32_t r = ref[k];
-		if (r == kNone)
-			continue;
-		if (r & kLeafBit)
-			tri_base = min(tri_base, leaf_first(r));
-		else {
-			c.imask |= (uint8_t)(1u << k);
-			child_base = min(child_base, r);
-		}
-	}
-	c.child_base = child_base == kNone ? 0u : child_base;
-	c.tri_base = tri_base == kNone ? 0u : tri_base;
-	for (int k = 0; k < 8; ++k) {
-		const uint32_t r = ref[k];
-		if (r != kNone && (r & kLeafBit)) {
-			c.c[k].count = (uint8_t)leaf_count(r);
-			c.c[k].first = (uint8_t)(leaf_first(r) - c.tri_base);
-		}
-	}
 	float org[3];
-	uint8_t ex[3];
+	uint32_t ex[3];
 	for (int a = 0; a < 3; ++a) {
-		float mn = INFINITY, mx = -INFINITY;
-		for (int k = 0; k < 8; ++k) {
-			if (ref[k] == kNone)
-				continue;
-			mn = fminf(mn, lo[a][k]);
-			mx = fmaxf(mx, hi[a][k]);
+		if (!(mn[a] <= mx[a])) { // no children: an empty frame at the origin
+			mn[a] = 0.0f;
+			mx[a] = 0.0f;
 		}
-		if (!(mn <= mx)) {
-			mn = 0.0f;
-			mx = 0.0f;
-		}
-		org[a] = mn;
-		double range = (double)mx - (double)mn;
-		int e = 1;
-		if (range > 0.0) {
-			int est = (int)ceil(log2(range / 255.0)) + 127;
-			e = max(1, min(254, est - 1));
-		}
-		while (e < 254 && cdec(mn, 255u, cscale((uint8_t)e)) < mx)
-			++e;
-		ex[a] = (uint8_t)e;
+		org[a] = mn[a];
+		ex[a] = scale_exponent(mn[a], mx[a]);
 	}
-	c.ox = org[0];
-	c.oy = org[1];
-	c.oz = org[2];
-	c.ex = ex[0];
-	c.ey = ex[1];
-	c.ez = ex[2];
-	for (int a = 0; a < 3; ++a) {
-		float s = cscale(ex[a]);
-		for (int k = 0; k < 8; ++k) {
-			if (ref[k] == kNone)
-				continue;
-			uint8_t *qk = &c.c[k].qlo_x;
-			qk[2 * a] = (uint8_t)quant_lo(org[a], s, lo[a][k]);
-			qk[2 * a + 1] = (uint8_t)quant_hi(org[a], s, hi[a][k]);
+	const uint32_t tri_base = tb == kNone ? 0u : tb;
+	CChild8 c;
+	c.qlo_x = c.qhi_x = c.qlo_y = c.qhi_y = c.qlo_z = c.qhi_z = 0;
+	c.count = 0;
+	c.first = 0;
+	if (used) {
+		uint8_t q[6];
+		for (int a = 0; a < 3; ++a) {
+			const float sc = cscale((uint8_t)ex[a]);
+			q[2 * a] = (uint8_t)quant_lo(org[a], sc, lo[a]);
+			q[2 * a + 1] = (uint8_t)quant_hi(org[a], sc, hi[a]);
+		}
+		c.qlo_x = q[0];
+		c.qhi_x = q[1];
+		c.qlo_y = q[2];
+		c.qhi_y = q[3];
+		c.qlo_z = q[4];
+		c.qhi_z = q[5];
+		if (leaf) {
+			c.count = (uint8_t)leaf_count(r);
+			c.first = (uint8_t)(leaf_first(r) - tri_base);
 		}
 	}
-	cn[i] = c;
+	cn[i].c[k] = c;
+	if (k == 0) { // the 32-byte header as two 16-byte stores (ex, ey, ez, imask: bytes 12-15)
+		uint4 *h = reinterpret_cast<uint4 *>(&cn[i]);
+		h[0] = make_uint4(__float_as_uint(org[0]), __float_as_uint(org[1]),
+		                  __float_as_uint(org[2]),
+		                  ex[0] | (ex[1] << 8) | (ex[2] << 16) | (imask << 24));
+		h[1] = make_uint4(cb == kNone ? 0u : cb, tri_base, 0u, 0u);
+	}
 }
+static_assert(offsetof(CNode8, ex) == 12 && offsetof(CNode8, imask) == 15 &&
+                  offsetof(CNode8, child_base) == 16 && offsetof(CNode8, tri_base) == 20 &&
+                  offsetof(CNode8, c) == 32,
+              "CNode8 header layout");
 
 #define BUILD_TRY(call)                                                                        \
 	do {                                                                                       \
@@ -805,10 +958,10 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 	}
 	if (plan.compressed) {
 		if (host_checks)
-			k_compress<<<blocks_for(sc.n_nodes, 128), 128, 0, st>>>(
+			k_compress<<<blocks_for(8ull * sc.n_nodes, 256), 256, 0, st>>>(
 			    sc.nodes.as<Node8>(), sc.n_nodes, nullptr, sc.cnodes.as<CNode8>());
 		else
-			k_compress<<<blocks_for(plan.node_cap, 128), 128, 0, st>>>(
+			k_compress<<<blocks_for(8ull * plan.node_cap, 256), 256, 0, st>>>(
 			    sc.nodes.as<Node8>(), plan.node_cap, ctr + kCtrNodes, sc.cnodes.as<CNode8>());
 		sc.has_cnodes = true;
 	}
