@@ -345,6 +345,118 @@ def leg_precision(b, stream, steps):
     return res
 
 
+def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
+    """64 resident soup scenes (sizes log-uniform in [16, 1,048,576], seeds 5000+s) and
+    a request stream (seed 9000): scene uniform, rays log-uniform in [1,024, 1,048,576],
+    tags uniform over the 31 combinations; Poisson arrivals at fractions of the measured
+    capacity.  Latency = submit to records in (pinned) host memory, from the server's
+    own clock; the memory budget for request buffers is 2 GiB, 4 lanes."""
+    import threading
+
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    n_sc = 64
+    sizes = workloads.log_uniform_int(workloads.Stream(5000, 11), 16, 1_048_576, n_sc)
+    toff = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    T = int(toff[-1])
+    d_tris = torch.empty(T * 9, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for s_ in range(n_sc):
+        workloads.generate_dev(b, workloads.GEN_SOUP_TRIS, 5000 + s_, int(sizes[s_]),
+                               d_tris.data_ptr() + 36 * int(toff[s_]))
+    pool_n = 2 * 1_048_576
+    d_pool = torch.empty(pool_n * 6, dtype=torch.float32, device="cuda")
+    workloads.generate_dev(b, workloads.GEN_SOUP_RAYS, 9001, pool_n, d_pool.data_ptr())
+    b.sync()
+    h_pool = d_pool.cpu().pin_memory()
+    del d_pool
+    slots = 32
+    h_out = torch.empty(slots * 1_048_576 * 32, dtype=torch.uint8).pin_memory()
+    rs = workloads.Stream(9000, 1)
+    total = n_req * (1 + len(loads))
+    scene = np.minimum((rs.u01((total,)) * n_sc).astype(np.int64), n_sc - 1)
+    nray = workloads.log_uniform_int(rs, 1024, 1_048_576, total)
+    combo = np.minimum((rs.u01((total,)) * 31).astype(np.int64), 30)
+    start = (rs.u01((total,)) * (pool_n - 1_048_576)).astype(np.int64)
+    srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
+
+    def run(idx, rate):
+        """Submits requests idx at Poisson times of `rate` per second (0 = at once,
+        bounded only by the 32 output slots); returns latencies and the span."""
+        lat = [0.0] * len(idx)
+        free = [threading.Event() for _ in range(slots)]
+        for e in free:
+            e.set()
+        tickets = [None] * len(idx)
+        ready = [threading.Event() for _ in idx]
+
+        def waiter():
+            for j in range(len(idx)):
+                ready[j].wait()
+                lat[j] = srv.wait(tickets[j])
+                free[j % slots].set()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        gaps = -np.log(1.0 - np.random.default_rng(9002).random(len(idx))) / rate if rate else None
+        t0 = time.perf_counter()
+        due = t0
+        for j, i in enumerate(idx):
+            if rate:
+                due += gaps[j]
+                while time.perf_counter() < due:
+                    pass
+            free[j % slots].wait()
+            free[j % slots].clear()
+            tags = hitreg.TAG_COMBOS[int(combo[i])]
+            n = int(nray[i])
+            tickets[j] = srv.submit_ptr(int(scene[i]), h_pool.data_ptr() + 24 * int(start[i]), n,
+                                        tags, h_out.data_ptr() + (j % slots) * 1_048_576 * 32)
+            ready[j].set()
+        th.join()
+        span = time.perf_counter() - t0
+        return np.array(lat), span
+
+    res = {"workload": f"{n_sc} resident soup scenes ({T:,} tris); requests of 1,024 to "
+                       "1,048,576 rays (log-uniform), uniform scene and tag set; Poisson "
+                       "arrivals", "n_scenes": n_sc, "n_tris": T, "budget_bytes": 2 << 30,
+           "lanes": 4}
+    try:
+        idx = list(range(n_req))
+        run(idx[:50], 0)  # warm-up
+        lat, span = run(idx, 0)
+        rays = float(nray[idx].sum())
+        cap_mrays = rays / span / 1e6
+        cap_rps = n_req / span
+        res["capacity"] = {"mrays_s": cap_mrays, "requests_s": cap_rps,
+                           "p50_ms": float(np.percentile(lat, 50)),
+                           "p99_ms": float(np.percentile(lat, 99))}
+        res["loads"] = []
+        for k, f in enumerate(loads):
+            idx = list(range(n_req * (k + 1), n_req * (k + 2)))
+            w0 = srv.stat("waves")
+            lat, span = run(idx, f * cap_rps)
+            rays = float(nray[idx].sum())
+            res["loads"].append({"offered_fraction": f, "offered_requests_s": f * cap_rps,
+                                 "mrays_s": rays / span / 1e6,
+                                 "p50_ms": float(np.percentile(lat, 50)),
+                                 "p99_ms": float(np.percentile(lat, 99)),
+                                 "max_ms": float(lat.max()),
+                                 "waves": srv.stat("waves") - w0})
+            if log:
+                log(f"serving load {f}: {res['loads'][-1]}")
+        res["max_in_flight_waves"] = srv.stat("max_in_flight_waves")
+        res["max_wave_requests"] = srv.stat("max_wave_requests")
+        res["peak_bytes"] = srv.stat("peak_bytes")
+    finally:
+        srv.close()
+    del d_tris, h_out, h_pool
+    torch.cuda.empty_cache()
+    return res
+
+
 # --------------------------------------------------------------------------- GPU side
 
 def run_gpu(args, world, rank):
@@ -498,6 +610,8 @@ def run_gpu(args, world, rank):
         out["precision"] = leg_precision(b, stream, min(args.steps, 10))
     if "batch" in legs:
         out["batch"] = leg_batch(b, stream, min(args.steps, 10), log=log)
+    if "serving" in legs:
+        out["serving"] = leg_serving(b, stream, log=log)
     if rank == 0 and not args.no_cpu:
         _, cb = cpu_baseline(tris, rays, sample_rays=131_072)
         out["cpu_baseline"] = cb
@@ -513,8 +627,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="b200", choices=["b200", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="precision,batch",
-                    help="other configurations to measure: precision, batch (comma list)")
+    ap.add_argument("--legs", default="precision,batch,serving",
+                    help="other configurations to measure: precision, batch, serving "
+                         "(comma list; 'none' for the heightfield alone)")
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -184,6 +184,33 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
 
+/* Request server (no counterpart in portableRT): S scenes (device triangles and
+ * offsets as for prt_b200_batch_set_tris_dev) are built once and stay resident; requests
+ * (scene, host rays, record layout, host output) are admitted in arrival order while
+ * their device buffers (24 B per ray rounded up to 256 B, plus the records) fit in a
+ * region of budget_bytes reserved at creation, and each group of admitted requests
+ * (a wave) runs as one persistent launch on one of n_lanes streams, so up to n_lanes
+ * waves overlap.  Each request's records equal nearest_hits on its scene alone.  The
+ * node format is the context's at creation.  Host buffers should be pinned: a copy
+ * to or from pageable memory makes the scheduler wait for it.  Buffers belong to the
+ * caller until prt_b200_server_wait returns for the ticket. */
+typedef struct prt_b200_server prt_b200_server;
+int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_t *tri_off,
+                           uint32_t n_scenes, uint64_t budget_bytes, uint32_t n_lanes,
+                           prt_b200_server **server);
+void prt_b200_server_destroy(prt_b200_server *server);
+/* Queues a request (any thread); PRT_ERR_LIMIT if it can never fit the budget. */
+int prt_b200_server_submit(prt_b200_server *server, uint32_t scene, const float *rays6,
+                           uint64_t n_rays, uint32_t field_mask, uint32_t rec_size,
+                           const uint8_t offs[8], void *out_host, uint64_t *ticket);
+/* Blocks until the request is answered; latency_ms = submit to records in host memory.
+ * Returns the request's status; the ticket is then forgotten. */
+int prt_b200_server_wait(prt_b200_server *server, uint64_t ticket, double *latency_ms);
+/* "waves", "max_in_flight_waves", "max_wave_requests", "completed", "rays", "waiting",
+ * "bytes_in_use", "peak_bytes", "budget_bytes", "n_scenes", "n_tris". */
+int prt_b200_server_stat(prt_b200_server *server, const char *key, double *value);
+const char *prt_b200_server_last_error(prt_b200_server *server);
+
 /* Seeded synthetic workloads written straight into device memory (no counterpart in
  * portableRT, whose examples read meshes from files).  SplitMix64 streams; the same
  * generators as portablert_gb300/workloads.py (values that pass through log/cos may

@@ -21,6 +21,8 @@ EXPORTS = (
     "prt_b200_batch_create", "prt_b200_batch_destroy", "prt_b200_batch_set_tris_dev",
     "prt_b200_batch_query_dev", "prt_b200_batch_run_graph", "prt_b200_batch_sync",
     "prt_b200_batch_stat", "prt_b200_generate", "prt_b200_t_error",
+    "prt_b200_server_create", "prt_b200_server_destroy", "prt_b200_server_submit",
+    "prt_b200_server_wait", "prt_b200_server_stat", "prt_b200_server_last_error",
 )
 
 
@@ -88,6 +90,20 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_batch_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.prt_b200_generate.restype = c_int
     L.prt_b200_generate.argtypes = [vp, c_int, c_u64, c_u64, ctypes.c_double, vp, vp]
+    L.prt_b200_server_create.restype = c_int
+    L.prt_b200_server_create.argtypes = [vp, vp, ctypes.POINTER(c_u64), c_u32, c_u64, c_u32,
+                                         ctypes.POINTER(vp)]
+    L.prt_b200_server_destroy.restype = None
+    L.prt_b200_server_destroy.argtypes = [vp]
+    L.prt_b200_server_submit.restype = c_int
+    L.prt_b200_server_submit.argtypes = [vp, c_u32, vp, c_u64, c_u32, c_u32, ctypes.c_char_p, vp,
+                                         ctypes.POINTER(c_u64)]
+    L.prt_b200_server_wait.restype = c_int
+    L.prt_b200_server_wait.argtypes = [vp, c_u64, ctypes.POINTER(ctypes.c_double)]
+    L.prt_b200_server_stat.restype = c_int
+    L.prt_b200_server_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
+    L.prt_b200_server_last_error.restype = ctypes.c_char_p
+    L.prt_b200_server_last_error.argtypes = [vp]
     L.prt_b200_t_error.restype = c_int
     L.prt_b200_t_error.argtypes = [vp, vp, c_u64, vp, c_u64, vp, c_u32, c_u32, ctypes.c_char_p,
                                    ctypes.POINTER(ctypes.c_double)]

@@ -16,20 +16,15 @@
 #include <vector>
 
 #include "../../include/prt_b200.h"
+#include "prt_batch.cuh"
 #include "prt_build.cuh"
 #include "prt_ctx.cuh"
 #include "prt_traverse.cuh"
 
 namespace {
 
-constexpr int kSlots = 8; // launches that may be in flight on one batch
-
-struct Slot {
-	prt::DevBuf segs;  // SegDesc table of the launch
-	prt::DevBuf work;  // [0] ray counter, [1] error word, [16..31] visit counters
-	cudaEvent_t done = nullptr;
-	bool pending = false;
-};
+using prt::kSlots;
+using Slot = prt::BatchSlot;
 
 int bfail(prt_b200_ctx *ctx, int code, const std::string &msg) {
 	ctx->err = msg;
@@ -49,28 +44,6 @@ int bcuda(prt_b200_ctx *ctx, cudaError_t e, const char *what) {
 	} while (0)
 
 } // namespace
-
-struct prt_b200_batch {
-	prt_b200_ctx *ctx = nullptr;
-	prt::SceneGPU arena;
-	// The batch's own build scratch: a captured graph reads tables uploaded before the
-	// capture, so nothing outside the batch may overwrite them between replays.
-	prt::BuildScratch ws;
-	bool built = false;
-	prt::DevBuf scenes_fp32, scenes_comp; // SceneDesc[S] for each node format
-	Slot slots[kSlots];
-	int next_slot = 0;
-	double build_ms = 0.0;
-	unsigned long long visits[2] = {0, 0};
-	uint32_t *h_words = nullptr; // pinned: error word and visit counters read back
-	// CUDA graph of build + query
-	cudaGraph_t graph = nullptr;
-	cudaGraphExec_t gexec = nullptr;
-	size_t graph_key = 0;
-	Slot gslot;
-	prt::BuildPlan gplan;
-	bool graph_dirty = false;   // arena stats not read back since the last replay
-};
 
 namespace {
 

@@ -1,0 +1,485 @@
+// prt_serve.cu - a request server over resident scenes (continuous batching).
+//
+// The server keeps S built scenes resident in HBM (a batch, prt_batch.cu) and answers
+// nearest-hit requests (scene, host rays, record layout, host output) as they arrive:
+//
+//   submit  -> FIFO queue (any thread)
+//   admit   -> the scheduler thread takes requests from the head of the queue while
+//              their rays and records fit in the device memory budget (one region
+//              reserved at start-up, carved by a first-fit range allocator) and a
+//              lane is free; the admitted requests form one wave
+//   run     -> per wave, on the lane's stream: rays copied in, ONE persistent launch
+//              of the segment traversal over every request of the wave, records
+//              copied out; up to n_lanes waves are in flight at once, so requests
+//              that arrive while others run are admitted into the next wave as soon
+//              as memory and a lane are free, and their work overlaps on the device
+//   retire  -> each lane's completer thread waits for its wave, stamps the finish
+//              time, returns the memory and wakes the waiters
+//
+// A request's records are exactly nearest_hits<Tags...> on its scene alone: the wave's
+// launch gives each request its own segment (rays padded to whole warps), and the
+// traversal of a ray depends only on the ray, its scene and the record layout.
+//
+// No counterpart in the reference (portableRT answers one synchronous call at a time,
+// include/portableRT/nearest_hits_impl.hpp:28-36).
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/prt_b200.h"
+#include "prt_batch.cuh"
+#include "prt_range_alloc.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+constexpr uint32_t kMaxWaveRequests = 1024;
+constexpr uint64_t kMaxRequestRays = 1ull << 31;
+
+struct Request {
+	uint64_t id = 0;
+	uint32_t scene = 0, mask = 0, rec = 0;
+	uint8_t offs[8] = {};
+	const float *rays = nullptr;
+	uint64_t n = 0;
+	void *out = nullptr;
+	uint64_t off = 0, ray_bytes = 0, bytes = 0; // range in the budget region
+	Clock::time_point t_submit, t_launch, t_done;
+	int status = PRT_OK;
+	bool done = false;
+};
+
+struct Lane {
+	cudaStream_t st = nullptr;
+	cudaEvent_t ev = nullptr;
+	prt::DevBuf segs;                // SegDesc table of the wave
+	prt::DevBuf work;                // [0] ray counter, [1] error word, [4..7] visits
+	prt::SegDesc *h_segs = nullptr;  // pinned staging of the table
+	uint32_t *h_err = nullptr;       // pinned copy of the error word
+	std::vector<Request *> wave;     // requests in flight on this lane
+	bool launched = false;           // the wave's work (and event) has been queued
+	std::thread completer;
+	std::condition_variable cv;
+};
+
+} // namespace
+
+struct prt_b200_server {
+	prt_b200_ctx *ctx = nullptr;
+	prt_b200_batch *batch = nullptr;
+	int format = PRT_NODES_FP32;
+	prt::DevBuf region;
+	prt::RangeAllocator alloc;
+	std::vector<std::unique_ptr<Lane>> lanes;
+	std::thread sched;
+	std::mutex mu;
+	std::condition_variable cv_sched, cv_done;
+	std::deque<Request *> waiting;
+	std::unordered_map<uint64_t, Request *> reqs;
+	uint64_t next_id = 1;
+	bool stop = false;
+	std::string err;
+	// statistics
+	uint64_t waves = 0, in_flight = 0, max_in_flight = 0, max_wave_requests = 0;
+	uint64_t completed = 0, rays_done = 0;
+};
+
+namespace {
+
+// Records an error message; the caller holds the server's lock.
+int sfail(prt_b200_server *s, int code, const std::string &msg) {
+	s->err = msg;
+	return code;
+}
+
+int sfail_unlocked(prt_b200_server *s, int code, const std::string &msg) {
+	std::lock_guard<std::mutex> lk(s->mu);
+	return sfail(s, code, msg);
+}
+
+uint64_t round256(uint64_t b) { return (b + 255) & ~255ull; }
+
+Lane *free_lane(prt_b200_server *s) {
+	for (auto &l : s->lanes)
+		if (l->wave.empty())
+			return l.get();
+	return nullptr;
+}
+
+// Queues the wave's copies, launch and event on the lane's stream (no lock held).
+cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
+	prt_b200_batch *b = s->batch;
+	uint8_t *base = s->region.as<uint8_t>();
+	unsigned long long nv = 0;
+	const uint32_t k = (uint32_t)L.wave.size();
+	for (uint32_t i = 0; i < k; ++i) {
+		Request *r = L.wave[i];
+		prt::SegDesc &d = L.h_segs[i];
+		d.vbegin = nv;
+		d.rays = reinterpret_cast<const float *>(base + r->off);
+		d.out = base + r->off + r->ray_bytes;
+		d.n_rays = (uint32_t)r->n;
+		d.scene = r->scene;
+		d.mask = r->mask;
+		d.rec_size = r->rec;
+		std::memcpy(d.off, r->offs, 8);
+		d.store_mode = prt::store_mode_for(d.out);
+		d.pad = 0;
+		nv += (r->n + 31ull) & ~31ull;
+		cudaError_t e = cudaMemcpyAsync(base + r->off, r->rays, 24 * r->n,
+		                                cudaMemcpyHostToDevice, L.st);
+		if (e != cudaSuccess)
+			return e;
+	}
+	cudaError_t e = cudaMemcpyAsync(L.segs.p, L.h_segs, sizeof(prt::SegDesc) * k,
+	                                cudaMemcpyHostToDevice, L.st);
+	if (e == cudaSuccess)
+		e = cudaMemsetAsync(L.work.as<uint32_t>() + 1, 0, 4, L.st);
+	if (e != cudaSuccess)
+		return e;
+	prt::TravConfig cfg;
+	cfg.format = s->format;
+	cfg.block = s->ctx->block;
+	const prt::SceneDesc *tab = s->format == PRT_NODES_COMPRESSED
+	                                ? b->scenes_comp.as<prt::SceneDesc>()
+	                                : b->scenes_fp32.as<prt::SceneDesc>();
+	uint32_t *w = L.work.as<uint32_t>();
+	e = prt::launch_nearest_hits_segments(tab, L.segs.as<prt::SegDesc>(), k, nv, b->arena.depth,
+	                                      b->arena.leaf_size, b->arena.n_nodes, cfg, w,
+	                                      reinterpret_cast<unsigned long long *>(w + 4), w + 1,
+	                                      L.st, s->ctx->sms);
+	if (e != cudaSuccess)
+		return e;
+	for (uint32_t i = 0; i < k; ++i) {
+		Request *r = L.wave[i];
+		e = cudaMemcpyAsync(r->out, base + r->off + r->ray_bytes, (uint64_t)r->rec * r->n,
+		                    cudaMemcpyDeviceToHost, L.st);
+		if (e != cudaSuccess)
+			return e;
+	}
+	e = cudaMemcpyAsync(L.h_err, w + 1, 4, cudaMemcpyDeviceToHost, L.st);
+	if (e == cudaSuccess)
+		e = cudaEventRecord(L.ev, L.st);
+	return e;
+}
+
+// Finishes the requests of a lane's wave (caller holds the lock).
+void retire(prt_b200_server *s, Lane &L, int status, Clock::time_point t) {
+	for (Request *r : L.wave) {
+		r->t_done = t;
+		r->status = status;
+		r->done = true;
+		s->alloc.release(r->off, r->bytes);
+		++s->completed;
+		s->rays_done += r->n;
+	}
+	L.wave.clear();
+	L.launched = false;
+	--s->in_flight;
+	s->cv_done.notify_all();
+	s->cv_sched.notify_one();
+}
+
+void scheduler(prt_b200_server *s) {
+	cudaSetDevice(s->ctx->device);
+	std::unique_lock<std::mutex> lk(s->mu);
+	while (!s->stop) {
+		Lane *L = s->waiting.empty() ? nullptr : free_lane(s);
+		if (L) {
+			unsigned long long nv = 0;
+			while (!s->waiting.empty() && L->wave.size() < kMaxWaveRequests) {
+				Request *r = s->waiting.front();
+				const unsigned long long pad = (r->n + 31ull) & ~31ull;
+				if (nv + pad > (1ull << 31))
+					break;
+				const uint64_t off = s->alloc.alloc(r->bytes);
+				if (off == prt::RangeAllocator::kFail)
+					break; // FIFO: later requests wait behind the head
+				r->off = off;
+				r->t_launch = Clock::now();
+				nv += pad;
+				s->waiting.pop_front();
+				L->wave.push_back(r);
+			}
+		}
+		if (!L || L->wave.empty()) {
+			s->cv_sched.wait(lk); // a submit, a retired wave or stop
+			continue;
+		}
+		++s->waves;
+		++s->in_flight;
+		s->max_in_flight = std::max(s->max_in_flight, s->in_flight);
+		s->max_wave_requests = std::max<uint64_t>(s->max_wave_requests, L->wave.size());
+		lk.unlock();
+		const cudaError_t e = launch_wave(s, *L);
+		lk.lock();
+		if (e != cudaSuccess) {
+			// Nothing of a failed wave is waited for: wait for its stream so that no
+			// copy still uses the memory, then fail its requests.
+			lk.unlock();
+			cudaStreamSynchronize(L->st);
+			lk.lock();
+			s->err = std::string("server wave: ") + cudaGetErrorString(e);
+			retire(s, *L, PRT_ERR_CUDA, Clock::now());
+			continue;
+		}
+		L->launched = true;
+		L->cv.notify_one();
+	}
+	// Stopping: requests that were never admitted fail.
+	for (Request *r : s->waiting) {
+		r->status = PRT_ERR_ARG;
+		r->t_done = Clock::now();
+		r->done = true;
+	}
+	s->waiting.clear();
+	s->cv_done.notify_all();
+}
+
+void completer(prt_b200_server *s, Lane *L) {
+	cudaSetDevice(s->ctx->device);
+	std::unique_lock<std::mutex> lk(s->mu);
+	for (;;) {
+		L->cv.wait(lk, [&] { return L->launched || (s->stop && L->wave.empty()); });
+		if (!L->launched)
+			return;
+		lk.unlock();
+		// The wave's kernels end by themselves (bounded traversal steps), so this wait
+		// ends too.
+		const cudaError_t e = cudaEventSynchronize(L->ev);
+		const Clock::time_point t = Clock::now();
+		lk.lock();
+		int status = PRT_OK;
+		if (e != cudaSuccess) {
+			status = PRT_ERR_CUDA;
+			s->err = std::string("server wave: ") + cudaGetErrorString(e);
+		} else if (*L->h_err) {
+			status = PRT_ERR_DEVICE;
+			s->err = "server wave: kernel reported an error";
+		}
+		retire(s, *L, status, t);
+	}
+}
+
+void shutdown(prt_b200_server *s) {
+	{
+		std::lock_guard<std::mutex> lk(s->mu);
+		s->stop = true;
+	}
+	s->cv_sched.notify_all();
+	if (s->sched.joinable())
+		s->sched.join();
+	for (auto &l : s->lanes) {
+		{
+			std::lock_guard<std::mutex> lk(s->mu);
+			l->cv.notify_all();
+		}
+		if (l->completer.joinable())
+			l->completer.join();
+	}
+}
+
+} // namespace
+
+extern "C" {
+
+int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_t *tri_off,
+                           uint32_t n_scenes, uint64_t budget_bytes, uint32_t n_lanes,
+                           prt_b200_server **out) {
+	if (!ctx || !out)
+		return PRT_ERR_ARG;
+	*out = nullptr;
+	if (n_lanes < 1 || n_lanes > 16 || budget_bytes < 4096) {
+		ctx->err = "server: n_lanes must be in [1, 16] and the budget at least 4 KiB";
+		return PRT_ERR_ARG;
+	}
+	std::unique_ptr<prt_b200_server> s(new (std::nothrow) prt_b200_server());
+	if (!s)
+		return PRT_ERR_OOM;
+	s->ctx = ctx;
+	int rc = prt_b200_batch_create(ctx, &s->batch);
+	if (rc != PRT_OK)
+		return rc;
+	rc = prt_b200_batch_set_tris_dev(s->batch, d_tris, tri_off, n_scenes);
+	if (rc != PRT_OK) {
+		prt_b200_batch_destroy(s->batch);
+		return rc;
+	}
+	{
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		s->format = ctx->node_format;
+	}
+	cudaError_t e = cudaSetDevice(ctx->device);
+	if (e == cudaSuccess)
+		e = s->region.reserve(budget_bytes);
+	s->alloc.reset(budget_bytes, 256);
+	for (uint32_t i = 0; i < n_lanes && e == cudaSuccess; ++i) {
+		std::unique_ptr<Lane> L(new Lane());
+		e = cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking);
+		if (e == cudaSuccess)
+			e = cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming);
+		if (e == cudaSuccess)
+			e = L->segs.reserve(sizeof(prt::SegDesc) * kMaxWaveRequests);
+		if (e == cudaSuccess)
+			e = L->work.reserve(64);
+		if (e == cudaSuccess)
+			e = cudaMemset(L->work.p, 0, 64);
+		if (e == cudaSuccess)
+			e = cudaMallocHost(&L->h_segs, sizeof(prt::SegDesc) * kMaxWaveRequests);
+		if (e == cudaSuccess)
+			e = cudaMallocHost(&L->h_err, 16);
+		s->lanes.push_back(std::move(L));
+	}
+	if (e != cudaSuccess) {
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		ctx->err = std::string("server create: ") + cudaGetErrorString(e);
+		prt_b200_server_destroy(s.release());
+		return e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA;
+	}
+	prt_b200_server *sp = s.get();
+	for (auto &l : sp->lanes)
+		l->completer = std::thread(completer, sp, l.get());
+	sp->sched = std::thread(scheduler, sp);
+	*out = s.release();
+	return PRT_OK;
+}
+
+void prt_b200_server_destroy(prt_b200_server *s) {
+	if (!s)
+		return;
+	shutdown(s);
+	cudaSetDevice(s->ctx->device);
+	for (auto &l : s->lanes) {
+		if (l->st)
+			cudaStreamSynchronize(l->st);
+		l->segs.release();
+		l->work.release();
+		if (l->h_segs)
+			cudaFreeHost(l->h_segs);
+		if (l->h_err)
+			cudaFreeHost(l->h_err);
+		if (l->ev)
+			cudaEventDestroy(l->ev);
+		if (l->st)
+			cudaStreamDestroy(l->st);
+	}
+	for (auto &kv : s->reqs)
+		delete kv.second;
+	s->region.release();
+	if (s->batch)
+		prt_b200_batch_destroy(s->batch);
+	delete s;
+}
+
+int prt_b200_server_submit(prt_b200_server *s, uint32_t scene, const float *rays6, uint64_t n,
+                           uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                           void *out_host, uint64_t *ticket) {
+	if (!s || !ticket)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!prt::layout_ok(field_mask, rec_size, offs, why))
+		return sfail_unlocked(s, PRT_ERR_ARG, "server submit: " + why);
+	if (scene >= s->batch->arena.n_scenes)
+		return sfail_unlocked(s, PRT_ERR_ARG, "server submit: no such scene");
+	if (n && (!rays6 || !out_host))
+		return sfail_unlocked(s, PRT_ERR_ARG, "server submit: null buffer");
+	if (n > kMaxRequestRays)
+		return sfail_unlocked(s, PRT_ERR_LIMIT, "server submit: at most 2^31 rays per request");
+	std::unique_ptr<Request> r(new (std::nothrow) Request());
+	if (!r)
+		return PRT_ERR_OOM;
+	r->scene = scene;
+	r->mask = field_mask;
+	r->rec = rec_size;
+	std::memcpy(r->offs, offs, 8);
+	r->rays = rays6;
+	r->n = n;
+	r->out = out_host;
+	r->ray_bytes = round256(24 * n);
+	r->bytes = r->ray_bytes + (uint64_t)rec_size * n;
+	std::lock_guard<std::mutex> lk(s->mu);
+	if (s->stop)
+		return sfail(s, PRT_ERR_ARG, "server submit: server is stopping");
+	if (n && !s->alloc.fits_ever(r->bytes))
+		return sfail(s, PRT_ERR_LIMIT, "server submit: request larger than the memory budget");
+	r->id = s->next_id++;
+	r->t_submit = Clock::now();
+	*ticket = r->id;
+	Request *rp = r.release();
+	s->reqs[rp->id] = rp;
+	if (n == 0) {
+		rp->t_done = rp->t_submit;
+		rp->done = true;
+	} else {
+		s->waiting.push_back(rp);
+		s->cv_sched.notify_one();
+	}
+	return PRT_OK;
+}
+
+int prt_b200_server_wait(prt_b200_server *s, uint64_t ticket, double *latency_ms) {
+	if (!s)
+		return PRT_ERR_ARG;
+	std::unique_lock<std::mutex> lk(s->mu);
+	auto it = s->reqs.find(ticket);
+	if (it == s->reqs.end())
+		return sfail(s, PRT_ERR_ARG, "server wait: unknown ticket");
+	Request *r = it->second;
+	s->cv_done.wait(lk, [&] { return r->done; });
+	if (latency_ms)
+		*latency_ms =
+		    std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count();
+	const int status = r->status;
+	s->reqs.erase(it);
+	delete r;
+	return status;
+}
+
+int prt_b200_server_stat(prt_b200_server *s, const char *key, double *value) {
+	if (!s || !key || !value)
+		return PRT_ERR_ARG;
+	std::lock_guard<std::mutex> lk(s->mu);
+	const std::string k(key);
+	if (k == "waves")
+		*value = (double)s->waves;
+	else if (k == "max_in_flight_waves")
+		*value = (double)s->max_in_flight;
+	else if (k == "max_wave_requests")
+		*value = (double)s->max_wave_requests;
+	else if (k == "completed")
+		*value = (double)s->completed;
+	else if (k == "rays")
+		*value = (double)s->rays_done;
+	else if (k == "waiting")
+		*value = (double)s->waiting.size();
+	else if (k == "bytes_in_use")
+		*value = (double)s->alloc.used();
+	else if (k == "peak_bytes")
+		*value = (double)s->alloc.peak();
+	else if (k == "budget_bytes")
+		*value = (double)s->alloc.capacity();
+	else if (k == "n_scenes")
+		*value = (double)s->batch->arena.n_scenes;
+	else if (k == "n_tris")
+		*value = (double)s->batch->arena.n_tris;
+	else
+		return sfail(s, PRT_ERR_ARG, "unknown server statistic " + k);
+	return PRT_OK;
+}
+
+const char *prt_b200_server_last_error(prt_b200_server *s) {
+	if (!s)
+		return "null server";
+	std::lock_guard<std::mutex> lk(s->mu);
+	return s->err.c_str();
+}
+
+} // extern "C"

@@ -1,0 +1,129 @@
+"""Request server: every request's records equal nearest_hits on its scene alone, in
+any mix of scenes, sizes and tag sets, with requests arriving from several threads
+while others run; admission respects the memory budget."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from portablert_gb300 import hitreg, workloads
+from portablert_gb300._lib import PrtError
+
+pytestmark = pytest.mark.gpu
+
+COMBOS = hitreg.TAG_COMBOS
+
+
+def _fields_equal(a, b, lay):
+    for f in lay.numpy_dtype().names:
+        x, y = a[f], b[f]
+        if x.dtype.kind == "f":
+            x, y = x.view(np.uint32), y.view(np.uint32)
+        if not np.array_equal(x, y):
+            return f
+    return None
+
+
+def _scenes(torch, sizes, seed):
+    tris = [workloads.soup_tris(seed + s, n) for s, n in enumerate(sizes)]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
+    d = torch.from_numpy(np.concatenate(tris)).cuda()
+    torch.cuda.synchronize()
+    return tris, off, d
+
+
+def test_mix_equals_alone(gpu_backend):
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    sizes = [16, 300, 5000, 40_000, 1, 2, 120_000, 777]
+    tris, off, d_tris = _scenes(torch, sizes, 5000)
+    rng = np.random.default_rng(9000)
+    reqs = []
+    for i in range(60):
+        s = int(rng.integers(len(sizes)))
+        n = int(np.exp(rng.uniform(np.log(1), np.log(300_000))))
+        tags = COMBOS[int(rng.integers(len(COMBOS)))]
+        reqs.append((s, workloads.soup_rays(9100 + i, n), tags))
+    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=64 << 20, lanes=4)
+    results = [None] * len(reqs)
+    try:
+        def client(k):
+            for i in range(k, len(reqs), 3):
+                s, rays, tags = reqs[i]
+                # pinned host buffers, so copies do not hold up the scheduler
+                h_r = torch.from_numpy(rays).pin_memory()
+                lay = hitreg.layout(tags)
+                h_o = torch.zeros(len(rays) * lay.size, dtype=torch.uint8).pin_memory()
+                t = srv.submit_ptr(s, h_r.data_ptr(), len(rays), tags, h_o.data_ptr())
+                results[i] = (t, h_r, h_o)
+                time.sleep(0.0005 * (i % 4))
+        th = [threading.Thread(target=client, args=(k,)) for k in range(3)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        lat = [srv.wait(r[0]) for r in results]
+        assert all(x >= 0 for x in lat)
+        assert srv.stat("completed") == len(reqs)
+        assert srv.stat("waves") >= 2
+        assert srv.stat("peak_bytes") <= srv.stat("budget_bytes")
+        assert srv.stat("bytes_in_use") == 0
+    finally:
+        srv.close()
+    for i, (s, rays, tags) in enumerate(reqs):
+        lay = hitreg.layout(tags)
+        got = results[i][2].numpy().view(lay.numpy_dtype())
+        gpu_backend.set_tris(tris[s])
+        want = gpu_backend.nearest_hits(rays, tags)
+        bad = _fields_equal(got, want, lay)
+        assert bad is None, (i, s, len(rays), tags, bad)
+
+
+def test_budget_admission_and_limits(gpu_backend):
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    tris, off, d_tris = _scenes(torch, [2000, 3000], 5100)
+    tags = ("t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    n = 20_000  # 480,000 B of rays + 320,000 B of records per request
+    per = ((24 * n + 255) // 256) * 256 + lay.size * n
+    budget = 2 * per + 1000  # two requests fit at once, not three
+    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=budget, lanes=4)
+    try:
+        subs = [srv.submit(i % 2, workloads.soup_rays(5200 + i, n), tags) for i in range(9)]
+        for t, _ in subs:
+            srv.wait(t)
+        assert srv.stat("peak_bytes") <= budget
+        assert srv.stat("waves") >= 5  # at most two requests per wave
+        assert srv.stat("max_wave_requests") <= 2
+        for i, (_, out) in enumerate(subs):
+            gpu_backend.set_tris(tris[i % 2])
+            want = gpu_backend.nearest_hits(workloads.soup_rays(5200 + i, n), tags)
+            assert _fields_equal(out, want, lay) is None
+        with pytest.raises(PrtError):  # can never fit
+            srv.submit(0, workloads.soup_rays(1, 3 * n), tags)
+        with pytest.raises(PrtError):
+            srv.submit(7, workloads.soup_rays(1, 10), tags)  # no such scene
+        t, out = srv.submit(1, np.zeros((0, 6), np.float32), tags)  # empty request
+        assert srv.wait(t) >= 0 and len(out) == 0
+        with pytest.raises(PrtError):
+            srv.wait(123456789)
+    finally:
+        srv.close()
+
+
+def test_close_with_requests_queued(gpu_backend):
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    _, off, d_tris = _scenes(torch, [50_000], 5300)
+    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=32 << 20, lanes=2)
+    keep = [srv.submit(0, workloads.soup_rays(5400 + i, 100_000), ("valid",)) for i in range(6)]
+    srv.close()  # answers or fails every queued request, joins its threads
+    assert keep
