@@ -447,12 +447,93 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
                                  "waves": srv.stat("waves") - w0})
             if log:
                 log(f"serving load {f}: {res['loads'][-1]}")
+        # Work per ray on the largest scene (counting pass, 65,536 rays of the pool).
+        big = int(np.argmax(sizes))
+        b.set_tris_dev(d_tris.data_ptr() + 36 * int(toff[big]), int(sizes[big]))
+        b.set_option("count_visits", 1)
+        b.nearest_hits(h_pool.numpy().reshape(-1, 6)[:65536], ("valid",))
+        res["largest_scene"] = {"n_tris": int(sizes[big]),
+                                "node_visits_per_ray": b.stat("visits_nodes") / 65536,
+                                "tri_tests_per_ray": b.stat("visits_tris") / 65536}
+        b.set_option("count_visits", 0)
         res["max_in_flight_waves"] = srv.stat("max_in_flight_waves")
         res["max_wave_requests"] = srv.stat("max_wave_requests")
         res["peak_bytes"] = srv.stat("peak_bytes")
     finally:
         srv.close()
     del d_tris, h_out, h_pool
+    torch.cuda.empty_cache()
+    return res
+
+
+def leg_camera(b, stream, steps, size=4096, log=None):
+    """The examples' bunny set-up (4096 x 4096 pinhole sensor rays from (0, -0.02, -0.3),
+    sensor 0.05 wide at 0.05) on a bunny-sized synthetic mesh read back through the OBJ
+    reader (the bunny file is not part of this repository): rays built inside the
+    traversal (no ray buffer) against the same rays from a buffer, the Lambert shading
+    pass, and a frame rendered to pinned host memory (camera -> hits -> RGBA8 -> host)."""
+    import tempfile
+
+    import torch
+
+    from portablert_gb300 import obj
+    from portablert_gb300._lib import Camera
+
+    v, f = obj.blob_mesh(60, 84)
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "blob.obj")
+        obj.write_obj(path, v, f)
+        tris = obj.load_obj(path)
+    b.set_tris(tris)
+    cam = Camera()
+    cam.width = cam.height = size
+    cam.form = 0
+    cam.pos[:] = [0.0, -0.02, -0.3]
+    cam.sensor_size, cam.sensor_dist = 0.05, 0.05
+    cam.sensor_z = float(np.float32(-0.3) + np.float32(0.05))
+    n = size * size
+    tags = ("t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    rec = torch.empty(n * lay.size, dtype=torch.uint8, device="cuda")
+    rays = torch.empty(n * 6, dtype=torch.float32, device="cuda")
+    rgba = torch.empty(n * 4, dtype=torch.uint8, device="cuda")
+    h_rgba = torch.empty(n * 4, dtype=torch.uint8).pin_memory()
+    sp = stream.cuda_stream
+    torch.cuda.synchronize()
+    b.camera_rays(cam, rays.data_ptr(), sp)
+    fused = lambda: b.nearest_hits_camera(cam, rec.data_ptr(), tags, sp)
+    buffered = lambda: b.nearest_hits_dev(rays.data_ptr(), n, rec.data_ptr(), tags, sp)
+    shade = lambda: b.shade_lambert(rec.data_ptr(), tags, rgba.data_ptr(), cam=cam, stream=sp)
+
+    def frame():  # all on `stream`, which is torch's current stream here
+        fused()
+        shade()
+        h_rgba.copy_(rgba, non_blocking=True)
+
+    res = {"workload": f"{len(tris):,}-tri bunny-sized mesh (OBJ), {size}x{size} pinhole "
+                       "sensor rays of the examples' bunny set-up; tags t, primitive_id, valid",
+           "n_tris": len(tris), "n_rays": n}
+    for name, fn in (("fused_camera", fused), ("ray_buffer", buffered), ("shade", shade)):
+        for _ in range(3):
+            fn()
+        b.sync()
+        ms = float(np.median(_events(torch, stream, fn, max(3, steps))))
+        b.sync()
+        res[name] = {"ms": ms, "mrays_s": n / ms / 1e3}
+    for _ in range(2):
+        frame()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    k = max(3, min(steps, 10))
+    for _ in range(k):
+        frame()
+    torch.cuda.synchronize()
+    fms = 1e3 * (time.perf_counter() - t0) / k
+    res["frame_to_host"] = {"ms": fms, "fps": 1e3 / fms, "mrays_s": n / fms / 1e3,
+                            "d2h_bytes": 4 * n}
+    img = h_rgba.numpy().reshape(size, size, 4)
+    res["lit_pixels"] = int((img[:, :, 0] > 0).sum())
+    del rec, rays, rgba, h_rgba
     torch.cuda.empty_cache()
     return res
 
@@ -612,6 +693,8 @@ def run_gpu(args, world, rank):
         out["batch"] = leg_batch(b, stream, min(args.steps, 10), log=log)
     if "serving" in legs:
         out["serving"] = leg_serving(b, stream, log=log)
+    if "camera" in legs:
+        out["camera"] = leg_camera(b, stream, min(args.steps, 10), log=log)
     if rank == 0 and not args.no_cpu:
         _, cb = cpu_baseline(tris, rays, sample_rays=131_072)
         out["cpu_baseline"] = cb
@@ -627,8 +710,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="b200", choices=["b200", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="precision,batch,serving",
-                    help="other configurations to measure: precision, batch, serving "
+    ap.add_argument("--legs", default="precision,batch,serving,camera",
+                    help="other configurations to measure: precision, batch, serving, camera "
                          "(comma list; 'none' for the heightfield alone)")
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()

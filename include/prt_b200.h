@@ -211,6 +211,52 @@ int prt_b200_server_wait(prt_b200_server *server, uint64_t ticket, double *laten
 int prt_b200_server_stat(prt_b200_server *server, const char *key, double *value);
 const char *prt_b200_server_last_error(prt_b200_server *server);
 
+/* Pinhole sensor camera of portableRT's examples, generated on the device (no ray
+ * buffer, no ray copy).  Ray i is pixel x = i % width of row y = height - 1 - i / width
+ * (the examples' loop order), with origin pos and, per form:
+ *   PRT_CAMERA_PLANE (examples/bunny/main.cpp:101-124): sensor point (sx, sy, sensor_z),
+ *     direction = (sensor - pos) / |sensor - pos|;
+ *   PRT_CAMERA_PLANE_SENSOR_NORM (examples/validation/main.cpp:170-198): the same
+ *     direction divided by |sensor| instead;
+ *   PRT_CAMERA_ROTATED (examples/sponza/main.cpp:193-218): sensor point pos +
+ *     (cos_a sx + sin_a sensor_dist, sy, -sin_a sx + cos_a sensor_dist), direction
+ *     normalised by its length;
+ * where sx = sensor_size * (float(x) / width - 0.5) with the subtraction in double
+ * (likewise sy), all else in FP32 as the examples compute it: the rays are
+ * bit-identical to the examples'. */
+#define PRT_CAMERA_PLANE 0
+#define PRT_CAMERA_PLANE_SENSOR_NORM 1
+#define PRT_CAMERA_ROTATED 2
+typedef struct prt_b200_camera {
+	uint32_t width, height, form, pad;
+	float pos[3];
+	float sensor_size, sensor_dist, sensor_z, cos_a, sin_a;
+} prt_b200_camera;
+
+/* nearest_hits over the camera's width x height rays, records to device memory. */
+int prt_b200_nearest_hits_camera(prt_b200_ctx *ctx, const prt_b200_camera *camera,
+                                 uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                                 void *d_out, void *stream);
+/* The camera's rays written to device memory (6 floats each). */
+int prt_b200_camera_rays(prt_b200_ctx *ctx, const prt_b200_camera *camera, float *d_rays6,
+                         void *stream);
+/* Headless Lambert shading of examples/sponza/main.cpp:11-32,228-243 into RGBA8 (one
+ * grey byte in R, G and B, alpha 255): grey = 255 * clamp(N . -d, 0, 1) truncated, N the
+ * unit geometric normal of the hit triangle of the context's scene, black for a miss
+ * (t = inf).  Rays come from `camera` when it is not NULL, else from d_rays6; records
+ * (device) need the t and primitive_id fields. */
+int prt_b200_shade_lambert(prt_b200_ctx *ctx, const prt_b200_camera *camera,
+                           const float *d_rays6, uint64_t n, const void *d_records,
+                           uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                           uint8_t *d_rgba, void *stream);
+
+/* Triangles of a Wavefront OBJ file (positions of every face, polygons split as fans),
+ * in file order, as the examples read meshes for set_tris (examples/bunny/main.cpp:22-73).
+ * *tris9 is allocated by the library (free it with prt_b200_free); errors are reported
+ * by prt_b200_last_error(NULL).  Host only: needs no device. */
+int prt_b200_obj_load(const char *path, float **tris9, uint64_t *n_tris);
+void prt_b200_free(void *p);
+
 /* Seeded synthetic workloads written straight into device memory (no counterpart in
  * portableRT, whose examples read meshes from files).  SplitMix64 streams; the same
  * generators as portablert_gb300/workloads.py (values that pass through log/cos may

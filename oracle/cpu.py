@@ -63,6 +63,8 @@ def lib():
         L.orc_intersect_tri.restype = ctypes.c_int
         L.orc_ray_box.argtypes = [vp, vp, vp]
         L.orc_ray_box.restype = ctypes.c_int
+        L.orc_camera_rays.argtypes = [vp, vp]
+        L.orc_lambert.argtypes = [vp, vp, vp, sz, vp]
         _lib = L
     return _lib
 
@@ -164,3 +166,29 @@ def run_reference(tris, rays, combos: bool = False, repeat: int = 1):
                     with open(os.path.join(d, f), "rb") as fh:
                         raw[f[:-4]] = fh.read()
     return full, raw, timing
+
+
+def camera_rays(width, height, form, pos, sensor_size, sensor_dist=0.0, sensor_z=0.0,
+                cos_a=1.0, sin_a=0.0) -> np.ndarray:
+    """The examples' pinhole sensor camera (orc_camera_rays)."""
+    class _Cam(ctypes.Structure):
+        _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                    ("form", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                    ("pos", ctypes.c_float * 3), ("sensor_size", ctypes.c_float),
+                    ("sensor_dist", ctypes.c_float), ("sensor_z", ctypes.c_float),
+                    ("cos_a", ctypes.c_float), ("sin_a", ctypes.c_float)]
+    c = _Cam(width, height, form, 0, (ctypes.c_float * 3)(*pos), sensor_size, sensor_dist,
+             sensor_z, cos_a, sin_a)
+    out = np.zeros((width * height, 6), np.float32)
+    lib().orc_camera_rays(ctypes.byref(c), out.ctypes.data)
+    return out
+
+
+def lambert(tris, rays, hits) -> np.ndarray:
+    """RGBA8 Lambert image of full hit records (orc_lambert)."""
+    tris, rays = _f32(tris, 9), _f32(rays, 6)
+    hits = np.ascontiguousarray(hits, dtype=HIT_DTYPE)
+    out = np.zeros((len(rays), 4), np.uint8)
+    lib().orc_lambert(tris.ctypes.data, rays.ctypes.data, hits.ctypes.data, len(rays),
+                      out.ctypes.data)
+    return out

@@ -531,3 +531,80 @@ void orc_brute_force_robust(const float *tris, size_t n_tris, const float *rays,
 	job p = {NULL, tris, n_tris, rays, 0, 0, out, NULL, 3};
 	run_parallel(p, n, nthreads);
 }
+
+
+/* ---------------------------------------------------------------- camera and shading */
+
+/* The sensor coordinate: sensor_size * (float(k) / extent - 0.5), evaluated as the
+ * reference writes it (the float quotient widened to double by the 0.5 literal, the
+ * product rounded to float on assignment): bunny/main.cpp:103-104. */
+static float sensor_coord(float size, uint32_t k, uint32_t extent) {
+	return (float)((double)size * ((double)((float)k / (float)extent) - 0.5));
+}
+
+void orc_camera_rays(const orc_camera *c, float *rays) {
+	const uint64_t n = (uint64_t)c->width * c->height;
+	for (uint64_t i = 0; i < n; ++i) {
+		const uint32_t x = (uint32_t)(i % c->width);
+		const uint32_t y = c->height - 1u - (uint32_t)(i / c->width);
+		const float sx = sensor_coord(c->sensor_size, x, c->width);
+		const float sy = sensor_coord(c->sensor_size, y, c->height);
+		float sp[3];
+		if (c->form == 2) { /* sponza/main.cpp:199-207 */
+			const float dx = c->cos_a * sx + c->sin_a * c->sensor_dist;
+			const float dz = -c->sin_a * sx + c->cos_a * c->sensor_dist;
+			sp[0] = c->pos[0] + dx;
+			sp[1] = c->pos[1] + sy;
+			sp[2] = c->pos[2] + dz;
+		} else { /* bunny/main.cpp:106-107 */
+			sp[0] = sx;
+			sp[1] = sy;
+			sp[2] = c->sensor_z;
+		}
+		float d[3] = {sp[0] - c->pos[0], sp[1] - c->pos[1], sp[2] - c->pos[2]};
+		/* bunny/main.cpp:113-115 (|direction|); validation/main.cpp:187-188 (|sensor|) */
+		const float *l = c->form == 1 ? sp : d;
+		const float len = sqrtf(l[0] * l[0] + l[1] * l[1] + l[2] * l[2]);
+		float *r = rays + 6 * i;
+		r[0] = c->pos[0];
+		r[1] = c->pos[1];
+		r[2] = c->pos[2];
+		r[3] = d[0] / len;
+		r[4] = d[1] / len;
+		r[5] = d[2] / len;
+	}
+}
+
+/* sponza/main.cpp:11-32 */
+static float lambert_shade(const float *tri, const float *ray) {
+	const float e1[3] = {tri[3] - tri[0], tri[4] - tri[1], tri[5] - tri[2]};
+	const float e2[3] = {tri[6] - tri[0], tri[7] - tri[1], tri[8] - tri[2]};
+	float N[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+	              e1[0] * e2[1] - e1[1] * e2[0]};
+	const float lenN = sqrtf(N[0] * N[0] + N[1] * N[1] + N[2] * N[2]);
+	if ((double)fabsf(lenN) > 0.001) {
+		N[0] /= lenN;
+		N[1] /= lenN;
+		N[2] /= lenN;
+	}
+	const float dotNV = N[0] * -ray[3] + N[1] * -ray[4] + N[2] * -ray[5];
+	const float m = (1.0f < dotNV) ? 1.0f : dotNV; /* std::min(dotNV, 1.0f) */
+	return (0.0f < m) ? m : 0.0f;                  /* std::max(0.0f, m) */
+}
+
+/* sponza/main.cpp:228-243 */
+void orc_lambert(const float *tris, const float *rays, const orc_hit *hits, size_t n,
+                 uint8_t *rgba) {
+	for (size_t i = 0; i < n; ++i) {
+		uint8_t g = 0;
+		if (hits[i].t != INFINITY) {
+			const float color = 255 * lambert_shade(tris + 9 * (size_t)hits[i].primitive_id,
+			                                        rays + 6 * i);
+			g = (uint8_t)color;
+		}
+		rgba[4 * i + 0] = g;
+		rgba[4 * i + 1] = g;
+		rgba[4 * i + 2] = g;
+		rgba[4 * i + 3] = 255;
+	}
+}

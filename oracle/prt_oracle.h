@@ -73,6 +73,25 @@ void orc_nearest_hits(const orc_bvh *bvh, const float *rays6, size_t n_rays, orc
 void orc_hit_stats(const orc_bvh *bvh, const float *rays6, size_t n_rays, orc_stats *out,
                    int nthreads);
 
+/* Pinhole sensor camera of portableRT's examples; the same fields as prt_b200_camera.
+ * form 0: bunny/main.cpp:101-124 (sensor plane at z = sensor_z, direction normalised
+ *         by its own length); form 1: validation/main.cpp:170-198 (the same, normalised
+ *         by the length of the sensor position); form 2: sponza/main.cpp:193-218 (sensor
+ *         rotated about y by an angle with cosine cos_a and sine sin_a, at sensor_dist).
+ * Ray i is pixel x = i % width of row y = height - 1 - i / width. */
+typedef struct {
+	uint32_t width, height, form, pad_;
+	float pos[3];
+	float sensor_size, sensor_dist, sensor_z, cos_a, sin_a;
+} orc_camera;
+
+void orc_camera_rays(const orc_camera *cam, float *rays6);
+
+/* Lambert shade of sponza/main.cpp:11-32 and its pixel loop (:228-243): RGBA8 per ray,
+ * grey = 255 * clamp(N . -d) for a hit (t != inf), black otherwise; alpha 255. */
+void orc_lambert(const float *tris9, const float *rays6, const orc_hit *hits, size_t n,
+                 uint8_t *rgba);
+
 /* Leaf-only semantics by exhaustive search: a triangle counts when the reference slab
  * test passes on its own box and Moller-Trumbore accepts it; best = smallest t, ties
  * broken by the smaller primitive id.  No tree involved. */

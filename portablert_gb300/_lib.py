@@ -23,6 +23,8 @@ EXPORTS = (
     "prt_b200_batch_stat", "prt_b200_generate", "prt_b200_t_error",
     "prt_b200_server_create", "prt_b200_server_destroy", "prt_b200_server_submit",
     "prt_b200_server_wait", "prt_b200_server_stat", "prt_b200_server_last_error",
+    "prt_b200_nearest_hits_camera", "prt_b200_camera_rays", "prt_b200_shade_lambert",
+    "prt_b200_obj_load", "prt_b200_free",
 )
 
 
@@ -32,6 +34,17 @@ class Query(ctypes.Structure):
                 ("rays", ctypes.c_void_p), ("n_rays", ctypes.c_uint64),
                 ("out", ctypes.c_void_p), ("rec_size", ctypes.c_uint32),
                 ("offs", ctypes.c_uint8 * 8)]
+
+class Camera(ctypes.Structure):
+    """prt_b200_camera (include/prt_b200.h): the examples' pinhole sensor camera."""
+    _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("form", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("pos", ctypes.c_float * 3), ("sensor_size", ctypes.c_float),
+                ("sensor_dist", ctypes.c_float), ("sensor_z", ctypes.c_float),
+                ("cos_a", ctypes.c_float), ("sin_a", ctypes.c_float)]
+
+
+CAMERA_PLANE, CAMERA_PLANE_SENSOR_NORM, CAMERA_ROTATED = 0, 1, 2
 
 PRT_OK = 0
 ERRORS = {1: "PRT_ERR_ARG", 2: "PRT_ERR_CUDA", 3: "PRT_ERR_NO_DEVICE", 4: "PRT_ERR_NO_SCENE",
@@ -104,6 +117,19 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_server_stat.argtypes = [vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.prt_b200_server_last_error.restype = ctypes.c_char_p
     L.prt_b200_server_last_error.argtypes = [vp]
+    L.prt_b200_obj_load.restype = c_int
+    L.prt_b200_obj_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
+                                    ctypes.POINTER(c_u64)]
+    L.prt_b200_free.restype = None
+    L.prt_b200_free.argtypes = [vp]
+    cp = ctypes.POINTER(Camera)
+    L.prt_b200_nearest_hits_camera.restype = c_int
+    L.prt_b200_nearest_hits_camera.argtypes = [vp, cp, c_u32, c_u32, ctypes.c_char_p, vp, vp]
+    L.prt_b200_camera_rays.restype = c_int
+    L.prt_b200_camera_rays.argtypes = [vp, cp, vp, vp]
+    L.prt_b200_shade_lambert.restype = c_int
+    L.prt_b200_shade_lambert.argtypes = [vp, cp, vp, c_u64, vp, c_u32, c_u32, ctypes.c_char_p, vp,
+                                         vp]
     L.prt_b200_t_error.restype = c_int
     L.prt_b200_t_error.argtypes = [vp, vp, c_u64, vp, c_u64, vp, c_u32, c_u32, ctypes.c_char_p,
                                    ctypes.POINTER(ctypes.c_double)]

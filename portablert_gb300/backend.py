@@ -95,6 +95,29 @@ class B200Backend:
         self._need()
         self._check(self._L.prt_b200_sync(self.ctx))
 
+    # -- the examples' camera and shading, on the device ------------------------------------
+    def nearest_hits_camera(self, cam, out_ptr: int, tags=ALL_TAGS, stream: int = 0) -> None:
+        """Records of the camera's width x height rays (built on the device) to out_ptr."""
+        self._need()
+        lay = hitreg.layout(tags)
+        self._check(self._L.prt_b200_nearest_hits_camera(self.ctx, ctypes.byref(cam), lay.mask,
+                                                         lay.size, lay.offsets8(), out_ptr,
+                                                         stream or None))
+
+    def camera_rays(self, cam, out_ptr: int, stream: int = 0) -> None:
+        self._need()
+        self._check(self._L.prt_b200_camera_rays(self.ctx, ctypes.byref(cam), out_ptr,
+                                                 stream or None))
+
+    def shade_lambert(self, records_ptr: int, tags, rgba_ptr: int, cam=None, rays_ptr: int = 0,
+                      n: int = 0, stream: int = 0) -> None:
+        """RGBA8 Lambert image of device records (t and primitive_id needed)."""
+        self._need()
+        lay = hitreg.layout(tags)
+        self._check(self._L.prt_b200_shade_lambert(
+            self.ctx, ctypes.byref(cam) if cam is not None else None, rays_ptr or None, n,
+            records_ptr, lay.mask, lay.size, lay.offsets8(), rgba_ptr, stream or None))
+
     def t_error(self, tris_ptr: int, n_tris: int, rays_ptr: int, n_rays: int, out_ptr: int,
                 tags) -> dict:
         """FP64 score of the t values in a device record buffer (prt_b200_t_error)."""

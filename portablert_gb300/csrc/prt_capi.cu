@@ -15,6 +15,7 @@
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
+#include "prt_camera.cuh"
 #include "prt_ctx.cuh"
 #include "prt_traverse.cuh"
 
@@ -71,25 +72,6 @@ int check_device_errors(prt_b200_ctx *ctx) {
 	return PRT_OK;
 }
 
-// The bookkeeping of a caller's stream (created at its first query).
-int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out) {
-	for (auto &q : ctx->query_streams)
-		if (q.st == st) {
-			*out = &q;
-			return PRT_OK;
-		}
-	prt_b200_ctx::QueryStream q{st, nullptr, nullptr};
-	CAPI_TRY(ctx, cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming));
-	cudaError_t e = cudaMalloc(&q.counter, 64);
-	if (e != cudaSuccess) {
-		cudaEventDestroy(q.ev);
-		return cuda_fail(ctx, e, "nearest_hits_dev: stream counter");
-	}
-	ctx->query_streams.push_back(q);
-	*out = &ctx->query_streams.back();
-	return PRT_OK;
-}
-
 int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	// Queries still reading the old scene on callers' streams finish before the
 	// rebuild overwrites its arrays.
@@ -122,6 +104,32 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 }
 
 } // namespace
+
+namespace prt {
+
+// The message prt_b200_last_error(NULL) returns on this thread.
+void set_global_error(const std::string &msg) { g_create_error = msg; }
+
+// The bookkeeping of a caller's stream (created at its first query).
+int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out) {
+	for (auto &q : ctx->query_streams)
+		if (q.st == st) {
+			*out = &q;
+			return PRT_OK;
+		}
+	prt_b200_ctx::QueryStream q{st, nullptr, nullptr};
+	CAPI_TRY(ctx, cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming));
+	cudaError_t e = cudaMalloc(&q.counter, 64);
+	if (e != cudaSuccess) {
+		cudaEventDestroy(q.ev);
+		return cuda_fail(ctx, e, "nearest_hits_dev: stream counter");
+	}
+	ctx->query_streams.push_back(q);
+	*out = &ctx->query_streams.back();
+	return PRT_OK;
+}
+
+} // namespace prt
 
 extern "C" {
 
@@ -260,19 +268,15 @@ int prt_b200_set_tris_dev(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n) {
 	return do_build(ctx, d_tris9, n);
 }
 
-int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n,
-                              uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
-                              void *d_out, void *stream) {
-	if (!ctx)
-		return PRT_ERR_ARG;
-	std::string why;
-	if (!layout_ok(field_mask, rec_size, offs, why))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
-	if (n && (!d_rays6 || !d_out))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
-	if (reinterpret_cast<uintptr_t>(d_rays6) % 8 != 0)
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: rays must be 8-byte aligned");
-	std::lock_guard<std::mutex> lk(ctx->mu);
+} // extern "C"
+
+namespace {
+
+// One query of the context's scene on `stream` (NULL = the context's stream): rays from
+// d_rays6 or, when cam is not null, from the camera.  Caller holds the context's lock.
+int queue_query(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n, uint32_t field_mask,
+                uint32_t rec_size, const uint8_t offs[8], void *d_out, void *stream,
+                const prt_b200_camera *cam) {
 	if (!ctx->scene_set)
 		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
 	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
@@ -291,16 +295,52 @@ int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t 
 	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
 	prt_b200_ctx::QueryStream *qs = nullptr;
 	if (st != ctx->stream) {
-		int rc = query_stream(ctx, st, &qs);
+		int rc = prt::query_stream(ctx, st, &qs);
 		if (rc != PRT_OK)
 			return rc;
 	}
 	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays6, n, lay, d_out, cfg,
 	                                       qs ? qs->counter : ctx->d_work(), ctx->d_visits(),
-	                                       ctx->d_err(), st, ctx->sms));
+	                                       ctx->d_err(), st, ctx->sms, cam));
 	if (qs)
 		CAPI_TRY(ctx, cudaEventRecord(qs->ev, st));
 	return PRT_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n,
+                              uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                              void *d_out, void *stream) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!layout_ok(field_mask, rec_size, offs, why))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
+	if (n && (!d_rays6 || !d_out))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
+	if (reinterpret_cast<uintptr_t>(d_rays6) % 8 != 0)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits: rays must be 8-byte aligned");
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	return queue_query(ctx, d_rays6, n, field_mask, rec_size, offs, d_out, stream, nullptr);
+}
+
+int prt_b200_nearest_hits_camera(prt_b200_ctx *ctx, const prt_b200_camera *camera,
+                                 uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
+                                 void *d_out, void *stream) {
+	if (!ctx)
+		return PRT_ERR_ARG;
+	std::string why;
+	if (!prt::camera_ok(camera, why) || !layout_ok(field_mask, rec_size, offs, why))
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: " + why);
+	if (!d_out)
+		return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: null output");
+	std::lock_guard<std::mutex> lk(ctx->mu);
+	const prt_b200_camera cam = *camera;
+	return queue_query(ctx, nullptr, (uint64_t)cam.width * cam.height, field_mask, rec_size,
+	                   offs, d_out, stream, &cam);
 }
 
 int prt_b200_sync(prt_b200_ctx *ctx) {

@@ -58,6 +58,11 @@ struct prt_b200_ctx {
 
 namespace prt {
 
+// The bookkeeping of a caller's stream that reads the context's scene (created at its
+// first use): record ->ev on the stream after the work, and set_tris waits for it.
+// Caller holds the context's lock.
+int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out);
+
 // Validates a HitReg layout descriptor.
 inline bool layout_ok(uint32_t mask, uint32_t rec, const uint8_t *off, std::string &why) {
 	if (mask == 0 || mask > 31u) {

@@ -34,6 +34,7 @@
 #include <algorithm>
 
 #include "../../include/prt_b200.h"
+#include "prt_camera.cuh"
 #include "prt_traverse.cuh"
 
 namespace prt {
@@ -60,6 +61,8 @@ struct TravArgs {
 	uint32_t *counter;
 	uint32_t *err;
 	unsigned long long *visits;
+	uint32_t use_cam;        // 1: rays of the single run come from `cam`, not seg0.rays
+	prt_b200_camera cam;
 };
 
 // Per-warp shared memory: fixed part, then the queue and the pool (sizes per launch).
@@ -226,9 +229,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_trace8(TravArgs a) {
 		const void *__restrict__ nodes = sd.nodes;
 
 		if ((uint32_t)lane < nb) {
-			const float2 *rp = reinterpret_cast<const float2 *>(S.seg.rays + 6 * (size_t)(local + lane));
-			const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
-			const RayC r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+			RayC r;
+			if (a.use_cam) {
+				float o[3], d[3];
+				camera_ray(a.cam, local + lane, o, d);
+				r = make_ray(o[0], o[1], o[2], d[0], d[1], d[2]);
+			} else {
+				const float2 *rp =
+				    reinterpret_cast<const float2 *>(S.seg.rays + 6 * (size_t)(local + lane));
+				const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
+				r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
+			}
 			float *sr = S.ray[lane];
 			sr[0] = r.ox; sr[1] = r.oy; sr[2] = r.oz;
 			sr[3] = r.dx; sr[4] = r.dy; sr[5] = r.dz;
@@ -506,13 +517,18 @@ int traversal_stack_depth() { return kMaxDepth; }
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
                                 uint32_t *d_work, unsigned long long *d_visits, uint32_t *d_err,
-                                cudaStream_t st, int sm_count) {
+                                cudaStream_t st, int sm_count, const prt_b200_camera *cam) {
 	if (cfg.count)
 		cudaMemsetAsync(d_visits, 0, 2 * sizeof(unsigned long long), st);
 	const uint64_t chunk = 1ull << 31;
+	if (cam && n > chunk)
+		return cudaErrorInvalidValue; // camera rays are numbered within one launch
 	for (uint64_t s = 0; s < n; s += chunk) {
 		const uint64_t m = std::min(chunk, n - s);
 		TravArgs a;
+		a.use_cam = cam ? 1u : 0u;
+		if (cam)
+			a.cam = *cam;
 		a.scenes = nullptr;
 		a.segs = nullptr;
 		a.n_segs = 0;
@@ -523,7 +539,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.scene0.root = 0;
 		a.scene0.n_tris = (uint32_t)sc.n_tris;
 		a.seg0.vbegin = 0;
-		a.seg0.rays = d_rays + 6 * s;
+		a.seg0.rays = cam ? nullptr : d_rays + 6 * s;
 		a.seg0.out = static_cast<uint8_t *>(d_out) + s * lay.rec_size;
 		a.seg0.n_rays = (uint32_t)m;
 		a.seg0.scene = 0;

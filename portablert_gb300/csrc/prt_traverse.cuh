@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/prt_b200.h"
 #include "prt_build.cuh"
 
 namespace prt {
@@ -49,13 +50,15 @@ struct SegDesc {
 // Levels of the 8-wide tree the traversal can walk.
 int traversal_stack_depth();
 
-// Queues one nearest-hit pass over n rays of one scene (device memory, 6 floats each)
-// on `st`.  d_work: device scratch (ray counter); d_visits: 2 uint64 counters (node
-// visits, triangle tests), used when cfg.count.
+// Queues one nearest-hit pass over n rays of one scene (device memory, 6 floats each,
+// or when cam is not null the camera's rays 0..n-1, n <= 2^31) on `st`.  d_work:
+// device scratch (ray counter); d_visits: 2 uint64 counters (node visits, triangle
+// tests), used when cfg.count.
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
                                 uint32_t *d_work, unsigned long long *d_visits, uint32_t *d_err,
-                                cudaStream_t st, int sm_count);
+                                cudaStream_t st, int sm_count,
+                                const prt_b200_camera *cam = nullptr);
 
 // One persistent launch over several runs of rays, each against its own scene and with
 // its own output layout.  d_scenes / d_segs: device copies of the tables (segments

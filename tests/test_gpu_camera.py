@@ -1,0 +1,121 @@
+"""The examples' camera built on the device, traversal fused with it, and the headless
+Lambert shading: bit-identical to the CPU oracle's restatement of the examples."""
+import math
+
+import numpy as np
+import pytest
+
+from parity import compare
+from portablert_gb300 import hitreg, obj
+from portablert_gb300._lib import Camera
+
+pytestmark = pytest.mark.gpu
+
+TAGS = hitreg.TAGS
+F32 = np.float32
+
+
+def _cameras(w, h):
+    """The bunny (form 0), validation (form 1) and sponza (form 2) set-ups."""
+    bunny = dict(width=w, height=h, form=0, pos=(0.0, -0.02, -0.3), sensor_size=0.05,
+                 sensor_dist=0.05, sensor_z=float(F32(-0.3) + F32(0.05)))
+    valid = dict(width=w, height=h, form=1, pos=(0.0, 0.0, -0.5), sensor_size=0.05,
+                 sensor_dist=0.05, sensor_z=float(F32(-0.5) + F32(0.05)))
+    a = F32(-1.58)
+    sponza = dict(width=w, height=h, form=2, pos=(0.3, 0.1, -0.05), sensor_size=0.05,
+                  sensor_dist=0.05, cos_a=float(F32(math.cos(a))), sin_a=float(F32(math.sin(a))))
+    return [bunny, valid, sponza]
+
+
+def _ccam(d):
+    c = Camera()
+    c.width, c.height, c.form = d["width"], d["height"], d["form"]
+    c.pos[:] = list(d["pos"])
+    c.sensor_size, c.sensor_dist = d["sensor_size"], d.get("sensor_dist", 0.0)
+    c.sensor_z, c.cos_a, c.sin_a = d.get("sensor_z", 0.0), d.get("cos_a", 1.0), d.get("sin_a", 0.0)
+    return c
+
+
+def _ocam(oracle_lib, d):
+    return oracle_lib.camera_rays(d["width"], d["height"], d["form"], d["pos"], d["sensor_size"],
+                                  d.get("sensor_dist", 0.0), d.get("sensor_z", 0.0),
+                                  d.get("cos_a", 1.0), d.get("sin_a", 0.0))
+
+
+@pytest.fixture(scope="module")
+def blob(tmp_path_factory):
+    v, f = obj.blob_mesh(40, 48)
+    p = tmp_path_factory.mktemp("mesh") / "blob.obj"
+    obj.write_obj(str(p), v, f)
+    return obj.load_obj(str(p))
+
+
+def test_camera_rays_equal_oracle(gpu_backend, oracle_lib):
+    import torch
+
+    for d in _cameras(97, 61) + _cameras(256, 256):
+        n = d["width"] * d["height"]
+        out = torch.empty(n * 6, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        gpu_backend.camera_rays(_ccam(d), out.data_ptr())
+        gpu_backend.sync()
+        got = out.cpu().numpy().reshape(n, 6)
+        want = _ocam(oracle_lib, d)
+        assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), d
+
+
+def test_fused_camera_traversal_and_shading(gpu_backend, oracle_lib, blob):
+    import torch
+
+    gpu_backend.set_tris(blob)
+    bvh = oracle_lib.BVH(blob)
+    lay = hitreg.layout(TAGS)
+    for d in _cameras(320, 200):
+        n = d["width"] * d["height"]
+        cam = _ccam(d)
+        rec = torch.zeros(n * lay.size, dtype=torch.uint8, device="cuda")
+        torch.cuda.synchronize()
+        gpu_backend.nearest_hits_camera(cam, rec.data_ptr(), TAGS)
+        gpu_backend.sync()
+        got = rec.cpu().numpy().view(lay.numpy_dtype())
+        rays = _ocam(oracle_lib, d)
+        want = bvh.nearest_hits(rays)
+        assert (want["valid"] != 0).sum() > n // 50, d  # the mesh is in view
+        rep = compare(got, want, TAGS, blob, rays, oracle_lib)
+        assert rep["n_bad"] == 0, rep["bad"][:10]
+        # Lambert from the fused camera and from a ray buffer: both equal the oracle's
+        # shading of the same hits (the GPU's records, so exact ties in t shade alike).
+        hits = np.zeros(n, oracle_lib.HIT_DTYPE)
+        for f in ("t", "primitive_id", "valid"):
+            hits[f] = got[f]
+        want_rgba = oracle_lib.lambert(blob, rays, hits)
+        assert len(np.unique(want_rgba[:, 0])) > 20  # shading varies over the image
+        for use_cam in (True, False):
+            rgba = torch.zeros(n * 4, dtype=torch.uint8, device="cuda")
+            d_rays = torch.from_numpy(rays).cuda()
+            torch.cuda.synchronize()
+            if use_cam:
+                gpu_backend.shade_lambert(rec.data_ptr(), TAGS, rgba.data_ptr(), cam=cam)
+            else:
+                gpu_backend.shade_lambert(rec.data_ptr(), TAGS, rgba.data_ptr(),
+                                          rays_ptr=d_rays.data_ptr(), n=n)
+            gpu_backend.sync()
+            assert np.array_equal(rgba.cpu().numpy().reshape(n, 4), want_rgba), (d, use_cam)
+
+
+def test_camera_arguments_checked(gpu_backend):
+    import torch
+
+    from portablert_gb300._lib import PrtError
+
+    gpu_backend.set_tris(np.array([[-1, -1, 0, 1, -1, 0, 0, 1, 0]], np.float32))
+    out = torch.zeros(64, dtype=torch.uint8, device="cuda")
+    bad = _ccam(dict(width=0, height=4, form=0, pos=(0, 0, -1), sensor_size=0.05))
+    with pytest.raises(PrtError):
+        gpu_backend.nearest_hits_camera(bad, out.data_ptr(), TAGS)
+    bad = _ccam(dict(width=4, height=4, form=7, pos=(0, 0, -1), sensor_size=0.05))
+    with pytest.raises(PrtError):
+        gpu_backend.camera_rays(bad, out.data_ptr())
+    with pytest.raises(PrtError):  # records without primitive_id cannot be shaded
+        gpu_backend.shade_lambert(out.data_ptr(), ("t", "valid"), out.data_ptr(),
+                                  rays_ptr=out.data_ptr(), n=1)
