@@ -42,12 +42,33 @@ def _ocam(oracle_lib, d):
                                   d.get("cos_a", 1.0), d.get("sin_a", 0.0))
 
 
-@pytest.fixture(scope="module")
-def blob(tmp_path_factory):
-    v, f = obj.blob_mesh(40, 48)
+def _mesh(tmp_path_factory, **kw):
+    v, f = obj.blob_mesh(40, 48, **kw)
     p = tmp_path_factory.mktemp("mesh") / "blob.obj"
     obj.write_obj(str(p), v, f)
     return obj.load_obj(str(p))
+
+
+@pytest.fixture(scope="module")
+def blob(tmp_path_factory):
+    """Bunny-sized: the examples' lambert_shade leaves normals of such small triangles
+    unnormalised (|N| < 0.001), so its image is black, as the reference's would be."""
+    return _mesh(tmp_path_factory)
+
+
+@pytest.fixture(scope="module")
+def big_blob(tmp_path_factory):
+    """Radius 1 at z = 3, in front of a camera at the origin: normals are normalised."""
+    return _mesh(tmp_path_factory, centre=(0.0, 0.0, 3.0), radius=1.0)
+
+
+def _front_cameras(w, h):
+    plane = dict(width=w, height=h, form=0, pos=(0.0, 0.0, 0.0), sensor_size=0.05,
+                 sensor_z=0.05)
+    a = F32(0.2)
+    rot = dict(width=w, height=h, form=2, pos=(0.0, 0.1, 0.0), sensor_size=0.05,
+               sensor_dist=0.05, cos_a=float(F32(math.cos(a))), sin_a=float(F32(math.sin(a))))
+    return [plane, rot]
 
 
 def test_camera_rays_equal_oracle(gpu_backend, oracle_lib):
@@ -64,13 +85,16 @@ def test_camera_rays_equal_oracle(gpu_backend, oracle_lib):
         assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), d
 
 
-def test_fused_camera_traversal_and_shading(gpu_backend, oracle_lib, blob):
+@pytest.mark.parametrize("scene", ["bunny_sized", "unit_sized"])
+def test_fused_camera_traversal_and_shading(gpu_backend, oracle_lib, blob, big_blob, scene):
     import torch
 
-    gpu_backend.set_tris(blob)
-    bvh = oracle_lib.BVH(blob)
+    mesh, cams = (blob, _cameras(320, 200)) if scene == "bunny_sized" else \
+        (big_blob, _front_cameras(320, 200))
+    gpu_backend.set_tris(mesh)
+    bvh = oracle_lib.BVH(mesh)
     lay = hitreg.layout(TAGS)
-    for d in _cameras(320, 200):
+    for d in cams:
         n = d["width"] * d["height"]
         cam = _ccam(d)
         rec = torch.zeros(n * lay.size, dtype=torch.uint8, device="cuda")
@@ -81,15 +105,16 @@ def test_fused_camera_traversal_and_shading(gpu_backend, oracle_lib, blob):
         rays = _ocam(oracle_lib, d)
         want = bvh.nearest_hits(rays)
         assert (want["valid"] != 0).sum() > n // 50, d  # the mesh is in view
-        rep = compare(got, want, TAGS, blob, rays, oracle_lib)
+        rep = compare(got, want, TAGS, mesh, rays, oracle_lib)
         assert rep["n_bad"] == 0, rep["bad"][:10]
         # Lambert from the fused camera and from a ray buffer: both equal the oracle's
         # shading of the same hits (the GPU's records, so exact ties in t shade alike).
         hits = np.zeros(n, oracle_lib.HIT_DTYPE)
         for f in ("t", "primitive_id", "valid"):
             hits[f] = got[f]
-        want_rgba = oracle_lib.lambert(blob, rays, hits)
-        assert len(np.unique(want_rgba[:, 0])) > 20  # shading varies over the image
+        want_rgba = oracle_lib.lambert(mesh, rays, hits)
+        if scene == "unit_sized":
+            assert len(np.unique(want_rgba[:, 0])) > 20  # shading varies over the image
         for use_cam in (True, False):
             rgba = torch.zeros(n * 4, dtype=torch.uint8, device="cuda")
             d_rays = torch.from_numpy(rays).cuda()
