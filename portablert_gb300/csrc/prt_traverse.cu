@@ -86,6 +86,14 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 	return m;
 }
 
+// One 32-byte read-only load (sm_100 and later; p 32-byte aligned): a whole child
+// record, or a compressed node's header, in one instruction and one L1 sector.
+__device__ __forceinline__ void ld_nc_256(const void *p, float4 &a, float4 &b) {
+	asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+	    : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+	    : "l"(p));
+}
+
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
 	return r.kind == 0 ? regular_box(r, lx, hx, ly, hy, lz, hz)
@@ -138,9 +146,8 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 	child = 0;
 	leaf_n = 0;
 	if (FMT == PRT_NODES_FP32) {
-		const float4 *cp =
-		    reinterpret_cast<const float4 *>(&(static_cast<const Node8 *>(nodes) + node)->c[k]);
-		const float4 lo = __ldg(cp), hi = __ldg(cp + 1);
+		float4 lo, hi;
+		ld_nc_256(&(static_cast<const Node8 *>(nodes) + node)->c[k], lo, hi);
 		const uint32_t ref = __float_as_uint(lo.w);
 		if (ref != kNone) {
 			inner = !ref_is_leaf(ref);
@@ -150,8 +157,11 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 		}
 	} else {
 		const CNode8 *cn = static_cast<const CNode8 *>(nodes) + node;
-		const uint4 w0 = __ldg(reinterpret_cast<const uint4 *>(cn));
-		const uint2 w1 = __ldg(reinterpret_cast<const uint2 *>(cn) + 2);
+		float4 h0, h1;
+		ld_nc_256(cn, h0, h1); // the 32-byte header (96-byte nodes keep it 32-byte aligned)
+		const uint4 w0 = make_uint4(__float_as_uint(h0.x), __float_as_uint(h0.y),
+		                            __float_as_uint(h0.z), __float_as_uint(h0.w));
+		const uint2 w1 = make_uint2(__float_as_uint(h1.x), __float_as_uint(h1.y));
 		const uint2 ck = __ldg(reinterpret_cast<const uint2 *>(&cn->c[k]));
 		const uint32_t imask = byte_of(w0.w, 3);
 		const uint32_t m = byte_of(ck.y, 2);
