@@ -604,9 +604,7 @@ __global__ void k_relayout(const float *__restrict__ tris, const uint32_t *__res
 	tri4[3 * (size_t)i + 2] = make_float4(t[6], t[7], t[8], 0.0f);
 }
 
-__device__ __forceinline__ float cdec(float o, uint32_t q, float s) {
-	return __fadd_rn(o, __fmul_rn((float)q, s));
-}
+__device__ __forceinline__ float cdec(float o, uint32_t q, float s) { return cdec_f(o, (float)q, s); }
 
 // Largest q in [0, 255] whose decoded value is <= v (decoding is monotone in q and
 // q = 0 decodes to the origin, which is <= every child bound).  The estimate comes from

@@ -47,9 +47,15 @@ struct alignas(16) Node8 {
 };
 static_assert(sizeof(Node8) == 256, "Node8 layout");
 
+// A decoded compressed bound, origin + q * scale with one rounding (a fused multiply-add:
+// q <= 255 times a power of two is exact, so this is o + q * s correctly rounded, even
+// where q * s alone would overflow).  The builder verifies every bound with this
+// function and the traversal decodes with it, so the two agree bit for bit.
+__device__ __forceinline__ float cdec_f(float o, float q, float s) { return __fmaf_rn(q, s, o); }
+
 // Compressed 8-wide node (96 B = 37.5 % of Node8), the same tree as Node8.  Child box
 // k, per axis a: lo = origin_a + q_lo * 2^(e_a - 127), hi = origin_a + q_hi * 2^(e_a - 127),
-// evaluated in FP32 exactly as the traversal does (cdec); the builder chooses each q so
+// evaluated in FP32 exactly as the traversal does (cdec_f); the builder chooses each q so
 // that the decoded box contains the child's FP32 box (rounded outward), which keeps
 // every box test conservative.  Child k is an inner node when bit k of imask is set, at
 // index child_base + (number of inner children before k); otherwise, when count > 0,

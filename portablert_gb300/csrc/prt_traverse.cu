@@ -102,6 +102,13 @@ __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, floa
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 
+// float(byte k of w), exactly: the byte placed in the mantissa of 2^23 (one byte
+// permute), minus 2^23 -- full-rate instructions instead of an integer conversion.
+__device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
+	return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k)),
+	                 8388608.0f);
+}
+
 __device__ __forceinline__ RayC slot_ray(const WarpFixed &S, uint32_t s) {
 	RayC r;
 	r.ox = S.ray[s][0];
@@ -172,12 +179,12 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 			const float sz = cscale((uint8_t)byte_of(w0.w, 2));
 			const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
 			            oz = __uint_as_float(w0.z);
-			const float lx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 0), sx));
-			const float hx = __fadd_rn(ox, __fmul_rn((float)byte_of(ck.x, 1), sx));
-			const float ly = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 2), sy));
-			const float hy = __fadd_rn(oy, __fmul_rn((float)byte_of(ck.x, 3), sy));
-			const float lz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 0), sz));
-			const float hz = __fadd_rn(oz, __fmul_rn((float)byte_of(ck.y, 1), sz));
+			const float lx = cdec_f(ox, byte_as_float(ck.x, 0), sx);
+			const float hx = cdec_f(ox, byte_as_float(ck.x, 1), sx);
+			const float ly = cdec_f(oy, byte_as_float(ck.x, 2), sy);
+			const float hy = cdec_f(oy, byte_as_float(ck.x, 3), sy);
+			const float lz = cdec_f(oz, byte_as_float(ck.y, 0), sz);
+			const float hz = cdec_f(oz, byte_as_float(ck.y, 1), sz);
 			hit = box_test(r, lx, hx, ly, hy, lz, hz);
 			if (inner) {
 				child = w1.x + __popc(imask & ((1u << k) - 1u));
