@@ -179,6 +179,11 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  and a tree it does not fit makes the query fail with
  *                  PRT_ERR_DEVICE, never a wrong answer)
  *   "build_compressed" 1 = set_tris also builds the compressed nodes (default 1)
+ *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
+ *                  copies and traversals overlap (default 8)
+ *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
+ *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
+ *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);

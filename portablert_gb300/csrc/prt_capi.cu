@@ -382,14 +382,30 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 	cfg.format = ctx->node_format;
 	cfg.block = ctx->block;
 	cfg.count = ctx->count;
-	// Chunks: about kPipe of them, at least 2^18 rays each (whole warps), one when the
-	// visit counters are on (each launch would reset them).  Chunk c is copied in on s_in,
-	// traversed on stream c % 2 (so a chunk's last blocks overlap the next chunk's first)
-	// and copied out on s_out.  Every chunk has its own rays, records and events; the two
-	// compute streams have their own ray counters.
-	const uint64_t per = (n + prt_b200_ctx::kPipe - 1) / prt_b200_ctx::kPipe;
-	const uint64_t chunk = ctx->count ? n : std::max<uint64_t>(1ull << 18, (per + 31) & ~31ull);
-	const int nc = (int)((n + chunk - 1) / chunk);
+	// Chunks: pipe_chunks of them (fewer when a chunk would hold under pipe_min_rays), one
+	// when the visit counters are on (each launch would reset them).  With pipe_ramp the
+	// sizes ramp up and down (weights 1, 2, 4, 8, ..., 8, 4, 2, 1), so the copy-in of the
+	// first chunk and the copy-out of the last, which nothing overlaps, are short.  Chunk
+	// c is copied in on s_in, traversed on stream c % 2 (so a chunk's last blocks overlap
+	// the next chunk's first) and copied out on s_out.  Every chunk has its own rays,
+	// records and events; the two compute streams have their own ray counters.
+	int nc = ctx->count ? 1 : ctx->pipe_chunks;
+	if (nc > 1 && n / (uint64_t)nc < ctx->pipe_min_rays)
+		nc = (int)std::max<uint64_t>(1, n / ctx->pipe_min_rays);
+	uint64_t bnd[prt_b200_ctx::kPipe + 1];
+	{
+		uint32_t w[prt_b200_ctx::kPipe], total = 0;
+		for (int i = 0; i < nc; ++i) {
+			w[i] = ctx->pipe_ramp ? 1u << std::min(std::min(i, nc - 1 - i), 3) : 1u;
+			total += w[i];
+		}
+		bnd[0] = 0;
+		uint64_t cum = 0;
+		for (int i = 0; i < nc; ++i) {
+			cum += w[i];
+			bnd[i + 1] = (i + 1 == nc) ? n : ((unsigned __int128)n * cum / total) & ~31ull;
+		}
+	}
 	cudaStream_t ks[2] = {ctx->stream, ctx->s_k2};
 	uint32_t *ctr[2] = {ctx->d_work(), ctx->d_work() + 8};
 	// Earlier work of the context's stream (a _dev call) finishes before the chunks start.
@@ -400,7 +416,7 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 	uint8_t *rout = static_cast<uint8_t *>(out_host);
 	for (int c = 0; c <= nc; ++c) {
 		if (c < nc) {
-			const uint64_t b = (uint64_t)c * chunk, m = std::min(chunk, n - b);
+			const uint64_t b = bnd[c], m = bnd[c + 1] - bnd[c];
 			CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.as<uint8_t>() + 24 * b, rin + 24 * b,
 			                              24 * m, cudaMemcpyHostToDevice, ctx->s_in));
 			CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[c], ctx->s_in));
@@ -416,7 +432,7 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 		// with pageable host memory (where the copy calls return only when done) the
 		// copy-in still overlaps the traversal.
 		if (c > 0) {
-			const uint64_t b = (uint64_t)(c - 1) * chunk, m = std::min(chunk, n - b);
+			const uint64_t b = bnd[c - 1], m = bnd[c] - bnd[c - 1];
 			CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->s_out, ctx->ev_k[c - 1], 0));
 			CAPI_TRY(ctx, cudaMemcpyAsync(rout + (uint64_t)rec_size * b,
 			                              ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b,
@@ -450,6 +466,16 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		if (v < 32 || v > 128 || v % 32)
 			return fail(ctx, PRT_ERR_ARG, "block must be 32, 64, 96 or 128");
 		ctx->block = (int)v;
+	} else if (k == "pipe_chunks") {
+		if (v < 1 || v > prt_b200_ctx::kPipe)
+			return fail(ctx, PRT_ERR_ARG, "pipe_chunks must be in [1, 16]");
+		ctx->pipe_chunks = (int)v;
+	} else if (k == "pipe_ramp") {
+		ctx->pipe_ramp = v != 0;
+	} else if (k == "pipe_min_rays") {
+		if (v < 32 || v > (1ll << 30) || v % 32)
+			return fail(ctx, PRT_ERR_ARG, "pipe_min_rays must be a multiple of 32 in [32, 2^30]");
+		ctx->pipe_min_rays = (uint32_t)v;
 	} else if (k == "pool_depth") {
 		if (v < 0 || v > prt::traversal_stack_depth())
 			return fail(ctx, PRT_ERR_ARG, "pool_depth must be in [0, 32]");

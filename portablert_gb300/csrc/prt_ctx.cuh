@@ -27,7 +27,10 @@ struct prt_b200_ctx {
 	                  // [32..35] ray counter of the second compute stream
 	// The host-buffer call splits large batches into chunks and overlaps the copy-in of a
 	// chunk, the traversal of the one before and the copy-out of the one before that.
-	static constexpr int kPipe = 8;
+	static constexpr int kPipe = 16; // most chunks of one call
+	int pipe_chunks = 8;             // chunks a call aims for ("pipe_chunks")
+	uint32_t pipe_min_rays = 1u << 15; // fewest rays in a chunk ("pipe_min_rays")
+	bool pipe_ramp = true;           // chunk sizes ramp up and down ("pipe_ramp")
 	cudaStream_t s_in = nullptr, s_out = nullptr, s_k2 = nullptr;
 	cudaEvent_t ev_in[kPipe] = {}, ev_k[kPipe] = {};
 	// Callers' streams that nearest_hits_dev has queued queries on.  Each has its own

@@ -20,14 +20,18 @@ def _device_records(torch, backend, rays, tags):
     return d_o.cpu().numpy()
 
 
-@pytest.mark.parametrize("n_rays", [(1 << 18) - 1, (1 << 18) + 1, 5 * (1 << 18) + 77, 2_500_001])
+@pytest.mark.parametrize("n_rays", [(1 << 15) - 1, 8 * (1 << 15) + 1, 5 * (1 << 18) + 77,
+                                    2_500_001])
 @pytest.mark.parametrize("fmt", [0, 1])
-def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt):
+@pytest.mark.parametrize("chunks,ramp", [(8, 1), (3, 0), (16, 1)])
+def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt, chunks, ramp):
     import torch
 
     tris = workloads.soup_tris(41, 20_000)
     rays = workloads.soup_rays(42, n_rays)
     gpu_backend.set_option("node_format", fmt)
+    gpu_backend.set_option("pipe_chunks", chunks)
+    gpu_backend.set_option("pipe_ramp", ramp)
     try:
         gpu_backend.set_tris(tris)
         for tags in [hitreg.TAGS, ("t", "primitive_id", "valid"), ("valid",)]:
@@ -36,6 +40,8 @@ def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt):
             assert np.array_equal(got, want), tags
     finally:
         gpu_backend.set_option("node_format", 0)
+        gpu_backend.set_option("pipe_chunks", 8)
+        gpu_backend.set_option("pipe_ramp", 1)
 
 
 def test_chunked_host_call_pinned_buffers(gpu_backend):
