@@ -196,8 +196,14 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 	}
 }
 
+// Resident blocks per SM the register budget is set for (8 x 4 warps: 64 registers).
+#ifndef PRT_TRAVERSE_MIN_BLOCKS
+#define PRT_TRAVERSE_MIN_BLOCKS 8
+#endif
+
 template <int FMT, bool COUNT>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, 8) k_trace8(TravArgs a) {
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, PRT_TRAVERSE_MIN_BLOCKS)
+    k_trace8(TravArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	unsigned char *wbase = smem_raw + (size_t)(threadIdx.x >> 5) * a.warp_bytes;
 	WarpFixed &S = *reinterpret_cast<WarpFixed *>(wbase);
