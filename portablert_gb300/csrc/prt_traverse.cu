@@ -196,13 +196,20 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 	}
 }
 
-// Resident blocks per SM the register budget is set for (8 x 4 warps: 64 registers).
-#ifndef PRT_TRAVERSE_MIN_BLOCKS
-#define PRT_TRAVERSE_MIN_BLOCKS 8
+// Resident blocks per SM the register budget is set for, per node format (measured on
+// the 1M-triangle heightfield: FP32 nodes gain 3 % at 9 blocks of 4 warps = 56 registers
+// with a few spilled words; the compressed decode needs 64 registers, 8 blocks).
+#ifndef PRT_TRAVERSE_MIN_BLOCKS_FP32
+#define PRT_TRAVERSE_MIN_BLOCKS_FP32 9
+#endif
+#ifndef PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED
+#define PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED 8
 #endif
 
 template <int FMT, bool COUNT>
-__global__ void __launch_bounds__(32 * kWarpsPerBlock, PRT_TRAVERSE_MIN_BLOCKS)
+__global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
+                                                           ? PRT_TRAVERSE_MIN_BLOCKS_FP32
+                                                           : PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED)
     k_trace8(TravArgs a) {
 	extern __shared__ __align__(16) unsigned char smem_raw[];
 	unsigned char *wbase = smem_raw + (size_t)(threadIdx.x >> 5) * a.warp_bytes;
