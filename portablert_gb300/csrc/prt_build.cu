@@ -309,6 +309,12 @@ __global__ void k_leaf_boxes(const float *__restrict__ tris, const uint32_t *__r
 	lbox[2 * i + 1] = hi;
 }
 
+__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
+	float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+	float a = dx * dy + dx * dz + dy * dz;
+	return isfinite(a) ? a : FLT_MAX;
+}
+
 __device__ __forceinline__ void child_box(uint32_t ref, const float4 *ibox, const float4 *lbox,
                                           float4 &lo, float4 &hi) {
 	if (ref & kLeafBit) {
@@ -324,7 +330,9 @@ __device__ __forceinline__ void child_box(uint32_t ref, const float4 *ibox, cons
 // One thread per leaf walks towards its scene's root; at each binary node the first
 // thread to arrive stops and the second, which then sees both children's boxes, writes
 // the union and continues.  No thread waits on another.  A scene of one triangle has
-// no binary node (parent_leaf stays kNone).
+// no binary node (parent_leaf stays kNone).  The unused w slots of a node's box carry
+// the surface areas of its two children (-1 for a leaf child), which the collapse
+// reads together with the child indices when it opens the node.
 __global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__ parent_leaf,
                         const uint32_t *__restrict__ parent_int, const uint32_t *__restrict__ left,
                         const uint32_t *__restrict__ right, const float4 *lbox, float4 *ibox,
@@ -345,12 +353,15 @@ __global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__
 			return;
 		__threadfence();
 		float4 alo, ahi, blo, bhi;
-		child_box(left[p], ibox, lbox, alo, ahi);
-		child_box(right[p], ibox, lbox, blo, bhi);
+		const uint32_t l = left[p], r = right[p];
+		child_box(l, ibox, lbox, alo, ahi);
+		child_box(r, ibox, lbox, blo, bhi);
+		const float al = (l & kLeafBit) ? -1.0f : half_area(alo, ahi);
+		const float ar = (r & kLeafBit) ? -1.0f : half_area(blo, bhi);
 		__stcg(&ibox[2 * p], make_float4(fminf(alo.x, blo.x), fminf(alo.y, blo.y),
-		                                 fminf(alo.z, blo.z), 0.0f));
+		                                 fminf(alo.z, blo.z), al));
 		__stcg(&ibox[2 * p + 1], make_float4(fmaxf(ahi.x, bhi.x), fmaxf(ahi.y, bhi.y),
-		                                     fmaxf(ahi.z, bhi.z), 0.0f));
+		                                     fmaxf(ahi.z, bhi.z), ar));
 		p = parent_int[p];
 	}
 }
@@ -380,11 +391,6 @@ __device__ __forceinline__ uint32_t bfirst(uint32_t ref, const uint32_t *rfirst)
 	return (ref & kLeafBit) ? (ref & ~kLeafBit) : rfirst[ref];
 }
 
-__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
-	float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-	float a = dx * dy + dx * dz + dy * dz;
-	return isfinite(a) ? a : FLT_MAX;
-}
 
 __device__ __forceinline__ float open_area(uint32_t r, const float4 *__restrict__ ibox) {
 	return (r & kLeafBit) ? -1.0f : half_area(ibox[2 * r], ibox[2 * r + 1]);
@@ -450,8 +456,9 @@ __global__ void __launch_bounds__(128)
 				for (int c = 0; c < 8; ++c)
 					if (c == best)
 						x = C[c];
+				// Children and their areas (stored by the refit) in one round of loads.
 				const uint32_t l = left[x], r = right[x];
-				const float al = open_area(l, ibox), ar = open_area(r, ibox);
+				const float al = ibox[2 * x].w, ar = ibox[2 * x + 1].w;
 #pragma unroll
 				for (int c = 0; c < 8; ++c) {
 					if (c == best) {
