@@ -315,6 +315,13 @@ __device__ __forceinline__ float half_area(float4 lo, float4 hi) {
 	return isfinite(a) ? a : FLT_MAX;
 }
 
+// atomicAdd(p, 1) with acquire-release ordering at device scope.
+__device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p) {
+	uint32_t old;
+	asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+	return old;
+}
+
 __device__ __forceinline__ void child_box(uint32_t ref, const float4 *ibox, const float4 *lbox,
                                           float4 &lo, float4 &hi) {
 	if (ref & kLeafBit) {
@@ -348,10 +355,10 @@ __global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__
 			atomicOr(err, kErrCollapse);
 			return;
 		}
-		__threadfence();
-		if (atomicAdd(&flags[p], 1u) == 0u)
+		// Release: the union this thread wrote one level down is visible before its
+		// arrival counts.  Acquire: the sibling's union is read after its arrival.
+		if (arrive_acq_rel(&flags[p]) == 0u)
 			return;
-		__threadfence();
 		float4 alo, ahi, blo, bhi;
 		const uint32_t l = left[p], r = right[p];
 		child_box(l, ibox, lbox, alo, ahi);
