@@ -102,55 +102,6 @@ __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, floa
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
 
-// 2^23 + byte k of w, as a float (exact): the byte placed in the mantissa of 2^23.
-__device__ __forceinline__ float byte_plus_2p23(uint32_t w, int k) {
-	return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u | (uint32_t)k));
-}
-
-// Slab test of a compressed child in the node's frame, for a ray with finite
-// reciprocals (kind 0), without decoding the bounds.  Per axis, with A = (o - ro) f and
-// B = s f (exact: s is a power of two), the entry/exit parameter of bound q is
-// t' = (2^23 + q) B + (A - 2^23 B) in one fused multiply-add.  The decoded test computes
-// t = ((q s + o) - ro) f with two roundings after the one of the decode.  With
-// u = 2^-24: |t' - t| <= 8u|A| + u|o f| + 0.5|B| + 1532u|B| (the 0.5|B| from rounding
-// A - 2^23 B), so E = 2^-20 (|A| + |o f|) + (0.5 + 2^-12)|B| + 2^-100 (underflow of B)
-// bounds it with room for the rounding of E and of the widened ends.  Each axis range
-// widened by E contains the decoded test's range, so this test passes whenever the
-// decoded one does -- it stays conservative for every triangle below (the leaf tests
-// decide the hits) and at most visits a few more boxes.  Returns false, leaving the
-// test to the decoded form, when a quantity is too large for the bound (|A - 2^23 B|,
-// |B| or E above 2^100, as in the [-FLT_MAX, FLT_MAX] frames of non-finite triangles).
-__device__ __forceinline__ bool quantised_box_test(const RayC &r, float ox, float oy, float oz,
-                                                   float sx, float sy, float sz, uint2 ck,
-                                                   bool &hit) {
-	const float o[3] = {ox, oy, oz}, ro[3] = {r.ox, r.oy, r.oz}, f[3] = {r.fx, r.fy, r.fz};
-	const float s[3] = {sx, sy, sz};
-	const float big = 1.2676506002282294e30f; // 2^100
-	float lo[3], hi[3];
-	bool ok = true;
-#pragma unroll
-	for (int a = 0; a < 3; ++a) {
-		const float B = __fmul_rn(s[a], f[a]);
-		const float A = __fmul_rn(__fsub_rn(o[a], ro[a]), f[a]);
-		const float A2 = __fsub_rn(A, __fmul_rn(8388608.0f, B));
-		const float E = 9.5367431640625e-7f * (fabsf(A) + fabsf(o[a] * f[a])) +
-		                0.500244140625f * fabsf(B) + 7.888609052210118e-31f;
-		ok = ok && fabsf(A2) < big && fabsf(B) < big && E < big;
-		const uint32_t w = a < 2 ? ck.x : ck.y;
-		const int b = (2 * a) & 3;
-		const float t1 = __fmaf_rn(byte_plus_2p23(w, b), B, A2);
-		const float t2 = __fmaf_rn(byte_plus_2p23(w, b + 1), B, A2);
-		lo[a] = fminf(t1, t2) - E;
-		hi[a] = fmaxf(t1, t2) + E;
-	}
-	if (!ok)
-		return false;
-	const float tmin = fmaxf(fmaxf(lo[0], lo[1]), lo[2]);
-	const float tmax = fminf(fminf(hi[0], hi[1]), hi[2]);
-	hit = tmax >= 0.0f && tmin <= tmax;
-	return true;
-}
-
 // float(byte k of w), exactly: the byte placed in the mantissa of 2^23 (one byte
 // permute), minus 2^23 -- full-rate instructions instead of an integer conversion.
 __device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
@@ -228,15 +179,13 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 			const float sz = cscale((uint8_t)byte_of(w0.w, 2));
 			const float ox = __uint_as_float(w0.x), oy = __uint_as_float(w0.y),
 			            oz = __uint_as_float(w0.z);
-			if (!(r.kind == 0 && quantised_box_test(r, ox, oy, oz, sx, sy, sz, ck, hit))) {
-				const float lx = cdec_f(ox, byte_as_float(ck.x, 0), sx);
-				const float hx = cdec_f(ox, byte_as_float(ck.x, 1), sx);
-				const float ly = cdec_f(oy, byte_as_float(ck.x, 2), sy);
-				const float hy = cdec_f(oy, byte_as_float(ck.x, 3), sy);
-				const float lz = cdec_f(oz, byte_as_float(ck.y, 0), sz);
-				const float hz = cdec_f(oz, byte_as_float(ck.y, 1), sz);
-				hit = box_test(r, lx, hx, ly, hy, lz, hz);
-			}
+			const float lx = cdec_f(ox, byte_as_float(ck.x, 0), sx);
+			const float hx = cdec_f(ox, byte_as_float(ck.x, 1), sx);
+			const float ly = cdec_f(oy, byte_as_float(ck.x, 2), sy);
+			const float hy = cdec_f(oy, byte_as_float(ck.x, 3), sy);
+			const float lz = cdec_f(oz, byte_as_float(ck.y, 0), sz);
+			const float hz = cdec_f(oz, byte_as_float(ck.y, 1), sz);
+			hit = box_test(r, lx, hx, ly, hy, lz, hz);
 			if (inner) {
 				child = w1.x + __popc(imask & ((1u << k) - 1u));
 			} else {
