@@ -133,6 +133,37 @@ def workload_config(n_tris, n_prim, n_rays):
             "tags": list(TAGS), "nodes": "fp32 8-wide", "l2": "flushed between steps (512 MB write)"}
 
 
+# --------------------------------------------------------------------------- ranks
+#
+# N > 1 (torchrun, one process per GPU): every rank runs a full replica -- the scene is
+# replicated and each rank traces its own copy of the rays; the only collectives are the
+# barrier before the timed region and the maximum of the timed totals after it.
+
+
+def sync_ranks(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device: str = "cuda") -> float:
+    """The largest x over all ranks (the job's time is its slowest rank's)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_mrays(world: int, n_per_rank: int, steps: int, max_total_ms: float) -> float:
+    """Whole-job Mrays/s: the rays of all ranks over the slowest rank's time."""
+    return world * n_per_rank * steps / (max_total_ms / 1e3) / 1e6
+
+
 # --------------------------------------------------------------------------- CPU side
 
 def cpu_baseline(tris, rays, sample_rays: int, seed: int = 0):
@@ -595,8 +626,7 @@ def run_gpu(args, world, rank):
     for _ in range(max(3, args.warmup)):
         step()
     b.sync()
-    if world > 1:
-        torch.distributed.barrier()
+    sync_ranks(world)
     torch.cuda.synchronize()
     clocks = ClockSampler(dev)
     clocks.start()
@@ -611,13 +641,9 @@ def run_gpu(args, world, rank):
     b.sync()
     clk = clocks.stop()
     ms = [s.elapsed_time(e) for s, e in ev]
-    total_ms = float(sum(ms))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(sum(ms)), world)
     torch.cuda.synchronize()
-    mrays = world * n * args.steps / (total_ms / 1e3) / 1e6
+    mrays = aggregate_mrays(world, n, args.steps, total_ms)
 
     # End to end through the host-buffer C ABI call (pinned host memory).
     h_rays = torch.from_numpy(rays).pin_memory()
@@ -687,7 +713,8 @@ def run_gpu(args, world, rank):
            "clocks": clk}
     del d_rays, d_out, flush
     torch.cuda.empty_cache()
-    legs = set(args.legs.split(",")) if args.legs else set()
+    # The other configurations are measured on rank 0 only (replicas would repeat them).
+    legs = set(args.legs.split(",")) if args.legs and rank == 0 else set()
     log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
     if "precision" in legs:
         out["precision"] = leg_precision(b, stream, min(args.steps, 10))
