@@ -42,7 +42,12 @@ namespace prt {
 namespace {
 
 constexpr int kWarpsPerBlock = 4;
-constexpr int kLanesPerNode = 4;
+// Lanes that test one node together (each takes 8 / kLanesPerNode children); a warp
+// step visits 32 / kLanesPerNode nodes.
+#ifndef PRT_TRAVERSE_LANES_PER_NODE
+#define PRT_TRAVERSE_LANES_PER_NODE 4
+#endif
+constexpr int kLanesPerNode = PRT_TRAVERSE_LANES_PER_NODE;
 constexpr int kItems = 32 / kLanesPerNode;       // items per step (K)
 constexpr int kChildPerLane = 8 / kLanesPerNode;
 constexpr int kMaxDepth = 32;
