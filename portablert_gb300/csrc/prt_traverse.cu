@@ -63,6 +63,7 @@ struct TravArgs {
 	uint32_t pool_cap;       // entries of the pool (>= 256, it also holds the staged records)
 	uint32_t queue_cap;      // entries of the triangle queue
 	uint32_t warp_bytes;     // shared memory per warp
+	uint32_t max_leaf;       // most triangles in a leaf of any scene of the launch
 	uint32_t *counter;
 	uint32_t *err;
 	unsigned long long *visits;
@@ -211,7 +212,8 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 #define PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED 8
 #endif
 
-template <int FMT, bool COUNT>
+// LEAF1: every leaf holds one triangle (leaf size 1), so a hit leaf queues exactly one.
+template <int FMT, bool COUNT, bool LEAF1>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
                                                            ? PRT_TRAVERSE_MIN_BLOCKS_FP32
                                                            : PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED)
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 					all_cnt += cnt[j];
 					single = single && cnt[j] <= 1u;
 				}
-				if (__all_sync(0xFFFFFFFFu, single)) {
+				if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
 					uint32_t n_add = 0, pre = 0;
 #pragma unroll
 					for (int j = 0; j < kChildPerLane; ++j) {
@@ -487,16 +489,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 }
 
 // Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each.
-template <int FMT, bool COUNT> int blocks_per_sm(int warps, uint32_t warp_bytes) {
+template <int FMT, bool COUNT, bool LEAF1> int blocks_per_sm(int warps, uint32_t warp_bytes) {
 	static int cached_warps = -1;
 	static uint32_t cached_bytes = 0;
 	static int cached = 0;
 	if (cached_warps != warps || cached_bytes != warp_bytes) {
 		const size_t smem = (size_t)warp_bytes * warps;
-		cudaFuncSetAttribute(k_trace8<FMT, COUNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                     (int)smem);
 		int b = 0;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT>, 32 * warps, smem);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1>, 32 * warps,
+		                                              smem);
 		cached = b > 0 ? b : 1;
 		cached_warps = warps;
 		cached_bytes = warp_bytes;
@@ -504,19 +507,29 @@ template <int FMT, bool COUNT> int blocks_per_sm(int warps, uint32_t warp_bytes)
 	return cached;
 }
 
-template <int FMT, bool COUNT>
-void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	const int bps = blocks_per_sm<FMT, COUNT>(warps, a.warp_bytes);
+template <int FMT, bool COUNT, bool LEAF1>
+void launch_t(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
+	const int bps = blocks_per_sm<FMT, COUNT, LEAF1>(warps, a.warp_bytes);
 	const uint64_t warps_needed = (a.n_virtual + 31ull) / 32ull;
 	const uint64_t need = (warps_needed + warps - 1) / warps;
 	const uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
-	k_trace8<FMT, COUNT><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(a);
+	k_trace8<FMT, COUNT, LEAF1><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(
+	    a);
+}
+
+template <int FMT, bool COUNT>
+void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
+	if (a.max_leaf <= 1u)
+		launch_t<FMT, COUNT, true>(a, warps, sm_count, st);
+	else
+		launch_t<FMT, COUNT, false>(a, warps, sm_count, st);
 }
 
 void size_smem(TravArgs &a, uint32_t depth, int leaf_size) {
 	depth = std::max<uint32_t>(depth, 1u);
 	a.pool_cap = std::max<uint32_t>(256u, 7u * kItems * (depth - 1u) + 2u * kItems);
 	a.queue_cap = 32u + (uint32_t)kItems * 8u * (uint32_t)std::max(leaf_size, 1);
+	a.max_leaf = (uint32_t)std::max(leaf_size, 1);
 	a.warp_bytes = (warp_smem_bytes(a.pool_cap, a.queue_cap) + 15u) & ~15u;
 }
 
