@@ -47,14 +47,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+def committed_profile(key: str):
+    """A figure (DRAM bytes per launch, L2 hit rate) from the committed ncu summary of the
+    heightfield traversal, if it exists."""
     p = os.path.join(ROOT, "profiles", "traverse_heightfield_traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for line in f:
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
     return None
 
@@ -673,7 +674,9 @@ def run_gpu(args, world, rank):
     per_launch_s = total_ms / 1e3 / args.steps
     achieved = n * b_ray / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = committed_traffic()
+    traffic = committed_profile("dram_bytes_per_launch")
+    # The bytes a ray must move at least (its 24-byte ray in, its record out).
+    io_floor = n * (24 + lay.size) / per_launch_s / 1e9
 
     # Compressed nodes on the same batch (same hits; checked in the tests).
     b.set_option("node_format", 1)
@@ -703,7 +706,9 @@ def run_gpu(args, world, rank):
                         "frac": achieved / peak, "traffic": traffic,
                         "peak_source": peak_kind,
                         "bytes_per_ray": b_ray, "node_visits_per_ray": v_nodes,
-                        "tri_tests_per_ray": v_tris, "node_bytes": node_size},
+                        "tri_tests_per_ray": v_tris, "node_bytes": node_size,
+                        "io_floor_gbs": io_floor, "io_floor_frac": io_floor / peak,
+                        "l2_hit_rate_pct": committed_profile("l2_hit_rate_pct")},
            "build": {"mtris_s_device": len(tris) / build_dev_ms / 1e3,
                      "mtris_s_e2e": len(tris) / build_e2e_ms / 1e3,
                      "ms_device": build_dev_ms, "nodes": b.stat("n_nodes"),
