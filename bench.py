@@ -412,7 +412,6 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
     nray = workloads.log_uniform_int(rs, 1024, 1_048_576, total)
     combo = np.minimum((rs.u01((total,)) * 31).astype(np.int64), 30)
     start = (rs.u01((total,)) * (pool_n - 1_048_576)).astype(np.int64)
-    srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
 
     def run(idx, rate):
         """Submits requests idx at Poisson times of `rate` per second (0 = at once,
@@ -455,6 +454,23 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
                        "1,048,576 rays (log-uniform), uniform scene and tag set; Poisson "
                        "arrivals", "n_scenes": n_sc, "n_tris": T, "budget_bytes": 2 << 30,
            "lanes": 4}
+    # Leaf size of the resident scenes, chosen by capacity on the first requests (the
+    # largest, densest scenes take most of the GPU time and favour larger leaves).
+    trial = {}
+    for leaf in (1, 4, 8):
+        b.set_option("leaf_size", leaf)
+        srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
+        try:
+            run(list(range(40)), 0)
+            _, span = run(list(range(200)), 0)
+            trial[leaf] = float(nray[:200].sum()) / span / 1e6
+        finally:
+            srv.close()
+    best_leaf = max(trial, key=trial.get)
+    res["leaf_size"] = {"chosen": best_leaf, "trial_mrays_s": trial}
+    b.set_option("leaf_size", best_leaf)
+    srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
+    b.set_option("leaf_size", 1)
     try:
         idx = list(range(n_req))
         run(idx[:50], 0)  # warm-up
@@ -484,7 +500,7 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
         b.set_tris_dev(d_tris.data_ptr() + 36 * int(toff[big]), int(sizes[big]))
         b.set_option("count_visits", 1)
         b.nearest_hits(h_pool.numpy().reshape(-1, 6)[:65536], ("valid",))
-        res["largest_scene"] = {"n_tris": int(sizes[big]),
+        res["largest_scene"] = {"n_tris": int(sizes[big]), "leaf_size": 1,
                                 "node_visits_per_ray": b.stat("visits_nodes") / 65536,
                                 "tri_tests_per_ray": b.stat("visits_tris") / 65536}
         b.set_option("count_visits", 0)

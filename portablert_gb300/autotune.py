@@ -2,7 +2,9 @@
 
 The knobs are the options of the C ABI that change speed and never answers:
 
-* ``leaf_size``   most triangles per leaf of the 8-wide tree (the build);
+* ``leaf_size``   most triangles per leaf of the 8-wide tree (the build): larger leaves
+                  trade node visits for triangle tests (a test costs about a quarter
+                  of a visit), which pays in dense scenes;
 * ``node_format`` FP32 or compressed 8-bit child boxes (the traversal's node bytes);
 * ``block``       threads per traversal block (warps per block: shared memory per
                   block against blocks per SM);
@@ -81,7 +83,7 @@ def time_graph(batch, backend, d_tris_ptr, tri_off, qarr, stream, reps: int):
     return out
 
 
-def candidates(formats=(0, 1), leaf_sizes=(1, 2, 4), blocks=(64, 128)):
+def candidates(formats=(0, 1), leaf_sizes=(1, 2, 4, 8), blocks=(64, 128)):
     for fmt in formats:
         for leaf in leaf_sizes:
             for blk in blocks:
@@ -89,7 +91,7 @@ def candidates(formats=(0, 1), leaf_sizes=(1, 2, 4), blocks=(64, 128)):
 
 
 def tune_batch(backend, d_tris_ptr: int, tri_off, queries, stream=None, reps: int = 3,
-               formats=(0, 1), leaf_sizes=(1, 2, 4), blocks=(64, 128), cache=DEFAULT_CACHE,
+               formats=(0, 1), leaf_sizes=(1, 2, 4, 8), blocks=(64, 128), cache=DEFAULT_CACHE,
                refresh: bool = False, log=None) -> dict:
     """Best knob set for this batch (and the timings of every candidate tried).
 
