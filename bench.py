@@ -684,6 +684,22 @@ def run_gpu(args, world, rank):
         e2e_t.append(time.perf_counter() - t0)
     e2e = n / float(np.median(e2e_t)) / 1e6
     assert rec["valid"].sum() > 0
+    # The same call on pageable memory (what portableRT's std::vector API passes).
+    pg_out = np.zeros(n * lay.size, np.uint8)
+
+    def e2e_pageable_step():
+        rc = L.prt_b200_nearest_hits(ctx, rays.ctypes.data, n, lay.mask, lay.size, off,
+                                     pg_out.ctypes.data)
+        if rc:
+            raise RuntimeError(L.prt_b200_last_error(ctx))
+
+    e2e_pageable_step()
+    pg_t = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        e2e_pageable_step()
+        pg_t.append(time.perf_counter() - t0)
+    e2e_pageable = n / float(np.median(pg_t)) / 1e6
 
     # Roofline of the traversal kernel (algorithmic bytes per launch / launch time).
     b_ray = 24 + lay.size + v_nodes * node_size + v_tris * 48
@@ -716,7 +732,8 @@ def run_gpu(args, world, rank):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
            "data": "synthetic", "config": workload_config(len(tris), len(prim), n),
            "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
-                   "d2h_bytes_per_step": lay.size * n},
+                   "d2h_bytes_per_step": lay.size * n, "host_memory": "pinned",
+                   "pageable_value": e2e_pageable},
            "gpu_launches": args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
