@@ -68,7 +68,7 @@ def _check(got, want):
         assert same.all(), f
 
 
-@pytest.mark.parametrize("seed", range(12))
+@pytest.mark.parametrize("seed", range(48))
 def test_fuzz_against_exhaustive_search(gpu_backend, oracle_lib, seed):
     rng = np.random.default_rng(7000 + seed)
     tris, scale = _scene(rng, int(rng.integers(1, 2500)))
