@@ -70,7 +70,8 @@ int prt_b200_create(int device, prt_b200_ctx **out);
 void prt_b200_destroy(prt_b200_ctx *ctx);
 
 /* Message of the last failing call on ctx ("" if none).  With ctx == NULL: the last
- * failure of prt_b200_create in this thread. */
+ * failure of prt_b200_create or prt_b200_obj_load in this thread.  The string is the
+ * calling thread's copy, valid until its next call of this function. */
 const char *prt_b200_last_error(const prt_b200_ctx *ctx);
 
 /* Replaces Backend::device_name (backend.hpp:23). */

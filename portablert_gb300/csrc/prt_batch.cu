@@ -372,7 +372,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 		if (rc != PRT_OK) {
 			if (g)
 				cudaGraphDestroy(g);
-			return rc == PRT_ERR_CUDA ? rc : bfail(ctx, rc, msg.empty() ? ctx->err : msg);
+			return rc == PRT_ERR_CUDA ? rc : bfail(ctx, rc, msg.empty() ? ctx->err.get() : msg);
 		}
 		if (ce != cudaSuccess)
 			return bcuda(ctx, ce, "batch run_graph: capture");

@@ -226,8 +226,11 @@ void prt_b200_destroy(prt_b200_ctx *ctx) {
 	delete ctx;
 }
 
+// The calling thread's copy of the message, valid until its next call here.
 const char *prt_b200_last_error(const prt_b200_ctx *ctx) {
-	return ctx ? ctx->err.c_str() : g_create_error.c_str();
+	thread_local std::string copy;
+	copy = ctx ? ctx->err.get() : g_create_error;
+	return copy.c_str();
 }
 
 int prt_b200_device_name(prt_b200_ctx *ctx, char *buf, size_t len) {

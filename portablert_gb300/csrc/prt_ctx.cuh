@@ -12,12 +12,35 @@
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
 
+namespace prt {
+
+// The message of a context's last failure.  Any thread may set it (argument checks run
+// before the context's lock is taken), so it has a lock of its own; readers get a copy.
+class ErrorText {
+  public:
+	ErrorText &operator=(const std::string &m) {
+		std::lock_guard<std::mutex> lk(mu_);
+		s_ = m;
+		return *this;
+	}
+	std::string get() const {
+		std::lock_guard<std::mutex> lk(mu_);
+		return s_;
+	}
+
+  private:
+	mutable std::mutex mu_;
+	std::string s_;
+};
+
+} // namespace prt
+
 struct prt_b200_ctx {
 	int device = 0;
 	int sms = 0;
 	cudaStream_t stream = nullptr;
 	std::mutex mu;
-	std::string err;
+	prt::ErrorText err;
 	prt::SceneGPU scene;
 	bool scene_set = false;
 	prt::BuildScratch ws;

@@ -475,11 +475,14 @@ int prt_b200_server_stat(prt_b200_server *s, const char *key, double *value) {
 	return PRT_OK;
 }
 
+// The calling thread's copy of the message, valid until its next call here.
 const char *prt_b200_server_last_error(prt_b200_server *s) {
 	if (!s)
 		return "null server";
+	thread_local std::string copy;
 	std::lock_guard<std::mutex> lk(s->mu);
-	return s->err.c_str();
+	copy = s->err;
+	return copy.c_str();
 }
 
 } // extern "C"

@@ -32,7 +32,7 @@ int main() {
 	REQUIRE(a.alloc(4096) == 0 && a.alloc(1) == RangeAllocator::kFail);
 
 	std::mt19937_64 rng(7);
-	for (int round = 0; round < 50; ++round) {
+	for (int trial = 0; trial < 50; ++trial) {
 		const uint64_t cap = 256 * (1 + rng() % 200);
 		RangeAllocator r(cap, 256);
 		std::vector<int> owner(cap / 256, -1);
