@@ -247,6 +247,44 @@ def _events(torch, stream, fn, reps):
     return ms
 
 
+def leg_small(b, stream, steps):
+    """The small configuration: 4,096-triangle soup (seed 0), 65,536 rays, tags
+    uv/t/primitive_id/valid.  At this size a call is bound by launch and copy latency:
+    the device time of one query and one build (CUDA events), and the host-buffer call
+    timed on the host clock."""
+    import torch
+
+    tris, rays = workloads.soup(0, 4096, 65536)
+    n = len(rays)
+    lay = hitreg.layout(C0_TAGS)
+    d_t = torch.from_numpy(tris).cuda()
+    d_r = torch.from_numpy(rays).cuda()
+    d_o = torch.empty(n * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    bms = []
+    for _ in range(max(3, steps)):
+        b.set_tris_dev(d_t.data_ptr(), len(tris))
+        bms.append(b.stat("build_ms"))
+    q = lambda: b.nearest_hits_dev(d_r.data_ptr(), n, d_o.data_ptr(), C0_TAGS, stream.cuda_stream)
+    for _ in range(3):
+        q()
+    b.sync()
+    ms = float(np.median(_events(torch, stream, q, max(10, steps))))
+    b.sync()
+    for _ in range(3):
+        b.nearest_hits(rays, C0_TAGS)
+    ts = []
+    for _ in range(max(10, steps)):
+        t0 = time.perf_counter()
+        b.nearest_hits(rays, C0_TAGS)
+        ts.append(time.perf_counter() - t0)
+    e2e_ms = 1e3 * float(np.median(ts))
+    return {"workload": "soup 4,096 tris (seed 0), 65,536 rays; tags uv, t, primitive_id, valid",
+            "query_ms": ms, "mrays_s": n / ms / 1e3, "build_ms": float(np.median(bms)),
+            "build_mtris_s": len(tris) / float(np.median(bms)) / 1e3,
+            "e2e_ms": e2e_ms, "e2e_mrays_s": n / e2e_ms / 1e3}
+
+
 def leg_batch(b, stream, steps, n_scenes=4096, log=None):
     """4,096 soup scenes (triangles log-uniform in [16, 65536], rays log-uniform in
     [64, 262144], seeds 1000+s, tags uv/t/primitive_id/valid) built and queried as one
@@ -754,6 +792,8 @@ def run_gpu(args, world, rank):
     # The other configurations are measured on rank 0 only (replicas would repeat them).
     legs = set(args.legs.split(",")) if args.legs and rank == 0 else set()
     log = (lambda m: print(m, file=sys.stderr, flush=True)) if args.verbose else None
+    if "small" in legs:
+        out["small"] = leg_small(b, stream, min(args.steps, 20))
     if "precision" in legs:
         out["precision"] = leg_precision(b, stream, min(args.steps, 10))
     if "batch" in legs:
@@ -777,8 +817,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="b200", choices=["b200", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
-    ap.add_argument("--legs", default="precision,batch,serving,camera",
-                    help="other configurations to measure: precision, batch, serving, camera "
+    ap.add_argument("--legs", default="small,precision,batch,serving,camera",
+                    help="other configurations to measure: small, precision, batch, serving, "
+                         "camera "
                          "(comma list; 'none' for the heightfield alone)")
     ap.add_argument("--verbose", action="store_true")
     args = ap.parse_args()
