@@ -195,8 +195,11 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
  * (scene, host rays, record layout, host output) are admitted in arrival order while
  * their device buffers (24 B per ray rounded up to 256 B, plus the records) fit in a
  * region of budget_bytes reserved at creation, and each group of admitted requests
- * (a wave) runs as one persistent launch on one of n_lanes streams, so up to n_lanes
- * waves overlap.  Each request's records equal nearest_hits on its scene alone.  The
+ * (a wave) runs as one launch on one of n_lanes streams, so up to n_lanes waves overlap.
+ * With several lanes, lane 0 is an express lane of the highest stream priority that
+ * carries only requests of at most 65,536 rays, taken ahead of larger ones; a wave's
+ * warps take at most two batches of 32 rays each, so a large wave's blocks retire as
+ * they finish and an express wave's blocks start meanwhile.  Each request's records equal nearest_hits on its scene alone.  The
  * node format is the context's at creation.  Host buffers should be pinned: a copy
  * to or from pageable memory makes the scheduler wait for it.  Buffers belong to the
  * caller until prt_b200_server_wait returns for the ticket. */
@@ -212,7 +215,8 @@ int prt_b200_server_submit(prt_b200_server *server, uint32_t scene, const float 
 /* Blocks until the request is answered; latency_ms = submit to records in host memory.
  * Returns the request's status; the ticket is then forgotten. */
 int prt_b200_server_wait(prt_b200_server *server, uint64_t ticket, double *latency_ms);
-/* "waves", "max_in_flight_waves", "max_wave_requests", "completed", "rays", "waiting",
+/* "waves", "express_waves", "max_in_flight_waves", "max_wave_requests", "completed",
+ * "rays", "waiting",
  * "bytes_in_use", "peak_bytes", "budget_bytes", "n_scenes", "n_tris". */
 int prt_b200_server_stat(prt_b200_server *server, const char *key, double *value);
 const char *prt_b200_server_last_error(prt_b200_server *server);

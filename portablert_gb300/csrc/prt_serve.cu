@@ -7,9 +7,13 @@
 //   admit   -> the scheduler thread takes requests from the head of the queue while
 //              their rays and records fit in the device memory budget (one region
 //              reserved at start-up, carved by a first-fit range allocator) and a
-//              lane is free; the admitted requests form one wave
-//   run     -> per wave, on the lane's stream: rays copied in, ONE persistent launch
-//              of the segment traversal over every request of the wave, records
+//              lane is free; the admitted requests form one wave.  With several lanes,
+//              lane 0 is an express lane (highest stream priority) that takes only
+//              small requests, passing over larger ones queued before them
+//   run     -> per wave, on the lane's stream: rays copied in, ONE launch of the
+//              segment traversal over every request of the wave (each warp takes at
+//              most a few batches, so the blocks of a long wave retire steadily and
+//              a higher-priority wave's blocks are scheduled in between), records
 //              copied out; up to n_lanes waves are in flight at once, so requests
 //              that arrive while others run are admitted into the next wave as soon
 //              as memory and a lane are free, and their work overlaps on the device
@@ -43,6 +47,13 @@ using Clock = std::chrono::steady_clock;
 
 constexpr uint32_t kMaxWaveRequests = 1024;
 constexpr uint64_t kMaxRequestRays = 1ull << 31;
+// Requests of at most this many rays may take the express lane (lane 0 of a server
+// with several lanes: its stream has the highest priority and it carries small waves
+// only), ahead of larger requests that arrived before them.
+constexpr uint64_t kExpressRays = 65536;
+// Batches of 32 rays a warp of a wave's launch takes before it exits: blocks retire
+// while a large wave runs, so the block scheduler can start an express wave's blocks.
+constexpr uint32_t kWaveBatchesPerWarp = 2;
 
 struct Request {
 	uint64_t id = 0;
@@ -89,6 +100,7 @@ struct prt_b200_server {
 	std::string err;
 	// statistics
 	uint64_t waves = 0, in_flight = 0, max_in_flight = 0, max_wave_requests = 0;
+	uint64_t express_waves = 0;
 	uint64_t completed = 0, rays_done = 0;
 };
 
@@ -107,10 +119,50 @@ int sfail_unlocked(prt_b200_server *s, int code, const std::string &msg) {
 
 uint64_t round256(uint64_t b) { return (b + 255) & ~255ull; }
 
-Lane *free_lane(prt_b200_server *s) {
-	for (auto &l : s->lanes)
-		if (l->wave.empty())
-			return l.get();
+// Moves waiting requests into L's wave while their buffers fit: in arrival order, up to
+// the first that does not fit, or (express) only those of at most kExpressRays rays,
+// passing over larger ones.  Caller holds the lock.
+void fill_wave(prt_b200_server *s, Lane &L, bool express) {
+	unsigned long long nv = 0;
+	for (auto it = s->waiting.begin();
+	     it != s->waiting.end() && L.wave.size() < kMaxWaveRequests;) {
+		Request *r = *it;
+		if (express && r->n > kExpressRays) {
+			++it;
+			continue;
+		}
+		const unsigned long long pad = (r->n + 31ull) & ~31ull;
+		if (nv + pad > (1ull << 31))
+			break;
+		const uint64_t off = s->alloc.alloc(r->bytes);
+		if (off == prt::RangeAllocator::kFail)
+			break; // later requests wait behind this one
+		r->off = off;
+		r->t_launch = Clock::now();
+		nv += pad;
+		it = s->waiting.erase(it);
+		L.wave.push_back(r);
+	}
+}
+
+// A lane with a new wave, or null.  The express lane takes small requests first; the
+// other lanes take requests in arrival order.
+Lane *admit(prt_b200_server *s) {
+	const size_t n = s->lanes.size();
+	if (n > 1 && s->lanes[0]->wave.empty()) {
+		fill_wave(s, *s->lanes[0], true);
+		if (!s->lanes[0]->wave.empty()) {
+			++s->express_waves;
+			return s->lanes[0].get();
+		}
+	}
+	for (size_t i = n > 1 ? 1 : 0; i < n; ++i) {
+		Lane &L = *s->lanes[i];
+		if (!L.wave.empty())
+			continue;
+		fill_wave(s, L, false);
+		return L.wave.empty() ? nullptr : &L;
+	}
 	return nullptr;
 }
 
@@ -148,6 +200,7 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 	prt::TravConfig cfg;
 	cfg.format = s->format;
 	cfg.block = s->ctx->block;
+	cfg.max_batches = kWaveBatchesPerWarp;
 	const prt::SceneDesc *tab = s->format == PRT_NODES_COMPRESSED
 	                                ? b->scenes_comp.as<prt::SceneDesc>()
 	                                : b->scenes_fp32.as<prt::SceneDesc>();
@@ -192,25 +245,8 @@ void scheduler(prt_b200_server *s) {
 	cudaSetDevice(s->ctx->device);
 	std::unique_lock<std::mutex> lk(s->mu);
 	while (!s->stop) {
-		Lane *L = s->waiting.empty() ? nullptr : free_lane(s);
-		if (L) {
-			unsigned long long nv = 0;
-			while (!s->waiting.empty() && L->wave.size() < kMaxWaveRequests) {
-				Request *r = s->waiting.front();
-				const unsigned long long pad = (r->n + 31ull) & ~31ull;
-				if (nv + pad > (1ull << 31))
-					break;
-				const uint64_t off = s->alloc.alloc(r->bytes);
-				if (off == prt::RangeAllocator::kFail)
-					break; // FIFO: later requests wait behind the head
-				r->off = off;
-				r->t_launch = Clock::now();
-				nv += pad;
-				s->waiting.pop_front();
-				L->wave.push_back(r);
-			}
-		}
-		if (!L || L->wave.empty()) {
+		Lane *L = s->waiting.empty() ? nullptr : admit(s);
+		if (!L) {
 			s->cv_sched.wait(lk); // a submit, a retired wave or stop
 			continue;
 		}
@@ -321,9 +357,14 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 	if (e == cudaSuccess)
 		e = s->region.reserve(budget_bytes);
 	s->alloc.reset(budget_bytes, 256);
+	int least = 0, greatest = 0;
+	if (e == cudaSuccess)
+		e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
 	for (uint32_t i = 0; i < n_lanes && e == cudaSuccess; ++i) {
 		std::unique_ptr<Lane> L(new Lane());
-		e = cudaStreamCreateWithFlags(&L->st, cudaStreamNonBlocking);
+		// Lane 0 of several is the express lane: the highest stream priority.
+		e = cudaStreamCreateWithPriority(&L->st, cudaStreamNonBlocking,
+		                                 (i == 0 && n_lanes > 1) ? greatest : least);
 		if (e == cudaSuccess)
 			e = cudaEventCreateWithFlags(&L->ev, cudaEventDisableTiming);
 		if (e == cudaSuccess)
@@ -452,6 +493,8 @@ int prt_b200_server_stat(prt_b200_server *s, const char *key, double *value) {
 		*value = (double)s->waves;
 	else if (k == "max_in_flight_waves")
 		*value = (double)s->max_in_flight;
+	else if (k == "express_waves")
+		*value = (double)s->express_waves;
 	else if (k == "max_wave_requests")
 		*value = (double)s->max_wave_requests;
 	else if (k == "completed")

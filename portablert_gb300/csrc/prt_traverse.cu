@@ -64,6 +64,7 @@ struct TravArgs {
 	uint32_t queue_cap;      // entries of the triangle queue
 	uint32_t warp_bytes;     // shared memory per warp
 	uint32_t max_leaf;       // most triangles in a leaf of any scene of the launch
+	uint32_t max_batches;    // batches per warp before it exits (0 = no bound)
 	uint32_t *counter;
 	uint32_t *err;
 	unsigned long long *visits;
@@ -230,7 +231,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 	// tree, which is reported instead of looping.
 	const uint64_t step_limit = 32ull * a.n_nodes + 64ull;
 
-	for (;;) {
+	for (uint32_t batch = 0;; ++batch) {
+		if (a.max_batches && batch == a.max_batches)
+			break;
 		uint32_t base = 0;
 		if (lane == 0)
 			base = atomicAdd(a.counter, 32u);
@@ -510,9 +513,12 @@ template <int FMT, bool COUNT, bool LEAF1> int blocks_per_sm(int warps, uint32_t
 template <int FMT, bool COUNT, bool LEAF1>
 void launch_t(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
 	const int bps = blocks_per_sm<FMT, COUNT, LEAF1>(warps, a.warp_bytes);
-	const uint64_t warps_needed = (a.n_virtual + 31ull) / 32ull;
-	const uint64_t need = (warps_needed + warps - 1) / warps;
-	const uint64_t grid = std::min<uint64_t>((uint64_t)sm_count * bps, need);
+	const uint64_t batches = (a.n_virtual + 31ull) / 32ull;
+	// Unbounded warps: at most one block per resident slot (persistent).  Bounded: enough
+	// blocks that every batch has a warp even if each warp takes its maximum.
+	const uint64_t per_block = (uint64_t)warps * (a.max_batches ? a.max_batches : 1u);
+	const uint64_t need = (batches + per_block - 1) / per_block;
+	const uint64_t grid = a.max_batches ? need : std::min<uint64_t>((uint64_t)sm_count * bps, need);
 	k_trace8<FMT, COUNT, LEAF1><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(
 	    a);
 }
@@ -530,6 +536,7 @@ void size_smem(TravArgs &a, uint32_t depth, int leaf_size) {
 	a.pool_cap = std::max<uint32_t>(256u, 7u * kItems * (depth - 1u) + 2u * kItems);
 	a.queue_cap = 32u + (uint32_t)kItems * 8u * (uint32_t)std::max(leaf_size, 1);
 	a.max_leaf = (uint32_t)std::max(leaf_size, 1);
+	a.max_batches = 0;
 	a.warp_bytes = (warp_smem_bytes(a.pool_cap, a.queue_cap) + 15u) & ~15u;
 }
 
@@ -599,6 +606,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.seg0.pad = 0;
 		a.n_nodes = sc.n_nodes;
 		size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : sc.depth, sc.leaf_size);
+		a.max_batches = cfg.max_batches;
 		a.counter = d_work;
 		a.err = d_err;
 		a.visits = d_visits;
@@ -629,6 +637,7 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
 	a.n_virtual = (uint32_t)n_virtual;
 	a.n_nodes = n_nodes;
 	size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : depth, leaf_size);
+	a.max_batches = cfg.max_batches;
 	a.counter = d_work;
 	a.err = d_err;
 	a.visits = d_visits;

@@ -20,6 +20,10 @@ struct TravConfig {
 	int block = 128;      // threads per block
 	bool count = false;   // accumulate visit counters into d_visits[0..1]
 	int pool_depth = 0;   // size the pool for this depth instead of the scene's (0 = scene)
+	// Batches of 32 rays a warp takes before it exits (0 = until the work runs out).  With
+	// a bound the grid covers all batches and blocks retire as they finish, so the block
+	// scheduler can interleave other launches (of higher-priority streams) meanwhile.
+	uint32_t max_batches = 0;
 };
 
 // One scene as the traversal sees it: its arrays, root node and triangle count.

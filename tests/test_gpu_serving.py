@@ -127,3 +127,29 @@ def test_close_with_requests_queued(gpu_backend):
     keep = [srv.submit(0, workloads.soup_rays(5400 + i, 100_000), ("valid",)) for i in range(6)]
     srv.close()  # answers or fails every queued request, joins its threads
     assert keep
+
+
+def test_small_requests_take_the_express_lane(gpu_backend):
+    """Small requests queued behind a large one on a dense scene go to the express lane
+    (lane 0, highest priority) and still equal their answers alone."""
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    tris, off, d_tris = _scenes(torch, [300_000, 2_000], 5500)
+    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=256 << 20, lanes=3)
+    tags = ("t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    try:
+        big = srv.submit(0, workloads.soup_rays(5600, 1_500_000), tags)
+        small = [(i % 2, workloads.soup_rays(5700 + i, 5_000 + 97 * i)) for i in range(12)]
+        subs = [srv.submit(s, r, tags) for s, r in small]
+        lat = [srv.wait(t) for t, _ in subs]
+        big_lat = srv.wait(big[0])
+        assert srv.stat("express_waves") >= 1
+        assert min(lat) <= big_lat
+        for (s, r), (_, out) in zip(small, subs):
+            gpu_backend.set_tris(tris[s])
+            assert _fields_equal(out, gpu_backend.nearest_hits(r, tags), lay) is None
+    finally:
+        srv.close()
