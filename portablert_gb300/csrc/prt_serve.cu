@@ -13,12 +13,13 @@
 //   run     -> per wave, on the lane's stream: rays copied in, ONE launch of the
 //              segment traversal over every request of the wave (each warp takes at
 //              most a few batches, so the blocks of a long wave retire steadily and
-//              a higher-priority wave's blocks are scheduled in between), records
-//              copied out; up to n_lanes waves are in flight at once, so requests
+//              a higher-priority wave's blocks are scheduled in between); up to
+//              n_lanes waves are in flight at once, so requests
 //              that arrive while others run are admitted into the next wave as soon
 //              as memory and a lane are free, and their work overlaps on the device
-//   retire  -> each lane's completer thread waits for its wave, stamps the finish
-//              time, returns the memory and wakes the waiters
+//   retire  -> each lane's completer thread waits for its wave's traversal, copies the
+//              records out, stamps the finish time, returns the memory and wakes the
+//              waiters
 //
 // A request's records are exactly nearest_hits<Tags...> on its scene alone: the wave's
 // launch gives each request its own segment (rays padded to whole warps), and the
@@ -211,17 +212,25 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 	                                      L.st, s->ctx->sms);
 	if (e != cudaSuccess)
 		return e;
-	for (uint32_t i = 0; i < k; ++i) {
-		Request *r = L.wave[i];
-		e = cudaMemcpyAsync(r->out, base + r->off + r->ray_bytes, (uint64_t)r->rec * r->n,
-		                    cudaMemcpyDeviceToHost, L.st);
-		if (e != cudaSuccess)
-			return e;
-	}
 	e = cudaMemcpyAsync(L.h_err, w + 1, 4, cudaMemcpyDeviceToHost, L.st);
 	if (e == cudaSuccess)
 		e = cudaEventRecord(L.ev, L.st);
 	return e;
+}
+
+// Copies the wave's records to the requests' host buffers, after its traversal (run by
+// the lane's completer, so a copy to pageable memory, which returns only when done,
+// never holds up the scheduler).
+cudaError_t copy_out(prt_b200_server *s, Lane &L) {
+	uint8_t *base = s->region.as<uint8_t>();
+	for (Request *r : L.wave) {
+		const cudaError_t e = cudaMemcpyAsync(r->out, base + r->off + r->ray_bytes,
+		                                      (uint64_t)r->rec * r->n, cudaMemcpyDeviceToHost,
+		                                      L.st);
+		if (e != cudaSuccess)
+			return e;
+	}
+	return cudaStreamSynchronize(L.st);
 }
 
 // Finishes the requests of a lane's wave (caller holds the lock).
@@ -290,7 +299,9 @@ void completer(prt_b200_server *s, Lane *L) {
 		lk.unlock();
 		// The wave's kernels end by themselves (bounded traversal steps), so this wait
 		// ends too.
-		const cudaError_t e = cudaEventSynchronize(L->ev);
+		cudaError_t e = cudaEventSynchronize(L->ev);
+		if (e == cudaSuccess && !*L->h_err)
+			e = copy_out(s, *L);
 		const Clock::time_point t = Clock::now();
 		lk.lock();
 		int status = PRT_OK;
