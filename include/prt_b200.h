@@ -183,6 +183,9 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
+ *   "serve_batches_per_warp" request servers created afterwards launch waves whose
+ *                  warps take at most this many batches of 32 rays (0 = until the
+ *                  work runs out; default 2): lower lets an express wave start sooner
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "node_bytes", "tri_bytes",
@@ -198,8 +201,9 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
  * (a wave) runs as one launch on one of n_lanes streams, so up to n_lanes waves overlap.
  * With several lanes, lane 0 is an express lane of the highest stream priority that
  * carries only requests of at most 65,536 rays, taken ahead of larger ones; a wave's
- * warps take at most two batches of 32 rays each, so a large wave's blocks retire as
- * they finish and an express wave's blocks start meanwhile.  Each request's records equal nearest_hits on its scene alone.  The
+ * warps take a bounded number of batches of 32 rays (option "serve_batches_per_warp"),
+ * so a large wave's blocks retire as they finish and an express wave's blocks start
+ * meanwhile.  Each request's records equal nearest_hits on its scene alone.  The
  * node format is the context's at creation.  Host buffers should be pinned: a copy
  * to or from pageable memory makes the scheduler wait for it.  Buffers belong to the
  * caller until prt_b200_server_wait returns for the ticket. */

@@ -479,6 +479,10 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		if (v < 32 || v > (1ll << 30) || v % 32)
 			return fail(ctx, PRT_ERR_ARG, "pipe_min_rays must be a multiple of 32 in [32, 2^30]");
 		ctx->pipe_min_rays = (uint32_t)v;
+	} else if (k == "serve_batches_per_warp") {
+		if (v < 0 || v > (1 << 20))
+			return fail(ctx, PRT_ERR_ARG, "serve_batches_per_warp must be in [0, 2^20]");
+		ctx->serve_batches_per_warp = (int)v;
 	} else if (k == "pool_depth") {
 		if (v < 0 || v > prt::traversal_stack_depth())
 			return fail(ctx, PRT_ERR_ARG, "pool_depth must be in [0, 32]");

@@ -52,9 +52,7 @@ constexpr uint64_t kMaxRequestRays = 1ull << 31;
 // with several lanes: its stream has the highest priority and it carries small waves
 // only), ahead of larger requests that arrived before them.
 constexpr uint64_t kExpressRays = 65536;
-// Batches of 32 rays a warp of a wave's launch takes before it exits: blocks retire
-// while a large wave runs, so the block scheduler can start an express wave's blocks.
-constexpr uint32_t kWaveBatchesPerWarp = 2;
+
 
 struct Request {
 	uint64_t id = 0;
@@ -102,6 +100,10 @@ struct prt_b200_server {
 	// statistics
 	uint64_t waves = 0, in_flight = 0, max_in_flight = 0, max_wave_requests = 0;
 	uint64_t express_waves = 0;
+	// Batches of 32 rays a warp of a wave's launch takes before it exits (0 = until the
+	// wave's work runs out): blocks of a long wave retire as they finish, so the block
+	// scheduler can start an express wave's blocks meanwhile.
+	uint32_t batches_per_warp = 2;
 	uint64_t completed = 0, rays_done = 0;
 };
 
@@ -201,7 +203,7 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 	prt::TravConfig cfg;
 	cfg.format = s->format;
 	cfg.block = s->ctx->block;
-	cfg.max_batches = kWaveBatchesPerWarp;
+	cfg.max_batches = s->batches_per_warp;
 	const prt::SceneDesc *tab = s->format == PRT_NODES_COMPRESSED
 	                                ? b->scenes_comp.as<prt::SceneDesc>()
 	                                : b->scenes_fp32.as<prt::SceneDesc>();
@@ -363,6 +365,7 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 	{
 		std::lock_guard<std::mutex> lk(ctx->mu);
 		s->format = ctx->node_format;
+		s->batches_per_warp = (uint32_t)ctx->serve_batches_per_warp;
 	}
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e == cudaSuccess)
