@@ -144,3 +144,46 @@ def test_camera_arguments_checked(gpu_backend):
     with pytest.raises(PrtError):  # records without primitive_id cannot be shaded
         gpu_backend.shade_lambert(out.data_ptr(), ("t", "valid"), out.data_ptr(),
                                   rays_ptr=out.data_ptr(), n=1)
+
+
+def test_device_camera_equals_validation_program(gpu_backend):
+    """The validation program's 1024 x 1024 rays, built on the device (SHA-256 of all
+    of them against the fixture written from the reference's own program)."""
+    import hashlib
+    import os
+
+    import torch
+
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "camera_validation.npz"))
+    d = dict(width=1024, height=1024, form=1, pos=(0.0, 0.0, -0.5), sensor_size=0.05,
+             sensor_dist=0.05, sensor_z=float(F32(-0.5) + F32(0.05)))
+    out = torch.empty(1024 * 1024 * 6, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    gpu_backend.camera_rays(_ccam(d), out.data_ptr())
+    gpu_backend.sync()
+    assert hashlib.sha256(out.cpu().numpy().tobytes()).hexdigest() == str(z["sha256"])
+
+
+def test_bunny_setup_equals_bunny_program(gpu_backend):
+    """The bunny program's 4096 x 4096 valid mask on the fixture mesh, from the fused
+    camera traversal."""
+    import os
+
+    import torch
+
+    from conftest import GOLDEN
+
+    z = np.load(os.path.join(GOLDEN, "bunny_blob.npz"))
+    gpu_backend.set_tris(z["tris"])
+    d = dict(width=4096, height=4096, form=0, pos=(0.0, -0.02, -0.3), sensor_size=0.05,
+             sensor_dist=0.05, sensor_z=float(F32(-0.3) + F32(0.05)))
+    tags = ("valid",)
+    lay = hitreg.layout(tags)
+    rec = torch.zeros(4096 * 4096 * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    gpu_backend.nearest_hits_camera(_ccam(d), rec.data_ptr(), tags)
+    gpu_backend.sync()
+    valid = rec.cpu().numpy().view(lay.numpy_dtype())["valid"]
+    assert np.array_equal(np.packbits(valid != 0), z["mask_bits"])
