@@ -80,6 +80,8 @@ struct alignas(16) WarpFixed {
 	float ray[32][9];           // origin, direction, reciprocal per slot
 	int kind[32];
 	SegDesc seg;                // the run the current 32 rays belong to
+	uint32_t batches;           // batches this warp has taken (kept here, not in a register)
+	uint32_t pad_[3];
 };
 static_assert(sizeof(WarpFixed) % 16 == 0, "queue and pool must start 16-byte aligned");
 
@@ -214,7 +216,9 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 #endif
 
 // LEAF1: every leaf holds one triangle (leaf size 1), so a hit leaf queues exactly one.
-template <int FMT, bool COUNT, bool LEAF1>
+// BOUNDED: a warp takes at most a.max_batches batches (a separate instantiation, so the
+// unbounded kernels keep their register allocation).
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
                                                            ? PRT_TRAVERSE_MIN_BLOCKS_FP32
                                                            : PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED)
@@ -231,9 +235,17 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 	// tree, which is reported instead of looping.
 	const uint64_t step_limit = 32ull * a.n_nodes + 64ull;
 
-	for (uint32_t batch = 0;; ++batch) {
-		if (a.max_batches && batch == a.max_batches)
-			break;
+	if (BOUNDED && lane == 0)
+		S.batches = 0;
+	__syncwarp();
+	for (;;) {
+		if (BOUNDED) {
+			if (S.batches == a.max_batches)
+				break;
+			__syncwarp();
+			if (lane == 0)
+				++S.batches;
+		}
 		uint32_t base = 0;
 		if (lane == 0)
 			base = atomicAdd(a.counter, 32u);
@@ -492,17 +504,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 }
 
 // Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each.
-template <int FMT, bool COUNT, bool LEAF1> int blocks_per_sm(int warps, uint32_t warp_bytes) {
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
+int blocks_per_sm(int warps, uint32_t warp_bytes) {
 	static int cached_warps = -1;
 	static uint32_t cached_bytes = 0;
 	static int cached = 0;
 	if (cached_warps != warps || cached_bytes != warp_bytes) {
 		const size_t smem = (size_t)warp_bytes * warps;
-		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1, BOUNDED>,
+		                     cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                     (int)smem);
 		int b = 0;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1>, 32 * warps,
-		                                              smem);
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1, BOUNDED>,
+		                                              32 * warps, smem);
 		cached = b > 0 ? b : 1;
 		cached_warps = warps;
 		cached_bytes = warp_bytes;
@@ -510,25 +524,34 @@ template <int FMT, bool COUNT, bool LEAF1> int blocks_per_sm(int warps, uint32_t
 	return cached;
 }
 
-template <int FMT, bool COUNT, bool LEAF1>
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
 void launch_t(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	const int bps = blocks_per_sm<FMT, COUNT, LEAF1>(warps, a.warp_bytes);
+	const int bps = blocks_per_sm<FMT, COUNT, LEAF1, BOUNDED>(warps, a.warp_bytes);
 	const uint64_t batches = (a.n_virtual + 31ull) / 32ull;
 	// Unbounded warps: at most one block per resident slot (persistent).  Bounded: enough
 	// blocks that every batch has a warp even if each warp takes its maximum.
-	const uint64_t per_block = (uint64_t)warps * (a.max_batches ? a.max_batches : 1u);
+	const uint64_t per_block = (uint64_t)warps * (BOUNDED ? a.max_batches : 1u);
 	const uint64_t need = (batches + per_block - 1) / per_block;
-	const uint64_t grid = a.max_batches ? need : std::min<uint64_t>((uint64_t)sm_count * bps, need);
-	k_trace8<FMT, COUNT, LEAF1><<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(
-	    a);
+	const uint64_t grid = BOUNDED ? need : std::min<uint64_t>((uint64_t)sm_count * bps, need);
+	k_trace8<FMT, COUNT, LEAF1, BOUNDED>
+	    <<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(a);
 }
 
 template <int FMT, bool COUNT>
 void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	if (a.max_leaf <= 1u)
-		launch_t<FMT, COUNT, true>(a, warps, sm_count, st);
-	else
-		launch_t<FMT, COUNT, false>(a, warps, sm_count, st);
+	// Bounded warps only without the visit counters (a counting run takes the whole work).
+	const bool bounded = !COUNT && a.max_batches > 0;
+	if (a.max_leaf <= 1u) {
+		if (bounded)
+			launch_t<FMT, false, true, true>(a, warps, sm_count, st);
+		else
+			launch_t<FMT, COUNT, true, false>(a, warps, sm_count, st);
+	} else {
+		if (bounded)
+			launch_t<FMT, false, false, true>(a, warps, sm_count, st);
+		else
+			launch_t<FMT, COUNT, false, false>(a, warps, sm_count, st);
+	}
 }
 
 void size_smem(TravArgs &a, uint32_t depth, int leaf_size) {
