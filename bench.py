@@ -343,9 +343,10 @@ def leg_batch(b, stream, steps, n_scenes=4096, log=None):
             torch.cuda.synchronize()
             batched = d_out.clone()
     # The plain path: one scene at a time through set_tris_dev + nearest_hits_dev (FP32,
-    # default options), timed on the host clock around the whole loop.
+    # LBVH trees as the batch builds), timed on the host clock around the whole loop.
     autotune.apply(b, {"node_format": 0, "leaf_size": 1, "block": 128, "pool_depth": 0})
     b.set_option("build_compressed", 1)
+    b.set_option("build_sah", 0)
     pp = d_plain.data_ptr()
     t0 = time.perf_counter()
     for s in range(n_scenes):
@@ -355,6 +356,7 @@ def leg_batch(b, stream, steps, n_scenes=4096, log=None):
     b.sync()
     torch.cuda.synchronize()
     plain_s = time.perf_counter() - t0
+    b.set_option("build_sah", 1)
     out["plain_per_scene"] = {"ms": 1e3 * plain_s, "mrays_s": R / plain_s / 1e6,
                               "mtris_s_with_queries": T / plain_s / 1e6}
     res.update(out)
@@ -652,6 +654,16 @@ def run_gpu(args, world, rank):
         b.set_tris_dev(d_tris.data_ptr(), len(tris))
         build_ms.append(b.stat("build_ms"))
     build_dev_ms = float(np.median(build_ms))
+    sah_used = b.stat("build_sah")
+    # The LBVH build of the same scene (option build_sah = 0), for comparison.
+    b.set_option("build_sah", 0)
+    lbvh_ms = []
+    for _ in range(3):
+        b.set_tris_dev(d_tris.data_ptr(), len(tris))
+        lbvh_ms.append(b.stat("build_ms"))
+    lbvh_nodes = b.stat("n_nodes")
+    b.set_option("build_sah", 1)
+    lbvh_ms = float(np.median(lbvh_ms))
     del d_tris
     t0 = time.perf_counter()
     b.set_tris(tris)
@@ -783,7 +795,10 @@ def run_gpu(args, world, rank):
            "build": {"mtris_s_device": len(tris) / build_dev_ms / 1e3,
                      "mtris_s_e2e": len(tris) / build_e2e_ms / 1e3,
                      "ms_device": build_dev_ms, "nodes": b.stat("n_nodes"),
-                     "depth": b.stat("depth")},
+                     "depth": b.stat("depth"),
+                     "method": "binned SAH" if sah_used else "LBVH (SAH fell back)",
+                     "lbvh": {"ms_device": lbvh_ms, "mtris_s_device": len(tris) / lbvh_ms / 1e3,
+                              "nodes": lbvh_nodes}},
            "compressed": {"value": world * n * args.steps / (comp_ms / 1e3) / 1e6,
                           "unit": "Mrays/s", "node_bytes": comp_node_size},
            "clocks": clk}

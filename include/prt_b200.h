@@ -180,6 +180,11 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  and a tree it does not fit makes the query fail with
  *                  PRT_ERR_DEVICE, never a wrong answer)
  *   "build_compressed" 1 = set_tris also builds the compressed nodes (default 1)
+ *   "build_sah"    1 = set_tris builds the binary tree top-down with binned SAH, as
+ *                  portableRT's own build does (default 1: about 5x the build time of
+ *                  0 = Morton LBVH, for about 10 % fewer node visits per ray); an SAH
+ *                  tree too deep for the traversal falls back to the LBVH.  Batches
+ *                  and request servers always build LBVH trees.
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
@@ -188,7 +193,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  work runs out; default 2): lower lets an express wave start sooner
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
- * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "node_bytes", "tri_bytes",
+ * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree
+ *   is an SAH tree), "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);

@@ -26,6 +26,7 @@
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
+#include "prt_sah.cuh"
 
 namespace prt {
 
@@ -33,7 +34,8 @@ void BuildScratch::release() {
 	DevBuf *all[] = {&keys,        &vals,     &keys2,      &vals2,    &scene_of,   &int_off,
 	                 &left,        &right,    &parent_int, &parent_leaf, &rfirst,  &rlast,
 	                 &ibox,        &lbox,     &flags,      &items_a,  &items_b,    &counters,
-	                 &perm,        &sort_hist, &sort_tiles, &sort_status, &bounds};
+	                 &perm,        &sort_hist, &sort_tiles, &sort_status, &bounds,
+	                 &sah,         &roots};
 	for (DevBuf *b : all)
 		b->release();
 	if (h_counters)
@@ -775,7 +777,7 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 
 int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg) {
+               std::string &msg, bool sah) {
 	if (leaf_size < 1 || leaf_size > kMaxLeaf) {
 		msg = "leaf_size must be in [1, 8]";
 		return PRT_ERR_ARG;
@@ -800,6 +802,7 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	plan.leaf_size = leaf_size;
 	plan.compressed = compressed;
 	plan.multi = S > 1;
+	plan.sah = sah;
 	plan.toff.resize(S + 1);
 	plan.ioff.resize(S + 1);
 	for (uint32_t s = 0; s <= S; ++s)
@@ -831,7 +834,8 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	sc.h_tri_off.assign(tri_off64, tri_off64 + S + 1);
 
 	const size_t key_bytes = plan.multi ? 8 : 4;
-	const size_t ni = std::max<uint32_t>(plan.n_int, 1);
+	// SAH node ids run up to n_int + S (scene s's root is node s).
+	const size_t ni = std::max<size_t>((size_t)plan.n_int + (sah ? S : 0u), 1);
 	const size_t nn = std::max<uint32_t>(n, 1);
 	BUILD_TRY(sc.tri_off.reserve(4ull * (S + 1)));
 	BUILD_TRY(ws.keys.reserve(key_bytes * nn));
@@ -858,6 +862,10 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	BUILD_TRY(ws.sort_tiles.reserve(8 * 4));
 	BUILD_TRY(ws.sort_status.reserve(4 * sort_status_words(n)));
 	BUILD_TRY(ws.bounds.reserve(24ull * S));
+	if (sah) {
+		BUILD_TRY(ws.sah.reserve(sah_scratch_bytes(n, S)));
+		BUILD_TRY(ws.roots.reserve(4ull * S));
+	}
 	BUILD_TRY(sc.tri4.reserve(48 * nn));
 	BUILD_TRY(sc.inv.reserve(4 * nn));
 	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)plan.node_cap));
@@ -872,24 +880,22 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	return PRT_OK;
 }
 
-int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
-                  cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg) {
+// Morton codes, radix sort, Karras hierarchy and refit: the binary trees of the LBVH
+// path, with svals set to the sorted triangle order.
+static int lbvh_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &ws,
+                        const uint32_t *d_toff, const uint32_t *d_ioff, const uint32_t *scene_of,
+                        cudaStream_t st, uint32_t *d_err, const uint32_t *&svals, std::string &msg) {
 	const uint32_t S = plan.S, n = plan.n, n_int = plan.n_int;
 	const size_t ni = std::max<uint32_t>(n_int, 1);
 	const size_t nn = std::max<uint32_t>(n, 1);
-	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
-	uint32_t *d_ioff = ws.int_off.as<uint32_t>();
-	uint32_t *scene_of = plan.multi ? ws.scene_of.as<uint32_t>() : nullptr;
-	if (plan.multi)
-		k_scene_of<<<std::min(S, 4096u), 256, 0, st>>>(d_toff, S, scene_of);
 	uint32_t *gb = ws.bounds.as<uint32_t>();
+	svals = ws.vals.as<uint32_t>();
 	k_bounds_init<<<blocks_for(6ull * S, 256), 256, 0, st>>>(gb, S);
 	if (n)
 		k_centroid_bounds<<<std::min(blocks_for(n, 256), 2048u), 256, 0, st>>>(d_tris, n, scene_of,
 		                                                                        gb);
 	SortScratch ss{ws.sort_hist.as<uint32_t>(), ws.sort_tiles.as<uint32_t>(),
 	               ws.sort_status.as<uint32_t>()};
-	const uint32_t *svals = ws.vals.as<uint32_t>();
 	const void *skeys = ws.keys.p;
 	if (n && !plan.multi) {
 		k_morton<uint32_t><<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, nullptr, gb,
@@ -933,11 +939,40 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 			    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.lbox.as<float4>(),
 			    ws.ibox.as<float4>(), ws.flags.as<uint32_t>(), d_err);
 	}
+	return PRT_OK;
+}
+
+int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
+                  cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg) {
+	const uint32_t S = plan.S, n = plan.n, n_int = plan.n_int;
+	const size_t ni = std::max<uint32_t>(n_int, 1);
+	const size_t nn = std::max<uint32_t>(n, 1);
+	if (plan.sah && !host_checks) {
+		msg = "the SAH build reads its level counters on the host";
+		return PRT_ERR_ARG;
+	}
+	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
+	uint32_t *d_ioff = ws.int_off.as<uint32_t>();
+	uint32_t *scene_of = plan.multi ? ws.scene_of.as<uint32_t>() : nullptr;
+	if (plan.multi)
+		k_scene_of<<<std::min(S, 4096u), 256, 0, st>>>(d_toff, S, scene_of);
+	const uint32_t *svals = ws.vals.as<uint32_t>();
+	const uint32_t *roots = d_ioff;
+	if (plan.sah) {
+		int rc = sah_build_enqueue(d_tris, plan, ws, d_toff, scene_of, st, d_err, msg);
+		if (rc != PRT_OK)
+			return rc;
+		roots = ws.roots.as<uint32_t>();
+	} else {
+		int rc = lbvh_enqueue(d_tris, plan, ws, d_toff, d_ioff, scene_of, st, d_err, svals, msg);
+		if (rc != PRT_OK)
+			return rc;
+	}
 
 	uint32_t *ctr = ws.counters.as<uint32_t>();
 	BUILD_TRY(cudaMemsetAsync(ctr, 0, 4 * kCtrWords, st));
 	Item *items[2] = {ws.items_a.as<Item>(), ws.items_b.as<Item>()};
-	k_collapse_roots<<<blocks_for(S, 128), 128, 0, st>>>(d_toff, d_ioff, S, items[0], ctr);
+	k_collapse_roots<<<blocks_for(S, 128), 128, 0, st>>>(d_toff, roots, S, items[0], ctr);
 	int level = 0;
 	for (;;) {
 		for (int k = 0; (host_checks ? k < kLevelsPerCheck : true) && level < kMaxLevels;
@@ -1006,18 +1041,18 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
-                 uint32_t *d_err, std::string &msg) {
+                 uint32_t *d_err, std::string &msg, bool sah) {
 	BuildPlan plan;
-	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg);
+	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg, sah);
 	if (rc != PRT_OK)
 		return rc;
 	return build_enqueue(d_tris, plan, sc, ws, st, d_err, true, msg);
 }
 
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
-                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg) {
+                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg, bool sah) {
 	const uint64_t off[2] = {0, n};
-	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg);
+	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg, sah);
 }
 
 } // namespace prt

@@ -84,6 +84,8 @@ struct BuildScratch {
 	DevBuf perm;                      // leaf-order slot -> sorted index
 	DevBuf sort_hist, sort_tiles, sort_status;
 	DevBuf bounds;                    // centroid bounds, 6 ordered words per scene
+	DevBuf sah;                       // SAH build: records, task lists, bins, counters
+	DevBuf roots;                     // SAH build: root binary node of each scene
 	uint32_t *h_counters = nullptr;   // pinned mirror of `counters`
 	void release();
 };
@@ -93,14 +95,17 @@ struct BuildPlan {
 	uint32_t S = 0, n = 0, n_int = 0, node_cap = 0;
 	int leaf_size = 1, scene_digits = 0;
 	bool compressed = false, multi = false;
+	bool sah = false;                 // binned-SAH binary trees instead of LBVH
 	std::vector<uint32_t> toff, ioff; // triangle and binary-node offsets per scene
 };
 
 // Validates the offsets, reserves every buffer of the build and queues the uploads of
 // the offset tables on `st`.  Nothing after it allocates.
+// sah: build the binary trees top-down with binned SAH (prt_sah.cu) instead of the
+// Morton/Karras hierarchy; needs host checks.
 int build_plan(const uint64_t *tri_off, uint32_t n_scenes, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg);
+               std::string &msg, bool sah = false);
 
 // Queues the build kernels.  host_checks: read the level counters every few levels and
 // finish with build_finish (synchronises).  Without host checks nothing synchronises:
@@ -119,10 +124,11 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 // Synchronises `st` (a few times, never per tree level).  Returns PRT_* status.
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
-                 uint32_t *d_err, std::string &msg);
+                 uint32_t *d_err, std::string &msg, bool sah = false);
 
 // One scene: build_scenes with tri_off = {0, n}.
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
-                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg);
+                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg,
+                bool sah = false);
 
 } // namespace prt

@@ -67,6 +67,8 @@ int check_device_errors(prt_b200_ctx *ctx) {
 			m += " radix-sort look-back timed out;";
 		if (e & prt::kErrCollapse)
 			m += " collapse exceeded the node budget;";
+		if (e & prt::kErrSah)
+			m += " SAH build failed a range check;";
 		return fail(ctx, PRT_ERR_DEVICE, m);
 	}
 	return PRT_OK;
@@ -82,8 +84,17 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	CAPI_TRY(ctx, cudaEventCreate(&e1));
 	cudaEventRecord(e0, ctx->stream);
 	std::string msg;
+	bool sah = ctx->build_sah;
 	int rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
-	                          ctx->ws, ctx->stream, ctx->d_err(), msg);
+	                          ctx->ws, ctx->stream, ctx->d_err(), msg, sah);
+	if (sah && rc == PRT_ERR_LIMIT) {
+		// An SAH tree deeper than the collapse's 32 levels: the LBVH's depth is bounded.
+		sah = false;
+		msg.clear();
+		rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
+		                      ctx->ws, ctx->stream, ctx->d_err(), msg, false);
+	}
+	ctx->last_build_sah = sah;
 	cudaEventRecord(e1, ctx->stream);
 	cudaEventSynchronize(e1);
 	float ms = 0.0f;
@@ -491,6 +502,8 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		ctx->count = v != 0;
 	} else if (k == "build_compressed") {
 		ctx->build_compressed = v != 0;
+	} else if (k == "build_sah") {
+		ctx->build_sah = v != 0;
 	} else {
 		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
 	}
@@ -511,6 +524,8 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
 		*value = s.depth;
 	else if (k == "build_ms")
 		*value = ctx->build_ms;
+	else if (k == "build_sah")
+		*value = ctx->last_build_sah ? 1.0 : 0.0;
 	else if (k == "node_bytes")
 		*value = (double)s.n_nodes *
 		         (ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8) : sizeof(prt::Node8));

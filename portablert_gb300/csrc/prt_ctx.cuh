@@ -73,6 +73,8 @@ struct prt_b200_ctx {
 	int serve_batches_per_warp = 2; // request servers created later ("serve_batches_per_warp")
 	bool count = false;
 	bool build_compressed = true;
+	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)
+	bool last_build_sah = false; // the scene's tree is an SAH tree
 	double build_ms = 0.0;
 	unsigned long long visits[2] = {0, 0};
 

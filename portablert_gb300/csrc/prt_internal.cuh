@@ -31,6 +31,7 @@ enum : uint32_t {
 	kErrStack = 1u,    // traversal stack overflow (ray abandoned)
 	kErrLookback = 2u, // radix-sort look-back gave up waiting
 	kErrCollapse = 4u, // 8-wide collapse ran out of node slots
+	kErrSah = 8u,      // SAH build: a range, node id or task list check failed
 };
 
 // One child of an 8-wide FP32 node: its box and its reference, 32 B, so the lane that

@@ -75,13 +75,16 @@ def test_fuzz_against_exhaustive_search(gpu_backend, oracle_lib, seed):
     rays = _rays(rng, 3000, scale)
     want = oracle_lib.brute_force(tris, rays)
     try:
-        for leaf in (1, 4, 8):
-            gpu_backend.set_option("leaf_size", leaf)
-            gpu_backend.set_tris(tris)
-            for fmt in (0, 1):
-                gpu_backend.set_option("node_format", fmt)
-                got = gpu_backend.nearest_hits(rays, TAGS)
-                _check(got, want)
+        for sah in (1, 0):  # binned-SAH and LBVH builds
+            gpu_backend.set_option("build_sah", sah)
+            for leaf in (1, 4, 8):
+                gpu_backend.set_option("leaf_size", leaf)
+                gpu_backend.set_tris(tris)
+                for fmt in (0, 1):
+                    gpu_backend.set_option("node_format", fmt)
+                    got = gpu_backend.nearest_hits(rays, TAGS)
+                    _check(got, want)
     finally:
+        gpu_backend.set_option("build_sah", 1)
         gpu_backend.set_option("leaf_size", 1)
         gpu_backend.set_option("node_format", 0)

@@ -117,6 +117,43 @@ def test_budget_admission_and_limits(gpu_backend):
         srv.close()
 
 
+@pytest.mark.parametrize("leaf,fmt,per_warp", [(1, 0, 1), (8, 0, 2), (4, 1, 2), (8, 1, 0),
+                                               (1, 1, 3)])
+def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
+    """Every traversal variant a wave can run -- leaf sizes, node formats, warps bounded
+    to 1-3 batches of 32 rays or persistent (0) -- gives each request the records of
+    nearest_hits on its scene alone."""
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    sizes = [3000, 50_000, 7, 200_000]
+    tris, off, d_tris = _scenes(torch, sizes, 5800 + leaf)
+    tags = hitreg.TAGS
+    lay = hitreg.layout(tags)
+    try:
+        gpu_backend.set_option("leaf_size", leaf)
+        gpu_backend.set_option("node_format", fmt)
+        gpu_backend.set_option("serve_batches_per_warp", per_warp)
+        srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=128 << 20, lanes=3)
+        try:
+            reqs = [(i % len(sizes), workloads.soup_rays(5900 + i, [33, 70_000, 1, 9_999][i % 4]))
+                    for i in range(12)]
+            subs = [srv.submit(s, r, tags) for s, r in reqs]
+            for t, _ in subs:
+                assert srv.wait(t) >= 0
+        finally:
+            srv.close()
+        for (s, r), (_, out) in zip(reqs, subs):
+            gpu_backend.set_tris(tris[s])
+            bad = _fields_equal(out, gpu_backend.nearest_hits(r, tags), lay)
+            assert bad is None, (s, len(r), bad)
+    finally:
+        gpu_backend.set_option("leaf_size", 1)
+        gpu_backend.set_option("node_format", 0)
+        gpu_backend.set_option("serve_batches_per_warp", 2)
+
+
 def test_close_with_requests_queued(gpu_backend):
     import torch
 
