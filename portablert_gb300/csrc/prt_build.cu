@@ -1,9 +1,11 @@
-// prt_build.cu - LBVH build of 8-wide trees on the GPU, for one scene or many at once.
+// prt_build.cu - LBVH build of 8-wide trees on the GPU, for one scene or many at once,
+// and the stages every build shares (collapse, re-layout, compression).
 //
 // Replaces the single-threaded binned-SAH build of portableRT (bvh.hpp:58-193).  The
 // tree's shape does not affect the answers (every triangle whose own box passes the
-// reference slab test is examined; see prt_traverse.cu), so a fast parallel build is
-// used instead.  Several scenes are built in the same launches: scene s owns the input
+// reference slab test is examined; see prt_traverse.cu), only how many boxes a ray
+// passes: set_tris builds its binary tree with binned SAH (prt_sah.cu, steps 1-5
+// replaced), batches use this fast LBVH.  Several scenes are built in the same launches: scene s owns the input
 // triangles [tri_off[s], tri_off[s+1]), its sort key carries the scene index above the
 // Morton code, its binary nodes are the range [int_off[s], int_off[s+1]) and its 8-wide
 // root is node s.
