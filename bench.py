@@ -784,7 +784,8 @@ def run_gpu(args, world, rank):
            "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
                    "d2h_bytes_per_step": lay.size * n, "host_memory": "pinned",
                    "pageable_value": e2e_pageable},
-           "gpu_launches": args.steps,
+           # per step: the regular pass and the deferred pass of k_trace8
+           "gpu_launches": 2 * args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak, "traffic": traffic,
                         "peak_source": peak_kind,

@@ -5,10 +5,10 @@
 // tree's shape does not affect the answers (every triangle whose own box passes the
 // reference slab test is examined; see prt_traverse.cu), only how many boxes a ray
 // passes: set_tris builds its binary tree with binned SAH (prt_sah.cu, steps 1-5
-// replaced), batches use this fast LBVH.  Several scenes are built in the same launches: scene s owns the input
-// triangles [tri_off[s], tri_off[s+1]), its sort key carries the scene index above the
-// Morton code, its binary nodes are the range [int_off[s], int_off[s+1]) and its 8-wide
-// root is node s.
+// replaced), batches use this fast LBVH.  Several scenes are built in the same
+// launches: scene s owns the input triangles [tri_off[s], tri_off[s+1]), its sort key
+// carries the scene index above the Morton code, its binary nodes are the range
+// [int_off[s], int_off[s+1]) and its 8-wide root is node s.
 //   1. centroid bounds per scene  (k_centroid_bounds; warp reduce + ordered-int atomics)
 //   2. 30-bit Morton codes        (k_morton; 10 bits per axis, centroids normalised)
 //   3. onesweep radix sort        (prt_sort.cu; 4 digit passes, +1 or 2 for the scene)

@@ -66,6 +66,7 @@ struct TravArgs {
 	uint32_t max_leaf;       // most triangles in a leaf of any scene of the launch
 	uint32_t max_batches;    // batches per warp before it exits (0 = no bound)
 	uint32_t *counter;
+	uint32_t *deferred;      // batches the regular pass left to the general one
 	uint32_t *err;
 	unsigned long long *visits;
 	uint32_t use_cam;        // 1: rays of the single run come from `cam`, not seg0.rays
@@ -103,8 +104,11 @@ __device__ __forceinline__ void ld_nc_256(const void *p, float4 &a, float4 &b) {
 	    : "l"(p));
 }
 
+template <bool REGULAR>
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
+	if (REGULAR)
+		return regular_box(r, lx, hx, ly, hy, lz, hz);
 	return r.kind == 0 ? regular_box(r, lx, hx, ly, hy, lz, hz)
 	                   : conservative_box(r, lx, hx, ly, hy, lz, hz);
 }
@@ -153,7 +157,7 @@ __device__ __forceinline__ void test_queued(const float4 *__restrict__ tri4, War
 }
 
 // Child `k` of `node`: slab test and what it refers to.
-template <int FMT>
+template <int FMT, bool REGULAR>
 __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const RayC &r,
                                            uint32_t node, int k, bool &hit, bool &inner,
                                            uint32_t &child, uint32_t &leaf_n) {
@@ -167,7 +171,7 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 		const uint32_t ref = __float_as_uint(lo.w);
 		if (ref != kNone) {
 			inner = !ref_is_leaf(ref);
-			hit = box_test(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+			hit = box_test<REGULAR>(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
 			child = inner ? ref : leaf_first(ref);
 			leaf_n = inner ? 0u : leaf_count(ref);
 		}
@@ -194,7 +198,7 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 			const float hy = cdec_f(oy, byte_as_float(ck.x, 3), sy);
 			const float lz = cdec_f(oz, byte_as_float(ck.y, 0), sz);
 			const float hz = cdec_f(oz, byte_as_float(ck.y, 1), sz);
-			hit = box_test(r, lx, hx, ly, hy, lz, hz);
+			hit = box_test<REGULAR>(r, lx, hx, ly, hy, lz, hz);
 			if (inner) {
 				child = w1.x + __popc(imask & ((1u << k) - 1u));
 			} else {
@@ -215,10 +219,146 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 #define PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED 8
 #endif
 
+// The traversal of one batch of up to 32 rays (slots 0..nb-1 of S) through scene sd.
+// REGULAR: every ray of the batch has finite reciprocals, so inner boxes take the plain
+// slab test only (no branch to the conservative test per child).
+template <int FMT, bool COUNT, bool LEAF1, bool REGULAR>
+__device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uint32_t *queue,
+                                            uint32_t *pool, const SceneDesc &sd, uint32_t nb,
+                                            int lane, int g, int s, uint32_t lt,
+                                            uint32_t step_limit, uint32_t &n_visits,
+                                            uint32_t &n_tests) {
+	const float4 *__restrict__ tri4 = sd.tri4;
+	const void *__restrict__ nodes = sd.nodes;
+		uint32_t top = 0;  // items in the pool (warp-uniform)
+		uint32_t q = 0;    // queued triangles (warp-uniform)
+		uint32_t next = 0; // next slot whose root is not yet in the pool
+		uint32_t steps = 0;
+		for (;;) {
+			// Admit new rays while fewer than K items are pending.
+			if (top < (uint32_t)kItems && next < nb) {
+				const uint32_t add = min((uint32_t)kItems - top, nb - next);
+				if ((uint32_t)lane < add)
+					pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
+				top += add;
+				next += add;
+				__syncwarp();
+			}
+			if (top == 0u)
+				break;
+			if (++steps > step_limit) {
+				if (lane == 0)
+					atomicOr(a.err, kErrStack);
+				break;
+			}
+			const uint32_t take = min(top, (uint32_t)kItems);
+			top -= take;
+			const bool work = (uint32_t)g < take;
+			const uint32_t item = work ? pool[top + g] : 0u;
+			__syncwarp(); // the pops above are read before the pushes below overwrite them
+			const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
+			RayC r;
+			if (work)
+				r = slot_ray(S, slot);
+			if (COUNT && work && s == 0)
+				++n_visits;
+
+			bool hit[kChildPerLane], inner[kChildPerLane];
+			uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j) {
+				hit[j] = false;
+				inner[j] = false;
+				child[j] = 0;
+				leaf_n[j] = 0;
+				if (work)
+					test_child<FMT, REGULAR>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
+					                child[j], leaf_n[j]);
+			}
+
+			// Push the hit inner children as new items (lane order, then child order).
+			uint32_t n_push = 0, before = 0;
+			bool push[kChildPerLane];
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j) {
+				push[j] = hit[j] && inner[j];
+				const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
+				n_push += __popc(b);
+				before += __popc(b & lt);
+			}
+			if (top + n_push > a.pool_cap) {
+				if (lane == 0)
+					atomicOr(a.err, kErrStack);
+			} else {
+				uint32_t pos = top + before;
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j)
+					if (push[j])
+						pool[pos++] = (slot << kIndexBits) | child[j];
+				top += n_push;
+			}
+
+			// Queue the triangles of the hit leaf children.
+			uint32_t cnt[kChildPerLane], all_cnt = 0;
+			bool single = true;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j) {
+				cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
+				all_cnt += cnt[j];
+				single = single && cnt[j] <= 1u;
+			}
+			if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
+				uint32_t n_add = 0, pre = 0;
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j) {
+					const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
+					n_add += __popc(b);
+					pre += __popc(b & lt);
+				}
+				uint32_t pos = q + pre;
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j)
+					if (cnt[j])
+						queue[pos++] = (slot << kIndexBits) | child[j];
+				q += n_add;
+			} else {
+				uint32_t incl = all_cnt;
+#pragma unroll
+				for (int o = 1; o < 32; o <<= 1) {
+					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+					if (lane >= o)
+						incl += y;
+				}
+				uint32_t pos = q + incl - all_cnt;
+#pragma unroll
+				for (int j = 0; j < kChildPerLane; ++j)
+					for (uint32_t k = 0; k < cnt[j]; ++k)
+						queue[pos++] = (slot << kIndexBits) | (child[j] + k);
+				q += __shfl_sync(0xFFFFFFFFu, incl, 31);
+			}
+			__syncwarp();
+			while (q >= 32u) {
+				q -= 32u;
+				test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
+				__syncwarp();
+			}
+		}
+		while (q > 0u) {
+			const uint32_t n = min(q, 32u);
+			q -= n;
+			test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
+			__syncwarp();
+		}
+}
+
 // LEAF1: every leaf holds one triangle (leaf size 1), so a hit leaf queues exactly one.
 // BOUNDED: a warp takes at most a.max_batches batches (a separate instantiation, so the
 // unbounded kernels keep their register allocation).
-template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
+// PASS: 0 = every batch with the general box test (the counting runs); 1 = batches whose
+// rays all have finite reciprocals, with the plain slab test only (no conservative code
+// in the kernel at all: 8 % faster), the others counted in a.deferred and skipped; 2 =
+// the skipped batches with the general test (returns at once when there are none).
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
                                                            ? PRT_TRAVERSE_MIN_BLOCKS_FP32
                                                            : PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED)
@@ -233,7 +373,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 	uint32_t n_visits = 0, n_tests = 0;
 	// A tree is visited at most once per ray; more steps than this means a malformed
 	// tree, which is reported instead of looping.
-	const uint64_t step_limit = 32ull * a.n_nodes + 64ull;
+	const uint32_t step_limit = (uint32_t)min(32ull * a.n_nodes + 64ull, 0xFFFFFFFFull);
+	if (PASS == 2 && *(volatile const uint32_t *)a.deferred == 0u)
+		return; // the regular pass took every batch (it ran before, on the same stream)
+	// The deferred pass walks all batches in a fixed order, warp w taking w, w + W, ...
+	uint64_t next_batch = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
+	const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
 
 	if (BOUNDED && lane == 0)
 		S.batches = 0;
@@ -247,11 +392,19 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 				++S.batches;
 		}
 		uint32_t base = 0;
-		if (lane == 0)
-			base = atomicAdd(a.counter, 32u);
-		base = __shfl_sync(0xFFFFFFFFu, base, 0);
-		if (base >= a.n_virtual)
-			break;
+		if (PASS == 2) {
+			const uint64_t b64 = 32ull * next_batch;
+			next_batch += n_warps;
+			if (b64 >= a.n_virtual)
+				break;
+			base = (uint32_t)b64;
+		} else {
+			if (lane == 0)
+				base = atomicAdd(a.counter, 32u);
+			base = __shfl_sync(0xFFFFFFFFu, base, 0);
+			if (base >= a.n_virtual)
+				break;
+		}
 		// The run these 32 rays belong to (runs are padded to whole warps).
 		uint32_t si = 0;
 		if (a.n_segs) {
@@ -278,7 +431,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		const uint32_t nb = min(32u, run_rays - local);
 		const SceneDesc sd = a.n_segs ? a.scenes[S.seg.scene] : a.scene0;
 		const float4 *__restrict__ tri4 = sd.tri4;
-		const void *__restrict__ nodes = sd.nodes;
 
 		if ((uint32_t)lane < nb) {
 			RayC r;
@@ -302,125 +454,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		__syncwarp();
 
 		if (sd.n_tris) {
-			uint32_t top = 0;  // items in the pool (warp-uniform)
-			uint32_t q = 0;    // queued triangles (warp-uniform)
-			uint32_t next = 0; // next slot whose root is not yet in the pool
-			uint64_t steps = 0;
-			for (;;) {
-				// Admit new rays while fewer than K items are pending.
-				if (top < (uint32_t)kItems && next < nb) {
-					const uint32_t add = min((uint32_t)kItems - top, nb - next);
-					if ((uint32_t)lane < add)
-						pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
-					top += add;
-					next += add;
-					__syncwarp();
-				}
-				if (top == 0u)
-					break;
-				if (++steps > step_limit) {
-					if (lane == 0)
-						atomicOr(a.err, kErrStack);
-					break;
-				}
-				const uint32_t take = min(top, (uint32_t)kItems);
-				top -= take;
-				const bool work = (uint32_t)g < take;
-				const uint32_t item = work ? pool[top + g] : 0u;
-				__syncwarp(); // the pops above are read before the pushes below overwrite them
-				const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
-				RayC r;
-				if (work)
-					r = slot_ray(S, slot);
-				if (COUNT && work && s == 0)
-					++n_visits;
-
-				bool hit[kChildPerLane], inner[kChildPerLane];
-				uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j) {
-					hit[j] = false;
-					inner[j] = false;
-					child[j] = 0;
-					leaf_n[j] = 0;
-					if (work)
-						test_child<FMT>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
-						                child[j], leaf_n[j]);
-				}
-
-				// Push the hit inner children as new items (lane order, then child order).
-				uint32_t n_push = 0, before = 0;
-				bool push[kChildPerLane];
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j) {
-					push[j] = hit[j] && inner[j];
-					const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
-					n_push += __popc(b);
-					before += __popc(b & lt);
-				}
-				if (top + n_push > a.pool_cap) {
-					if (lane == 0)
-						atomicOr(a.err, kErrStack);
-				} else {
-					uint32_t pos = top + before;
-#pragma unroll
-					for (int j = 0; j < kChildPerLane; ++j)
-						if (push[j])
-							pool[pos++] = (slot << kIndexBits) | child[j];
-					top += n_push;
-				}
-
-				// Queue the triangles of the hit leaf children.
-				uint32_t cnt[kChildPerLane], all_cnt = 0;
-				bool single = true;
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j) {
-					cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
-					all_cnt += cnt[j];
-					single = single && cnt[j] <= 1u;
-				}
-				if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
-					uint32_t n_add = 0, pre = 0;
-#pragma unroll
-					for (int j = 0; j < kChildPerLane; ++j) {
-						const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
-						n_add += __popc(b);
-						pre += __popc(b & lt);
-					}
-					uint32_t pos = q + pre;
-#pragma unroll
-					for (int j = 0; j < kChildPerLane; ++j)
-						if (cnt[j])
-							queue[pos++] = (slot << kIndexBits) | child[j];
-					q += n_add;
-				} else {
-					uint32_t incl = all_cnt;
-#pragma unroll
-					for (int o = 1; o < 32; o <<= 1) {
-						const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-						if (lane >= o)
-							incl += y;
-					}
-					uint32_t pos = q + incl - all_cnt;
-#pragma unroll
-					for (int j = 0; j < kChildPerLane; ++j)
-						for (uint32_t k = 0; k < cnt[j]; ++k)
-							queue[pos++] = (slot << kIndexBits) | (child[j] + k);
-					q += __shfl_sync(0xFFFFFFFFu, incl, 31);
-				}
-				__syncwarp();
-				while (q >= 32u) {
-					q -= 32u;
-					test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
-					__syncwarp();
-				}
+			// Nearly every batch has only rays with finite reciprocals.
+			const bool regular =
+			    __all_sync(0xFFFFFFFFu, (uint32_t)lane >= nb || S.kind[lane] == 0);
+			if (PASS == 1 && !regular) {
+				if (lane == 0)
+					atomicAdd(a.deferred, 1u);
+				continue; // left to the deferred pass
 			}
-			while (q > 0u) {
-				const uint32_t n = min(q, 32u);
-				q -= n;
-				test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
-				__syncwarp();
-			}
+			if (PASS == 2 && regular)
+				continue; // done by the regular pass
+			trace_batch<FMT, COUNT, LEAF1, PASS == 1>(a, S, queue, pool, sd, nb, lane, g, s, lt,
+			                                          step_limit, n_visits, n_tests);
+		} else if (PASS == 2) {
+			continue; // the regular pass wrote this empty scene's misses
 		}
 		__syncwarp();
 
@@ -504,18 +551,18 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 }
 
 // Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each.
-template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 int blocks_per_sm(int warps, uint32_t warp_bytes) {
 	static int cached_warps = -1;
 	static uint32_t cached_bytes = 0;
 	static int cached = 0;
 	if (cached_warps != warps || cached_bytes != warp_bytes) {
 		const size_t smem = (size_t)warp_bytes * warps;
-		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1, BOUNDED>,
+		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>,
 		                     cudaFuncAttributeMaxDynamicSharedMemorySize,
 		                     (int)smem);
 		int b = 0;
-		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1, BOUNDED>,
+		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>,
 		                                              32 * warps, smem);
 		cached = b > 0 ? b : 1;
 		cached_warps = warps;
@@ -524,33 +571,40 @@ int blocks_per_sm(int warps, uint32_t warp_bytes) {
 	return cached;
 }
 
-template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED>
+template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 void launch_t(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	const int bps = blocks_per_sm<FMT, COUNT, LEAF1, BOUNDED>(warps, a.warp_bytes);
+	const int bps = blocks_per_sm<FMT, COUNT, LEAF1, BOUNDED, PASS>(warps, a.warp_bytes);
 	const uint64_t batches = (a.n_virtual + 31ull) / 32ull;
 	// Unbounded warps: at most one block per resident slot (persistent).  Bounded: enough
 	// blocks that every batch has a warp even if each warp takes its maximum.
 	const uint64_t per_block = (uint64_t)warps * (BOUNDED ? a.max_batches : 1u);
 	const uint64_t need = (batches + per_block - 1) / per_block;
 	const uint64_t grid = BOUNDED ? need : std::min<uint64_t>((uint64_t)sm_count * bps, need);
-	k_trace8<FMT, COUNT, LEAF1, BOUNDED>
+	k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>
 	    <<<(unsigned)grid, 32 * warps, (size_t)a.warp_bytes * warps, st>>>(a);
+}
+
+template <int FMT, bool LEAF1>
+void launch_passes(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
+	if (a.max_batches > 0)
+		launch_t<FMT, false, LEAF1, true, 1>(a, warps, sm_count, st);
+	else
+		launch_t<FMT, false, LEAF1, false, 1>(a, warps, sm_count, st);
+	launch_t<FMT, false, LEAF1, false, 2>(a, warps, sm_count, st);
 }
 
 template <int FMT, bool COUNT>
 void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	// Bounded warps only without the visit counters (a counting run takes the whole work).
-	const bool bounded = !COUNT && a.max_batches > 0;
-	if (a.max_leaf <= 1u) {
-		if (bounded)
-			launch_t<FMT, false, true, true>(a, warps, sm_count, st);
+	// A counting run is one general pass over all the work (no bounded warps).
+	if (COUNT) {
+		if (a.max_leaf <= 1u)
+			launch_t<FMT, true, true, false, 0>(a, warps, sm_count, st);
 		else
-			launch_t<FMT, COUNT, true, false>(a, warps, sm_count, st);
+			launch_t<FMT, true, false, false, 0>(a, warps, sm_count, st);
+	} else if (a.max_leaf <= 1u) {
+		launch_passes<FMT, true>(a, warps, sm_count, st);
 	} else {
-		if (bounded)
-			launch_t<FMT, false, false, true>(a, warps, sm_count, st);
-		else
-			launch_t<FMT, COUNT, false, false>(a, warps, sm_count, st);
+		launch_passes<FMT, false>(a, warps, sm_count, st);
 	}
 }
 
@@ -571,6 +625,8 @@ int warps_for(const TravConfig &cfg) {
 
 cudaError_t dispatch(const TravArgs &a, const TravConfig &cfg, int sm_count, cudaStream_t st) {
 	cudaError_t e = cudaMemsetAsync(a.counter, 0, 4, st);
+	if (e == cudaSuccess)
+		e = cudaMemsetAsync(a.deferred, 0, 4, st);
 	if (e != cudaSuccess)
 		return e;
 	const int warps = warps_for(cfg);
@@ -631,6 +687,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : sc.depth, sc.leaf_size);
 		a.max_batches = cfg.max_batches;
 		a.counter = d_work;
+		a.deferred = d_work + 2;
 		a.err = d_err;
 		a.visits = d_visits;
 		cudaError_t e = dispatch(a, cfg, sm_count, st);
@@ -662,6 +719,7 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
 	size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : depth, leaf_size);
 	a.max_batches = cfg.max_batches;
 	a.counter = d_work;
+	a.deferred = d_work + 2;
 	a.err = d_err;
 	a.visits = d_visits;
 	return dispatch(a, cfg, sm_count, st);

@@ -56,8 +56,9 @@ int traversal_stack_depth();
 
 // Queues one nearest-hit pass over n rays of one scene (device memory, 6 floats each,
 // or when cam is not null the camera's rays 0..n-1, n <= 2^31) on `st`.  d_work:
-// device scratch (ray counter); d_visits: 2 uint64 counters (node visits, triangle
-// tests), used when cfg.count.
+// device scratch of at least 3 words: [0] the ray counter, [2] the count of batches left
+// to the general pass ([1] is not touched: callers keep their error word there);
+// d_visits: 2 uint64 counters (node visits, triangle tests), used when cfg.count.
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
                                 uint32_t *d_work, unsigned long long *d_visits, uint32_t *d_err,
@@ -68,7 +69,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 // its own output layout.  d_scenes / d_segs: device copies of the tables (segments
 // sorted by vbegin); n_virtual: the padded ray count (end of the last run).  depth and
 // leaf_size: the largest over the scenes (they size the shared-memory pool and queue);
-// n_nodes: the largest node array (bounds the steps of a batch).
+// n_nodes: the largest node array (bounds the steps of a batch).  d_work as above.
 cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDesc *d_segs,
                                          uint32_t n_segs, unsigned long long n_virtual,
                                          uint32_t depth, int leaf_size, uint32_t n_nodes,
