@@ -66,7 +66,8 @@ struct TravArgs {
 	uint32_t max_leaf;       // most triangles in a leaf of any scene of the launch
 	uint32_t max_batches;    // batches per warp before it exits (0 = no bound)
 	uint32_t *counter;
-	uint32_t *deferred;      // batches the regular pass left to the general one
+	uint32_t *deferred;      // [0] batches the regular pass left to the general one,
+	                         // [1] the deferred pass's batch counter
 	uint32_t *err;
 	unsigned long long *visits;
 	uint32_t use_cam;        // 1: rays of the single run come from `cam`, not seg0.rays
@@ -376,9 +377,6 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 	const uint32_t step_limit = (uint32_t)min(32ull * a.n_nodes + 64ull, 0xFFFFFFFFull);
 	if (PASS == 2 && *(volatile const uint32_t *)a.deferred == 0u)
 		return; // the regular pass took every batch (it ran before, on the same stream)
-	// The deferred pass walks all batches in a fixed order, warp w taking w, w + W, ...
-	uint64_t next_batch = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5;
-	const uint64_t n_warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
 
 	if (BOUNDED && lane == 0)
 		S.batches = 0;
@@ -391,20 +389,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			if (lane == 0)
 				++S.batches;
 		}
+		// Batches are taken in order from a counter (the deferred pass has its own, so
+		// the few batches it works on spread over all warps).
 		uint32_t base = 0;
-		if (PASS == 2) {
-			const uint64_t b64 = 32ull * next_batch;
-			next_batch += n_warps;
-			if (b64 >= a.n_virtual)
-				break;
-			base = (uint32_t)b64;
-		} else {
-			if (lane == 0)
-				base = atomicAdd(a.counter, 32u);
-			base = __shfl_sync(0xFFFFFFFFu, base, 0);
-			if (base >= a.n_virtual)
-				break;
-		}
+		if (lane == 0)
+			base = atomicAdd(PASS == 2 ? a.deferred + 1 : a.counter, 32u);
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (base >= a.n_virtual)
+			break;
 		// The run these 32 rays belong to (runs are padded to whole warps).
 		uint32_t si = 0;
 		if (a.n_segs) {
@@ -595,12 +587,15 @@ void launch_passes(const TravArgs &a, int warps, int sm_count, cudaStream_t st) 
 
 template <int FMT, bool COUNT>
 void launch(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
-	// A counting run is one general pass over all the work (no bounded warps).
-	if (COUNT) {
+	// A counting run is one general pass over all the work (no bounded warps).  So are
+	// camera rays: the examples' cameras put a zero direction component in one batch of
+	// every row, and finding those batches again costs the deferred pass a recomputation
+	// of every ray.
+	if (COUNT || a.use_cam) {
 		if (a.max_leaf <= 1u)
-			launch_t<FMT, true, true, false, 0>(a, warps, sm_count, st);
+			launch_t<FMT, COUNT, true, false, 0>(a, warps, sm_count, st);
 		else
-			launch_t<FMT, true, false, false, 0>(a, warps, sm_count, st);
+			launch_t<FMT, COUNT, false, false, 0>(a, warps, sm_count, st);
 	} else if (a.max_leaf <= 1u) {
 		launch_passes<FMT, true>(a, warps, sm_count, st);
 	} else {
@@ -626,7 +621,7 @@ int warps_for(const TravConfig &cfg) {
 cudaError_t dispatch(const TravArgs &a, const TravConfig &cfg, int sm_count, cudaStream_t st) {
 	cudaError_t e = cudaMemsetAsync(a.counter, 0, 4, st);
 	if (e == cudaSuccess)
-		e = cudaMemsetAsync(a.deferred, 0, 4, st);
+		e = cudaMemsetAsync(a.deferred, 0, 8, st);
 	if (e != cudaSuccess)
 		return e;
 	const int warps = warps_for(cfg);

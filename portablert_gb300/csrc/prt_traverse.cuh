@@ -56,8 +56,9 @@ int traversal_stack_depth();
 
 // Queues one nearest-hit pass over n rays of one scene (device memory, 6 floats each,
 // or when cam is not null the camera's rays 0..n-1, n <= 2^31) on `st`.  d_work:
-// device scratch of at least 3 words: [0] the ray counter, [2] the count of batches left
-// to the general pass ([1] is not touched: callers keep their error word there);
+// device scratch of at least 4 words: [0] the ray counter, [2] the count of batches left
+// to the general pass, [3] that pass's batch counter ([1] is not touched: callers keep
+// their error word there);
 // d_visits: 2 uint64 counters (node visits, triangle tests), used when cfg.count.
 cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_t n,
                                 const OutLayout &lay, void *d_out, const TravConfig &cfg,
