@@ -165,7 +165,8 @@ int prt_b200_batch_run_graph(prt_b200_batch *batch, const float *d_tris,
 /* Waits for the batch's launches and reports kernel-side errors. */
 int prt_b200_batch_sync(prt_b200_batch *batch);
 
-/* "n_scenes", "n_tris", "n_nodes", "depth", "build_ms", "visits_nodes", "visits_tris". */
+/* "n_scenes", "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = set_tris_dev
+ * built SAH trees), "visits_nodes", "visits_tris". */
 int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
 
 /* Tuning and statistics.  Options (take effect at the next set_tris unless noted):
@@ -183,8 +184,9 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "build_sah"    1 = set_tris builds the binary tree top-down with binned SAH, as
  *                  portableRT's own build does (default 1: about 5x the build time of
  *                  0 = Morton LBVH, for about 10 % fewer node visits per ray); an SAH
- *                  tree too deep for the traversal falls back to the LBVH.  Batches
- *                  and request servers always build LBVH trees.
+ *                  tree too deep for the traversal falls back to the LBVH.  Also
+ *                  batch_set_tris_dev and request servers; batch graphs always build
+ *                  LBVH trees.
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)

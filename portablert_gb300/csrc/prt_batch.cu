@@ -260,8 +260,18 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 	B_TRY(ctx, cudaEventCreate(&e1));
 	cudaEventRecord(e0, ctx->stream);
 	std::string msg;
+	// Binned-SAH trees as set_tris builds them (option build_sah); a tree too deep for
+	// the collapse falls back to the LBVH.  Graph builds (run_graph) are always LBVH.
+	bool sah = ctx->build_sah;
 	int rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg);
+	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg, sah);
+	if (sah && rc == PRT_ERR_LIMIT) {
+		sah = false;
+		msg.clear();
+		rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
+		                       b->arena, b->ws, ctx->stream, ctx->d_err(), msg, false);
+	}
+	b->built_sah = sah;
 	cudaEventRecord(e1, ctx->stream);
 	cudaEventSynchronize(e1);
 	float ms = 0.0f;
@@ -442,6 +452,8 @@ int prt_b200_batch_stat(prt_b200_batch *b, const char *key, double *value) {
 		*value = a.depth;
 	else if (k == "build_ms")
 		*value = b->build_ms;
+	else if (k == "build_sah")
+		*value = b->built_sah ? 1.0 : 0.0;
 	else if (k == "visits_nodes")
 		*value = (double)b->visits[0];
 	else if (k == "visits_tris")

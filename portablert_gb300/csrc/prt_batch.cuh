@@ -34,6 +34,7 @@ struct prt_b200_batch {
 	prt::BatchSlot slots[prt::kSlots];
 	int next_slot = 0;
 	double build_ms = 0.0;
+	bool built_sah = false; // the resident trees are SAH trees (set_tris_dev)
 	unsigned long long visits[2] = {0, 0};
 	uint32_t *h_words = nullptr; // pinned: error word and visit counters read back
 	// CUDA graph of build + query

@@ -109,3 +109,37 @@ def test_equals_lbvh_with_fewer_visits(gpu_backend, scene):
         gpu_backend.set_option("build_sah", 1)
     assert res[0][0].tobytes() == res[1][0].tobytes()
     assert res[1][1] < res[0][1], (res[1][1], res[0][1])
+
+
+def test_many_scenes_in_one_sah_build(gpu_backend, oracle_lib):
+    """batch_set_tris_dev builds every scene's SAH tree in the same launches (tasks of all
+    scenes side by side): each scene's records equal its exhaustive search."""
+    import torch
+
+    from portablert_gb300.batch import Batch, make_query
+
+    sizes = [0, 1, 2, 33, 1025, 2049, 5000, 40_000, 3]
+    tris = [W.soup_tris(9300 + s, n) for s, n in enumerate(sizes)]
+    rays = [W.soup_rays(9400 + s, 1500) for s in range(len(sizes))]
+    off = np.cumsum([0] + sizes)
+    d_tris = torch.from_numpy(np.concatenate(tris)).cuda()
+    lay = hitreg.layout(TAGS)
+    keep, qs = [], []
+    for s, r in enumerate(rays):
+        d_r = torch.from_numpy(r).cuda()
+        d_o = torch.zeros(len(r) * lay.size, dtype=torch.uint8, device="cuda")
+        qs.append(make_query(s, d_r.data_ptr(), len(r), d_o.data_ptr(), TAGS))
+        keep.append((d_r, d_o))
+    torch.cuda.synchronize()
+    b = Batch(gpu_backend)
+    try:
+        b.set_tris_dev(d_tris.data_ptr(), off)
+        assert b.stat("build_sah") == 1.0
+        b.query_dev(qs)
+        b.sync()
+        torch.cuda.synchronize()
+        for s in range(len(sizes)):
+            got = keep[s][1].cpu().numpy().view(lay.numpy_dtype())
+            _same(got, oracle_lib.brute_force(tris[s], rays[s]))
+    finally:
+        b.close()
