@@ -187,6 +187,9 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  tree too deep for the traversal falls back to the LBVH.  Also
  *                  batch_set_tris_dev and request servers; batch graphs always build
  *                  LBVH trees.
+ *   "collapse_cost" 1 = the binary tree is collapsed to 8-wide nodes by the least
+ *                  expected cost per ray (a bottom-up pass chooses which subtrees become
+ *                  nodes and leaves), 0 = by opening the largest child first (default 1)
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)

@@ -155,8 +155,9 @@ size_t graph_key(const float *d_tris, const uint64_t *tri_off, uint32_t S,
 	std::string k(reinterpret_cast<const char *>(&d_tris), sizeof d_tris);
 	k.append(reinterpret_cast<const char *>(tri_off), sizeof(uint64_t) * (S + 1));
 	k.append(reinterpret_cast<const char *>(q), sizeof(prt_b200_query) * nq);
-	const int opts[6] = {ctx->leaf_size,      ctx->node_format,       ctx->block,
-	                     (int)ctx->count,     ctx->pool_depth,        (int)ctx->build_compressed};
+	const int opts[7] = {ctx->leaf_size,      ctx->node_format,       ctx->block,
+	                     (int)ctx->count,     ctx->pool_depth,        (int)ctx->build_compressed,
+	                     (int)ctx->collapse_cost};
 	k.append(reinterpret_cast<const char *>(opts), sizeof opts);
 	return h(k);
 }
@@ -264,12 +265,14 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 	// the collapse falls back to the LBVH.  Graph builds (run_graph) are always LBVH.
 	bool sah = ctx->build_sah;
 	int rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg, sah);
+	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg, sah,
+	                           ctx->collapse_cost);
 	if (sah && rc == PRT_ERR_LIMIT) {
 		sah = false;
 		msg.clear();
 		rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-		                       b->arena, b->ws, ctx->stream, ctx->d_err(), msg, false);
+		                       b->arena, b->ws, ctx->stream, ctx->d_err(), msg, false,
+		                       ctx->collapse_cost);
 	}
 	b->built_sah = sah;
 	cudaEventRecord(e1, ctx->stream);
@@ -350,7 +353,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 		std::string msg;
 		// Plan: reserve everything and upload the offset tables outside the graph.
 		rc = prt::build_plan(tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed, b->arena,
-		                     b->ws, ctx->stream, b->gplan, msg);
+		                     b->ws, ctx->stream, b->gplan, msg, false, ctx->collapse_cost);
 		if (rc != PRT_OK)
 			return bfail(ctx, rc, msg);
 		b->arena.has_cnodes = ctx->build_compressed;

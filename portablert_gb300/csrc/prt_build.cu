@@ -37,7 +37,7 @@ void BuildScratch::release() {
 	                 &left,        &right,    &parent_int, &parent_leaf, &rfirst,  &rlast,
 	                 &ibox,        &lbox,     &flags,      &items_a,  &items_b,    &counters,
 	                 &perm,        &sort_hist, &sort_tiles, &sort_status, &bounds,
-	                 &sah,         &roots};
+	                 &sah,         &roots,    &cost};
 	for (DevBuf *b : all)
 		b->release();
 	if (h_counters)
@@ -377,6 +377,144 @@ __global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__
 	}
 }
 
+// Cost-optimal collapse.  Without culling by t, a ray tests the children of every 8-wide
+// node whose box it passes and every triangle of every leaf box it passes, so the
+// expected work per ray is proportional to the sum of area x cost over those boxes: 1
+// per 8-wide node, kTriCost per triangle of a leaf.  A bottom-up pass computes for each
+// binary node the least cost of its subtree in a single child slot (c1: as a leaf, or
+// as an 8-wide node whose 8 slots are shared out below it) and in i = 2..8 slots when
+// the node itself is opened (cd), with the split of the slots between its children; the
+// collapse then opens exactly what the optimum opens.  (The dynamic programme of Ylitie,
+// Karras and Laine 2017 for compressed wide BVHs, restated for this traversal's costs.)
+// Costs are stored in units of the node's own surface area (expected work once a ray
+// passes its box), so they stay in float range whatever the scene's scale; a child
+// enters its parent's sums weighted by the ratio of the two areas, both computed from
+// half extents divided by the parent's largest one (values in [0, 1]: no overflow for
+// [-FLT_MAX, FLT_MAX] boxes, no underflow for tiny scenes).
+constexpr float kTriCost = 0.25f; // a triangle test against a node visit (measured)
+
+struct CostNode {
+	float c1;
+	float cd[7];   // slots 2..8
+	uint32_t bits; // 3 bits per slot count i = 2..8: (left share - 1); bit 31: leaf is best
+};
+
+__device__ __forceinline__ float3 half_extent(float4 lo, float4 hi) {
+	return make_float3(fmaxf(hi.x * 0.5f - lo.x * 0.5f, 0.0f),
+	                   fmaxf(hi.y * 0.5f - lo.y * 0.5f, 0.0f),
+	                   fmaxf(hi.z * 0.5f - lo.z * 0.5f, 0.0f));
+}
+
+// Surface area (up to a constant) of a box of half extents e, in units of unit^2.
+__device__ __forceinline__ float scaled_area(float3 e, float unit) {
+	if (!(unit > 0.0f))
+		return 0.0f;
+	const float x = fminf(e.x / unit, 1.0f), y = fminf(e.y / unit, 1.0f),
+	            z = fminf(e.z / unit, 1.0f);
+	return x * y + x * z + y * z;
+}
+
+__device__ __forceinline__ uint32_t split_of(uint32_t bits, uint32_t i) {
+	const uint32_t a = ((bits >> (3u * (i - 2u))) & 7u) + 1u;
+	return min(max(a, 1u), i - 1u);
+}
+
+// Costs of child `y` in j = 1..7 slots (cs[j]), in units of its own area; returns its
+// half extents.
+__device__ __forceinline__ float3 child_costs(uint32_t y, const CostNode *cost,
+                                              const float4 *ibox, const float4 *lbox,
+                                              float cs[8]) {
+	if (y & kLeafBit) {
+		const uint32_t k = y & ~kLeafBit;
+#pragma unroll
+		for (int j = 1; j < 8; ++j)
+			cs[j] = kTriCost;
+		return half_extent(__ldcg(&lbox[2 * k]), __ldcg(&lbox[2 * k + 1]));
+	}
+	const float c1 = __ldcg(&cost[y].c1);
+	cs[1] = c1;
+#pragma unroll
+	for (int j = 2; j < 8; ++j)
+		cs[j] = fminf(c1, __ldcg(&cost[y].cd[j - 2]));
+	return half_extent(__ldcg(&ibox[2 * y]), __ldcg(&ibox[2 * y + 1]));
+}
+
+// One thread per leaf walks towards the root like k_refit; the second thread to arrive
+// at a binary node computes its costs from both children's.
+__global__ void k_collapse_cost(uint32_t n, uint32_t n_ids, const uint32_t *__restrict__ parent_leaf,
+                                const uint32_t *__restrict__ parent_int,
+                                const uint32_t *__restrict__ left, const uint32_t *__restrict__ right,
+                                const uint32_t *__restrict__ rfirst,
+                                const uint32_t *__restrict__ rlast, const float4 *__restrict__ ibox,
+                                const float4 *__restrict__ lbox, uint32_t *flags, CostNode *cost,
+                                uint32_t leaf_size, uint32_t *err) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n)
+		return;
+	uint32_t p = parent_leaf[i];
+	for (uint32_t steps = 0; p != kNone; ++steps) {
+		if (p >= n_ids || steps >= n_ids) {
+			atomicOr(err, kErrCollapse);
+			return;
+		}
+		if (arrive_acq_rel(&flags[p]) == 0u)
+			return;
+		float cl[8], cr[8];
+		const float3 el = child_costs(left[p], cost, ibox, lbox, cl);
+		const float3 er = child_costs(right[p], cost, ibox, lbox, cr);
+		const float3 ep = half_extent(__ldcg(&ibox[2 * p]), __ldcg(&ibox[2 * p + 1]));
+		const float unit = fmaxf(ep.x, fmaxf(ep.y, ep.z));
+		const float ap = scaled_area(ep, unit);
+		const float rl = ap > 0.0f ? fminf(scaled_area(el, unit) / ap, 1.0f) : 0.0f;
+		const float rr = ap > 0.0f ? fminf(scaled_area(er, unit) / ap, 1.0f) : 0.0f;
+#pragma unroll
+		for (int j = 1; j < 8; ++j) {
+			cl[j] *= rl;
+			cr[j] *= rr;
+		}
+		CostNode c;
+		c.bits = 0;
+#pragma unroll
+		for (uint32_t s = 2; s <= 8; ++s) {
+			float best = INFINITY;
+			uint32_t ba = 1;
+#pragma unroll
+			for (uint32_t a = 1; a < s; ++a) {
+				const float v = cl[a] + cr[s - a];
+				if (v < best) {
+					best = v;
+					ba = a;
+				}
+			}
+			c.cd[s - 2] = best;
+			c.bits |= (ba - 1u) << (3u * (s - 2u));
+		}
+		const uint32_t count = rlast[p] - rfirst[p] + 1u;
+		const float as_node = 1.0f + c.cd[6];
+		const bool may_leaf = count <= leaf_size;
+		const float as_leaf = kTriCost * (float)count;
+		c.c1 = may_leaf ? fminf(as_node, as_leaf) : as_node;
+		if (may_leaf && as_leaf <= as_node)
+			c.bits |= 0x80000000u;
+		__stcg(&cost[p].c1, c.c1);
+#pragma unroll
+		for (int k = 0; k < 7; ++k)
+			__stcg(&cost[p].cd[k], c.cd[k]);
+		__stcg(&cost[p].bits, c.bits);
+		p = parent_int[p];
+	}
+}
+
+// Child slot `r` of an 8-wide node becomes an 8-wide node of its own (else a leaf).
+__device__ __forceinline__ bool is_inner(uint32_t r, uint32_t count, uint32_t leaf_size,
+                                         const CostNode *cost) {
+	if (r & kLeafBit)
+		return false;
+	if (count > leaf_size)
+		return true;
+	return cost ? (__ldg(&cost[r].bits) >> 31) == 0u : false;
+}
+
 // Level-0 frontier: the root of every scene becomes 8-wide node s; the node counter
 // starts after the roots.
 __global__ void k_collapse_roots(const uint32_t *tri_off, const uint32_t *int_off,
@@ -427,7 +565,8 @@ __global__ void __launch_bounds__(128)
                const uint32_t *__restrict__ left, const uint32_t *__restrict__ right,
                const uint32_t *__restrict__ rfirst, const uint32_t *__restrict__ rlast,
                const float4 *__restrict__ ibox, const float4 *__restrict__ lbox,
-               uint32_t leaf_size, uint32_t n_tris, uint32_t *err) {
+               uint32_t leaf_size, uint32_t n_tris, const CostNode *__restrict__ cost,
+               uint32_t *err) {
 	const uint32_t n_in = *in_count;
 	const uint32_t lane = threadIdx.x & 31u;
 	for (uint32_t w0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n_in;
@@ -447,7 +586,41 @@ __global__ void __launch_bounds__(128)
 			A[c] = -1.0f;
 		}
 		int nc = 0;
-		if (live && !empty_scene) {
+		if (live && !empty_scene && cost && !(it.ref & kLeafBit)) {
+			// Share out the 8 slots as the cost pass decided: a pending (subtree, slots)
+			// entry is opened when splitting it is cheaper than keeping it whole.  The
+			// shares of the pending entries add up to 8, so there are at most 8.
+			uint32_t py[8], pi[8];
+			const uint32_t a0 = split_of(cost[it.ref].bits, 8u);
+			py[0] = right[it.ref];
+			pi[0] = 8u - a0;
+			py[1] = left[it.ref];
+			pi[1] = a0;
+			int top = 2;
+			while (top > 0) {
+				--top;
+				const uint32_t y = py[top], i = pi[top];
+				bool open = false;
+				uint32_t a = 1;
+				if (!(y & kLeafBit) && i > 1u) {
+					open = cost[y].cd[i - 2u] < cost[y].c1;
+					a = split_of(cost[y].bits, i);
+				}
+				if (open && top <= 6) {
+					py[top] = right[y];
+					pi[top] = i - a;
+					py[top + 1] = left[y];
+					pi[top + 1] = a;
+					top += 2;
+				} else {
+#pragma unroll
+					for (int c = 0; c < 8; ++c)
+						if (c == nc)
+							C[c] = y;
+					nc = min(nc + 1, 8);
+				}
+			}
+		} else if (live && !empty_scene) {
 			C[0] = it.ref;
 			A[0] = open_area(it.ref, ibox);
 			nc = 1;
@@ -493,7 +666,7 @@ __global__ void __launch_bounds__(128)
 			if (c < nc) {
 				F[c] = bfirst(C[c], rfirst);
 				N[c] = bcount(C[c], rfirst, rlast);
-				if (!(C[c] & kLeafBit) && N[c] > leaf_size)
+				if (is_inner(C[c], N[c], leaf_size, cost))
 					++n_inner;
 				else
 					n_leaf_tris += N[c];
@@ -579,7 +752,7 @@ __global__ void __launch_bounds__(128)
 					lo = ibox[2 * r];
 					hi = ibox[2 * r + 1];
 				}
-				if (!(r & kLeafBit) && N[c] > leaf_size) {
+				if (is_inner(r, N[c], leaf_size, cost)) {
 					ref = base + k_inner;
 					out[obase + k_inner] = Item{r, ref};
 					++k_inner;
@@ -779,7 +952,7 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 
 int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg, bool sah) {
+               std::string &msg, bool sah, bool collapse_cost) {
 	if (leaf_size < 1 || leaf_size > kMaxLeaf) {
 		msg = "leaf_size must be in [1, 8]";
 		return PRT_ERR_ARG;
@@ -805,6 +978,7 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	plan.compressed = compressed;
 	plan.multi = S > 1;
 	plan.sah = sah;
+	plan.collapse_cost = collapse_cost;
 	plan.toff.resize(S + 1);
 	plan.ioff.resize(S + 1);
 	for (uint32_t s = 0; s <= S; ++s)
@@ -868,6 +1042,8 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 		BUILD_TRY(ws.sah.reserve(sah_scratch_bytes(n, S)));
 		BUILD_TRY(ws.roots.reserve(4ull * S));
 	}
+	if (collapse_cost)
+		BUILD_TRY(ws.cost.reserve(sizeof(CostNode) * ni));
 	BUILD_TRY(sc.tri4.reserve(48 * nn));
 	BUILD_TRY(sc.inv.reserve(4 * nn));
 	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)plan.node_cap));
@@ -970,6 +1146,18 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 		if (rc != PRT_OK)
 			return rc;
 	}
+	// Binary node ids run up to n_int (LBVH) or n_int + S (SAH: scene s's root is s).
+	const uint32_t n_ids = n_int + (plan.sah ? S : 0u);
+	const CostNode *cost = nullptr;
+	if (plan.collapse_cost && n_int) {
+		BUILD_TRY(cudaMemsetAsync(ws.flags.p, 0, 4ull * n_ids, st));
+		k_collapse_cost<<<blocks_for(n, 256), 256, 0, st>>>(
+		    n, n_ids, ws.parent_leaf.as<uint32_t>(), ws.parent_int.as<uint32_t>(),
+		    ws.left.as<uint32_t>(), ws.right.as<uint32_t>(), ws.rfirst.as<uint32_t>(),
+		    ws.rlast.as<uint32_t>(), ws.ibox.as<float4>(), ws.lbox.as<float4>(),
+		    ws.flags.as<uint32_t>(), ws.cost.as<CostNode>(), (uint32_t)plan.leaf_size, d_err);
+		cost = ws.cost.as<CostNode>();
+	}
 
 	uint32_t *ctr = ws.counters.as<uint32_t>();
 	BUILD_TRY(cudaMemsetAsync(ctr, 0, 4 * kCtrWords, st));
@@ -984,7 +1172,7 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 			    ctr + kCtrNodes, plan.node_cap, ctr + kCtrTris, sc.nodes.as<Node8>(),
 			    ws.perm.as<uint32_t>(), ws.left.as<uint32_t>(), ws.right.as<uint32_t>(),
 			    ws.rfirst.as<uint32_t>(), ws.rlast.as<uint32_t>(), ws.ibox.as<float4>(),
-			    ws.lbox.as<float4>(), (uint32_t)plan.leaf_size, n, d_err);
+			    ws.lbox.as<float4>(), (uint32_t)plan.leaf_size, n, cost, d_err);
 		if (!host_checks)
 			break;
 		BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ctr, 4 * kCtrWords, cudaMemcpyDeviceToHost, st));
@@ -1043,18 +1231,21 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
-                 uint32_t *d_err, std::string &msg, bool sah) {
+                 uint32_t *d_err, std::string &msg, bool sah, bool collapse_cost) {
 	BuildPlan plan;
-	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg, sah);
+	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg, sah,
+	                    collapse_cost);
 	if (rc != PRT_OK)
 		return rc;
 	return build_enqueue(d_tris, plan, sc, ws, st, d_err, true, msg);
 }
 
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
-                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg, bool sah) {
+                BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg, bool sah,
+                bool collapse_cost) {
 	const uint64_t off[2] = {0, n};
-	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg, sah);
+	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg, sah,
+	                    collapse_cost);
 }
 
 } // namespace prt

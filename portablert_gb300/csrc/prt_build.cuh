@@ -86,6 +86,7 @@ struct BuildScratch {
 	DevBuf bounds;                    // centroid bounds, 6 ordered words per scene
 	DevBuf sah;                       // SAH build: records, task lists, bins, counters
 	DevBuf roots;                     // SAH build: root binary node of each scene
+	DevBuf cost;                      // cost-optimal collapse: 36 B per binary node
 	uint32_t *h_counters = nullptr;   // pinned mirror of `counters`
 	void release();
 };
@@ -96,16 +97,19 @@ struct BuildPlan {
 	int leaf_size = 1, scene_digits = 0;
 	bool compressed = false, multi = false;
 	bool sah = false;                 // binned-SAH binary trees instead of LBVH
+	bool collapse_cost = true;        // cost-optimal 8-wide collapse (else largest area first)
 	std::vector<uint32_t> toff, ioff; // triangle and binary-node offsets per scene
 };
 
 // Validates the offsets, reserves every buffer of the build and queues the uploads of
 // the offset tables on `st`.  Nothing after it allocates.
 // sah: build the binary trees top-down with binned SAH (prt_sah.cu) instead of the
-// Morton/Karras hierarchy; needs host checks.
+// Morton/Karras hierarchy; needs host checks.  collapse_cost: collapse to 8-wide nodes
+// by the least expected cost (a bottom-up pass over the binary tree) instead of opening
+// the largest child first.
 int build_plan(const uint64_t *tri_off, uint32_t n_scenes, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg, bool sah = false);
+               std::string &msg, bool sah = false, bool collapse_cost = true);
 
 // Queues the build kernels.  host_checks: read the level counters every few levels and
 // finish with build_finish (synchronises).  Without host checks nothing synchronises:
@@ -124,11 +128,12 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 // Synchronises `st` (a few times, never per tree level).  Returns PRT_* status.
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
-                 uint32_t *d_err, std::string &msg, bool sah = false);
+                 uint32_t *d_err, std::string &msg, bool sah = false,
+                 bool collapse_cost = true);
 
 // One scene: build_scenes with tri_off = {0, n}.
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
                 BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg,
-                bool sah = false);
+                bool sah = false, bool collapse_cost = true);
 
 } // namespace prt

@@ -86,13 +86,13 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	std::string msg;
 	bool sah = ctx->build_sah;
 	int rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
-	                          ctx->ws, ctx->stream, ctx->d_err(), msg, sah);
+	                          ctx->ws, ctx->stream, ctx->d_err(), msg, sah, ctx->collapse_cost);
 	if (sah && rc == PRT_ERR_LIMIT) {
 		// An SAH tree deeper than the collapse's 32 levels: the LBVH's depth is bounded.
 		sah = false;
 		msg.clear();
 		rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
-		                      ctx->ws, ctx->stream, ctx->d_err(), msg, false);
+		                      ctx->ws, ctx->stream, ctx->d_err(), msg, false, ctx->collapse_cost);
 	}
 	ctx->last_build_sah = sah;
 	cudaEventRecord(e1, ctx->stream);
@@ -504,6 +504,8 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		ctx->build_compressed = v != 0;
 	} else if (k == "build_sah") {
 		ctx->build_sah = v != 0;
+	} else if (k == "collapse_cost") {
+		ctx->collapse_cost = v != 0;
 	} else {
 		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
 	}

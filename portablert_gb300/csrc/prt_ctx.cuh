@@ -74,6 +74,7 @@ struct prt_b200_ctx {
 	bool count = false;
 	bool build_compressed = true;
 	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)
+	bool collapse_cost = true;   // cost-optimal 8-wide collapse ("collapse_cost")
 	bool last_build_sah = false; // the scene's tree is an SAH tree
 	double build_ms = 0.0;
 	unsigned long long visits[2] = {0, 0};

@@ -82,6 +82,7 @@ struct SahArgs {
 	float4 *lbox;           // out: leaf boxes by position
 	uint32_t *left, *right, *rfirst, *rlast;
 	float4 *ibox;
+	uint32_t *parent_int, *parent_leaf; // for the bottom-up cost pass of the collapse
 	uint32_t node_cap, max_large, max_mid, max_small;
 	uint32_t n;             // triangles (records per buffer)
 	uint32_t *err;
@@ -371,6 +372,14 @@ __device__ void emit_split(const SahArgs &A, const SahTask &t, const Split &s, i
 	A.right[t.node] = rr;
 	A.rfirst[t.node] = t.begin;
 	A.rlast[t.node] = t.begin + t.count - 1u;
+	if (nl > 1)
+		A.parent_int[ids[0]] = t.node;
+	else
+		A.parent_leaf[t.begin] = t.node;
+	if (nr > 1)
+		A.parent_int[ids[1]] = t.node;
+	else
+		A.parent_leaf[t.begin + nl] = t.node;
 	// Children's areas: known now for a binned split (leaves keep -1); after halves each
 	// child writes its own when it is split.
 	write_node_box(A, t.node, s.node, (binned && nl > 1) ? box_area(s.left) : -1.0f,
@@ -926,6 +935,14 @@ __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 					A.right[node] = rr;
 					A.rfirst[node] = st.begin + f;
 					A.rlast[node] = st.begin + f + cnt - 1;
+					if (nl > 1)
+						A.parent_int[ids[0]] = node;
+					else
+						A.parent_leaf[st.begin + f] = node;
+					if (nr > 1)
+						A.parent_int[ids[1]] = node;
+					else
+						A.parent_leaf[st.begin + f + nl] = node;
 					write_node_box(A, node, nb, nl > 1 ? box_area(lb) : -1.0f,
 					               nr > 1 ? box_area(rb) : -1.0f);
 					if (root)
@@ -1032,6 +1049,8 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 	A.rfirst = ws.rfirst.as<uint32_t>();
 	A.rlast = ws.rlast.as<uint32_t>();
 	A.ibox = ws.ibox.as<float4>();
+	A.parent_int = ws.parent_int.as<uint32_t>();
+	A.parent_leaf = ws.parent_leaf.as<uint32_t>();
 	A.node_cap = plan.n_int + S;
 	A.max_large = (uint32_t)L.max_large;
 	A.max_mid = (uint32_t)L.max_mid;
@@ -1041,6 +1060,9 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 
 	uint32_t *gb = ws.bounds.as<uint32_t>();
 	cudaMemsetAsync(A.ctr, 0, 4 * kCtrWordsSah, st);
+	// No parent: the roots and the triangles of one-triangle scenes keep these.
+	cudaMemsetAsync(A.parent_int, 0xFF, 4ull * A.node_cap, st);
+	cudaMemsetAsync(A.parent_leaf, 0xFF, 4ull * n, st);
 	k_sah_bounds_init<<<blocks_for(6ull * S, 256), 256, 0, st>>>(gb, S);
 	if (n)
 		k_sah_records<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, scene_of, A.rec[0], gb);
