@@ -733,7 +733,22 @@ def run_gpu(args, world, rank):
         e2e_step()
         e2e_t.append(time.perf_counter() - t0)
     e2e = n / float(np.median(e2e_t)) / 1e6
+    in_place = b.stat("in_place") == 1.0
     assert rec["valid"].sum() > 0
+
+    def timed(f, k):
+        f()
+        ts = []
+        for _ in range(k):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return n / float(np.median(ts)) / 1e6
+
+    # The same call through the chunked copy pipeline (option host_direct = 0).
+    b.set_option("host_direct", 0)
+    e2e_copy = timed(e2e_step, max(1, min(args.steps, 5)))
+    b.set_option("host_direct", 1)
     # The same call on pageable memory (what portableRT's std::vector API passes).
     pg_out = np.zeros(n * lay.size, np.uint8)
 
@@ -743,13 +758,11 @@ def run_gpu(args, world, rank):
         if rc:
             raise RuntimeError(L.prt_b200_last_error(ctx))
 
-    e2e_pageable_step()
-    pg_t = []
-    for _ in range(max(1, min(args.steps, 5))):
-        t0 = time.perf_counter()
-        e2e_pageable_step()
-        pg_t.append(time.perf_counter() - t0)
-    e2e_pageable = n / float(np.median(pg_t)) / 1e6
+    e2e_pageable = timed(e2e_pageable_step, max(1, min(args.steps, 5)))
+    pg_in_place = b.stat("in_place") == 1.0
+    b.set_option("host_direct", 0)
+    e2e_pageable_copy = timed(e2e_pageable_step, max(1, min(args.steps, 5)))
+    b.set_option("host_direct", 1)
 
     # Roofline of the traversal kernel (algorithmic bytes per launch / launch time).
     b_ray = 24 + lay.size + v_nodes * node_size + v_tris * 48
@@ -783,7 +796,13 @@ def run_gpu(args, world, rank):
            "data": "synthetic", "config": workload_config(len(tris), len(prim), n),
            "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
                    "d2h_bytes_per_step": lay.size * n, "host_memory": "pinned",
-                   "pageable_value": e2e_pageable},
+                   "path": ("in place: the traversal reads each ray from and writes each "
+                            "record to the caller's host buffers over the host link")
+                   if in_place else "chunked copy pipeline",
+                   "copy_pipeline_value": e2e_copy,
+                   "pageable_value": e2e_pageable,
+                   "pageable_path": "in place" if pg_in_place else "chunked copy pipeline",
+                   "pageable_copy_pipeline_value": e2e_pageable_copy},
            # per step: the regular pass and the deferred pass of k_trace8
            "gpu_launches": 2 * args.steps,
            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -190,6 +190,11 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "collapse_cost" 1 = the binary tree is collapsed to 8-wide nodes by the least
  *                  expected cost per ray (a bottom-up pass chooses which subtrees become
  *                  nodes and leaves), 0 = by opening the largest child first (default 1)
+ *   "host_direct"  1 = a host-buffer nearest_hits whose buffers the device can reach in
+ *                  place (pinned memory; pageable memory where the device reads it
+ *                  through the host's page tables, as on Grace) traverses them there:
+ *                  rays read and records written over the host link, no staging copies
+ *                  (default 1); 0 = always the chunked copy pipeline below
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
@@ -199,7 +204,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree
- *   is an SAH tree), "node_bytes", "tri_bytes",
+ *   is an SAH tree), "in_place" (1 = the last host-buffer nearest_hits traversed the
+ *   caller's buffers in place), "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);

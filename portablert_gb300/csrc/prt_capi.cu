@@ -185,6 +185,9 @@ int prt_b200_create(int device, prt_b200_ctx **out) {
 		e = cudaMallocHost(&ctx->h_err, 16);
 	if (e == cudaSuccess)
 		e = cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+	if (e == cudaSuccess)
+		e = cudaDeviceGetAttribute(&ctx->pageable_access, cudaDevAttrPageableMemoryAccess,
+		                           device);
 	for (cudaStream_t *s : {&ctx->s_in, &ctx->s_out, &ctx->s_k2})
 		if (e == cudaSuccess)
 			e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
@@ -369,6 +372,33 @@ int prt_b200_sync(prt_b200_ctx *ctx) {
 	return check_device_errors(ctx);
 }
 
+namespace {
+
+// The address under which the device reaches host buffer p in place, or null: pinned
+// (page-locked, registered) memory through its device alias, pageable memory when the
+// device reads it through the host's page tables (Grace: NVLink-C2C with address
+// translation), managed and device memory as they are.
+void *device_alias(const prt_b200_ctx *ctx, const void *p) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	switch (a.type) {
+	case cudaMemoryTypeHost:
+		return a.devicePointer;
+	case cudaMemoryTypeDevice:
+	case cudaMemoryTypeManaged:
+		return a.device == ctx->device ? const_cast<void *>(p) : nullptr;
+	case cudaMemoryTypeUnregistered:
+		return ctx->pageable_access ? const_cast<void *>(p) : nullptr;
+	default:
+		return nullptr;
+	}
+}
+
+} // namespace
+
 int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uint32_t field_mask,
                           uint32_t rec_size, const uint8_t offs[8], void *out_host) {
 	if (!ctx)
@@ -386,8 +416,6 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 	if (n == 0)
 		return PRT_OK;
 	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-	CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
-	CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
 	prt::OutLayout lay;
 	lay.mask = field_mask;
 	lay.rec_size = rec_size;
@@ -396,6 +424,28 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 	cfg.format = ctx->node_format;
 	cfg.block = ctx->block;
 	cfg.count = ctx->count;
+	// In place when the device can reach both buffers: the traversal reads each ray from
+	// host memory once and writes each record there once, over the host link, with no
+	// staging buffers and nothing to overlap.
+	if (ctx->host_direct) {
+		const void *d_in = device_alias(ctx, rays6);
+		void *d_out = d_in ? device_alias(ctx, out_host) : nullptr;
+		ctx->last_in_place = d_in && d_out;
+		if (d_in && d_out) {
+			CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, static_cast<const float *>(d_in),
+			                                       n, lay, d_out, cfg, ctx->d_work(),
+			                                       ctx->d_visits(), ctx->d_err(), ctx->stream,
+			                                       ctx->sms));
+			CAPI_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+			if (ctx->count)
+				CAPI_TRY(ctx,
+				         cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
+			return check_device_errors(ctx);
+		}
+	}
+	ctx->last_in_place = false;
+	CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
+	CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
 	// Chunks: pipe_chunks of them (fewer when a chunk would hold under pipe_min_rays), one
 	// when the visit counters are on (each launch would reset them).  With pipe_ramp the
 	// sizes ramp up and down (weights 1, 2, 4, 8, ..., 8, 4, 2, 1), so the copy-in of the
@@ -506,6 +556,8 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		ctx->build_sah = v != 0;
 	} else if (k == "collapse_cost") {
 		ctx->collapse_cost = v != 0;
+	} else if (k == "host_direct") {
+		ctx->host_direct = v != 0;
 	} else {
 		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
 	}
@@ -528,6 +580,8 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
 		*value = ctx->build_ms;
 	else if (k == "build_sah")
 		*value = ctx->last_build_sah ? 1.0 : 0.0;
+	else if (k == "in_place")
+		*value = ctx->last_in_place ? 1.0 : 0.0;
 	else if (k == "node_bytes")
 		*value = (double)s.n_nodes *
 		         (ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8) : sizeof(prt::Node8));

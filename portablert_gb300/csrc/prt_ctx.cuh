@@ -38,6 +38,7 @@ class ErrorText {
 struct prt_b200_ctx {
 	int device = 0;
 	int sms = 0;
+	int pageable_access = 0; // the device reads pageable host memory in place
 	cudaStream_t stream = nullptr;
 	std::mutex mu;
 	prt::ErrorText err;
@@ -75,6 +76,8 @@ struct prt_b200_ctx {
 	bool build_compressed = true;
 	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)
 	bool collapse_cost = true;   // cost-optimal 8-wide collapse ("collapse_cost")
+	bool host_direct = true;     // host-buffer calls traverse in place when they can
+	bool last_in_place = false;  // the last host-buffer call did
 	bool last_build_sah = false; // the scene's tree is an SAH tree
 	double build_ms = 0.0;
 	unsigned long long visits[2] = {0, 0};

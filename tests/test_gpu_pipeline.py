@@ -1,7 +1,9 @@
-"""The host-buffer call (prt_b200_nearest_hits) splits large batches into chunks whose
-copies and traversals overlap on several streams.  Its records must be byte-identical
-to one device-buffer launch over the same rays, for pageable and pinned host memory,
-chunk counts from one to eight, ragged last chunks and every node format."""
+"""The host-buffer call (prt_b200_nearest_hits) either traverses the caller's buffers in
+place (option host_direct, when the device can reach them: pinned memory, and pageable
+memory where the device reads the host's page tables) or splits large batches into
+chunks whose copies and traversals overlap on several streams.  Its records must be
+byte-identical to one device-buffer launch over the same rays, for pageable and pinned
+host memory, chunk counts from one to eight, ragged last chunks and every node format."""
 import numpy as np
 import pytest
 
@@ -32,6 +34,7 @@ def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt, chunks, 
     gpu_backend.set_option("node_format", fmt)
     gpu_backend.set_option("pipe_chunks", chunks)
     gpu_backend.set_option("pipe_ramp", ramp)
+    gpu_backend.set_option("host_direct", 0)  # the copy pipeline
     try:
         gpu_backend.set_tris(tris)
         for tags in [hitreg.TAGS, ("t", "primitive_id", "valid"), ("valid",)]:
@@ -42,6 +45,45 @@ def test_chunked_host_call_equals_device_call(gpu_backend, n_rays, fmt, chunks, 
         gpu_backend.set_option("node_format", 0)
         gpu_backend.set_option("pipe_chunks", 8)
         gpu_backend.set_option("pipe_ramp", 1)
+        gpu_backend.set_option("host_direct", 1)
+
+
+@pytest.mark.parametrize("rays_mem,out_mem", [("pinned", "pinned"), ("pageable", "pageable"),
+                                              ("pinned", "pageable"), ("pageable", "pinned")])
+@pytest.mark.parametrize("direct", [1, 0])
+def test_host_call_in_place_and_copied(gpu_backend, rays_mem, out_mem, direct):
+    """Both forms of the host-buffer call, on every mix of pinned and pageable buffers,
+    the output starting at an odd address (byte stores) or aligned."""
+    import ctypes
+
+    import torch
+
+    tris = workloads.soup_tris(47, 8_000)
+    rays = workloads.soup_rays(48, 300_001)
+    gpu_backend.set_tris(tris)
+    for tags in [hitreg.TAGS, ("valid",)]:
+        lay = hitreg.layout(tags)
+        want = _device_records(torch, gpu_backend, rays, tags)
+        r = torch.from_numpy(rays).pin_memory() if rays_mem == "pinned" else rays
+        r_ptr = r.data_ptr() if rays_mem == "pinned" else rays.ctypes.data
+        for shift in (0, 1):
+            size = len(rays) * lay.size + 1
+            if out_mem == "pinned":
+                o = torch.zeros(size, dtype=torch.uint8).pin_memory()
+                o_ptr = o.data_ptr() + shift
+            else:
+                o = np.zeros(size, np.uint8)
+                o_ptr = o.ctypes.data + shift
+            L = gpu_backend._L
+            try:
+                gpu_backend.set_option("host_direct", direct)
+                gpu_backend._check(L.prt_b200_nearest_hits(
+                    gpu_backend.ctx, ctypes.c_void_p(r_ptr), len(rays), lay.mask, lay.size,
+                    lay.offsets8(), ctypes.c_void_p(o_ptr)))
+            finally:
+                gpu_backend.set_option("host_direct", 1)
+            got = (o.numpy() if out_mem == "pinned" else o)[shift:shift + len(rays) * lay.size]
+            assert np.array_equal(got, want), (tags, shift)
 
 
 def test_chunked_host_call_pinned_buffers(gpu_backend):
@@ -56,9 +98,13 @@ def test_chunked_host_call_pinned_buffers(gpu_backend):
     h_r = torch.from_numpy(rays).pin_memory()
     h_o = torch.zeros(len(rays) * lay.size, dtype=torch.uint8).pin_memory()
     L = gpu_backend._L
-    gpu_backend._check(L.prt_b200_nearest_hits(gpu_backend.ctx, ctypes.c_void_p(h_r.data_ptr()),
-                                               len(rays), lay.mask, lay.size, lay.offsets8(),
-                                               ctypes.c_void_p(h_o.data_ptr())))
+    gpu_backend.set_option("host_direct", 0)  # the copy pipeline
+    try:
+        gpu_backend._check(L.prt_b200_nearest_hits(
+            gpu_backend.ctx, ctypes.c_void_p(h_r.data_ptr()), len(rays), lay.mask, lay.size,
+            lay.offsets8(), ctypes.c_void_p(h_o.data_ptr())))
+    finally:
+        gpu_backend.set_option("host_direct", 1)
     want = _device_records(torch, gpu_backend, rays, hitreg.TAGS)
     assert np.array_equal(h_o.numpy(), want)
 
