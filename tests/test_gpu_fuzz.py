@@ -3,7 +3,8 @@
 The GPU's answer is, by construction, the exhaustive one: the smallest t over triangles
 that Moller-Trumbore accepts and whose own box passes the reference slab test, ties to
 the smaller primitive id (orc_brute_force).  So every field must match bit for bit, for
-every ray, whatever the tree -- across leaf sizes and node formats.  The scenes mix
+every ray, whatever the tree -- across both builders (binned SAH, LBVH), both collapses
+(least expected cost, largest child first), leaf sizes and node formats.  The scenes mix
 integer-grid vertices (coplanar and axis-aligned faces, shared edges), collinear and
 repeated-vertex triangles and scales from 1e-20 to 1e20; the rays include zero
 direction components, origins on grid planes and tiny or huge direction lengths."""
@@ -75,8 +76,10 @@ def test_fuzz_against_exhaustive_search(gpu_backend, oracle_lib, seed):
     rays = _rays(rng, 3000, scale)
     want = oracle_lib.brute_force(tris, rays)
     try:
-        for sah in (1, 0):  # binned-SAH and LBVH builds
+        # binned-SAH and LBVH builds, collapsed by least cost or largest child first
+        for sah, cc in ((1, 1), (0, 1), (0, 0), (1, 0)):
             gpu_backend.set_option("build_sah", sah)
+            gpu_backend.set_option("collapse_cost", cc)
             for leaf in (1, 4, 8):
                 gpu_backend.set_option("leaf_size", leaf)
                 gpu_backend.set_tris(tris)
@@ -86,5 +89,6 @@ def test_fuzz_against_exhaustive_search(gpu_backend, oracle_lib, seed):
                     _check(got, want)
     finally:
         gpu_backend.set_option("build_sah", 1)
+        gpu_backend.set_option("collapse_cost", 1)
         gpu_backend.set_option("leaf_size", 1)
         gpu_backend.set_option("node_format", 0)
