@@ -231,125 +231,125 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
                                             uint32_t &n_tests) {
 	const float4 *__restrict__ tri4 = sd.tri4;
 	const void *__restrict__ nodes = sd.nodes;
-		uint32_t top = 0;  // items in the pool (warp-uniform)
-		uint32_t q = 0;    // queued triangles (warp-uniform)
-		uint32_t next = 0; // next slot whose root is not yet in the pool
-		uint32_t steps = 0;
-		for (;;) {
-			// Admit new rays while fewer than K items are pending.
-			if (top < (uint32_t)kItems && next < nb) {
-				const uint32_t add = min((uint32_t)kItems - top, nb - next);
-				if ((uint32_t)lane < add)
-					pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
-				top += add;
-				next += add;
-				__syncwarp();
-			}
-			if (top == 0u)
-				break;
-			if (++steps > step_limit) {
-				if (lane == 0)
-					atomicOr(a.err, kErrStack);
-				break;
-			}
-			const uint32_t take = min(top, (uint32_t)kItems);
-			top -= take;
-			const bool work = (uint32_t)g < take;
-			const uint32_t item = work ? pool[top + g] : 0u;
-			__syncwarp(); // the pops above are read before the pushes below overwrite them
-			const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
-			RayC r;
+	uint32_t top = 0;  // items in the pool (warp-uniform)
+	uint32_t q = 0;    // queued triangles (warp-uniform)
+	uint32_t next = 0; // next slot whose root is not yet in the pool
+	uint32_t steps = 0;
+	for (;;) {
+		// Admit new rays while fewer than K items are pending.
+		if (top < (uint32_t)kItems && next < nb) {
+			const uint32_t add = min((uint32_t)kItems - top, nb - next);
+			if ((uint32_t)lane < add)
+				pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
+			top += add;
+			next += add;
+			__syncwarp();
+		}
+		if (top == 0u)
+			break;
+		if (++steps > step_limit) {
+			if (lane == 0)
+				atomicOr(a.err, kErrStack);
+			break;
+		}
+		const uint32_t take = min(top, (uint32_t)kItems);
+		top -= take;
+		const bool work = (uint32_t)g < take;
+		const uint32_t item = work ? pool[top + g] : 0u;
+		__syncwarp(); // the pops above are read before the pushes below overwrite them
+		const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
+		RayC r;
+		if (work)
+			r = slot_ray(S, slot);
+		if (COUNT && work && s == 0)
+			++n_visits;
+
+		bool hit[kChildPerLane], inner[kChildPerLane];
+		uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
+#pragma unroll
+		for (int j = 0; j < kChildPerLane; ++j) {
+			hit[j] = false;
+			inner[j] = false;
+			child[j] = 0;
+			leaf_n[j] = 0;
 			if (work)
-				r = slot_ray(S, slot);
-			if (COUNT && work && s == 0)
-				++n_visits;
-
-			bool hit[kChildPerLane], inner[kChildPerLane];
-			uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
-#pragma unroll
-			for (int j = 0; j < kChildPerLane; ++j) {
-				hit[j] = false;
-				inner[j] = false;
-				child[j] = 0;
-				leaf_n[j] = 0;
-				if (work)
-					test_child<FMT, REGULAR>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
-					                child[j], leaf_n[j]);
-			}
-
-			// Push the hit inner children as new items (lane order, then child order).
-			uint32_t n_push = 0, before = 0;
-			bool push[kChildPerLane];
-#pragma unroll
-			for (int j = 0; j < kChildPerLane; ++j) {
-				push[j] = hit[j] && inner[j];
-				const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
-				n_push += __popc(b);
-				before += __popc(b & lt);
-			}
-			if (top + n_push > a.pool_cap) {
-				if (lane == 0)
-					atomicOr(a.err, kErrStack);
-			} else {
-				uint32_t pos = top + before;
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j)
-					if (push[j])
-						pool[pos++] = (slot << kIndexBits) | child[j];
-				top += n_push;
-			}
-
-			// Queue the triangles of the hit leaf children.
-			uint32_t cnt[kChildPerLane], all_cnt = 0;
-			bool single = true;
-#pragma unroll
-			for (int j = 0; j < kChildPerLane; ++j) {
-				cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
-				all_cnt += cnt[j];
-				single = single && cnt[j] <= 1u;
-			}
-			if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
-				uint32_t n_add = 0, pre = 0;
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j) {
-					const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
-					n_add += __popc(b);
-					pre += __popc(b & lt);
-				}
-				uint32_t pos = q + pre;
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j)
-					if (cnt[j])
-						queue[pos++] = (slot << kIndexBits) | child[j];
-				q += n_add;
-			} else {
-				uint32_t incl = all_cnt;
-#pragma unroll
-				for (int o = 1; o < 32; o <<= 1) {
-					const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-					if (lane >= o)
-						incl += y;
-				}
-				uint32_t pos = q + incl - all_cnt;
-#pragma unroll
-				for (int j = 0; j < kChildPerLane; ++j)
-					for (uint32_t k = 0; k < cnt[j]; ++k)
-						queue[pos++] = (slot << kIndexBits) | (child[j] + k);
-				q += __shfl_sync(0xFFFFFFFFu, incl, 31);
-			}
-			__syncwarp();
-			while (q >= 32u) {
-				q -= 32u;
-				test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
-				__syncwarp();
-			}
+				test_child<FMT, REGULAR>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
+				                child[j], leaf_n[j]);
 		}
-		while (q > 0u) {
-			const uint32_t n = min(q, 32u);
-			q -= n;
-			test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
+
+		// Push the hit inner children as new items (lane order, then child order).
+		uint32_t n_push = 0, before = 0;
+		bool push[kChildPerLane];
+#pragma unroll
+		for (int j = 0; j < kChildPerLane; ++j) {
+			push[j] = hit[j] && inner[j];
+			const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
+			n_push += __popc(b);
+			before += __popc(b & lt);
+		}
+		if (top + n_push > a.pool_cap) {
+			if (lane == 0)
+				atomicOr(a.err, kErrStack);
+		} else {
+			uint32_t pos = top + before;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j)
+				if (push[j])
+					pool[pos++] = (slot << kIndexBits) | child[j];
+			top += n_push;
+		}
+
+		// Queue the triangles of the hit leaf children.
+		uint32_t cnt[kChildPerLane], all_cnt = 0;
+		bool single = true;
+#pragma unroll
+		for (int j = 0; j < kChildPerLane; ++j) {
+			cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
+			all_cnt += cnt[j];
+			single = single && cnt[j] <= 1u;
+		}
+		if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
+			uint32_t n_add = 0, pre = 0;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j) {
+				const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
+				n_add += __popc(b);
+				pre += __popc(b & lt);
+			}
+			uint32_t pos = q + pre;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j)
+				if (cnt[j])
+					queue[pos++] = (slot << kIndexBits) | child[j];
+			q += n_add;
+		} else {
+			uint32_t incl = all_cnt;
+#pragma unroll
+			for (int o = 1; o < 32; o <<= 1) {
+				const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+				if (lane >= o)
+					incl += y;
+			}
+			uint32_t pos = q + incl - all_cnt;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j)
+				for (uint32_t k = 0; k < cnt[j]; ++k)
+					queue[pos++] = (slot << kIndexBits) | (child[j] + k);
+			q += __shfl_sync(0xFFFFFFFFu, incl, 31);
+		}
+		__syncwarp();
+		while (q >= 32u) {
+			q -= 32u;
+			test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
 			__syncwarp();
 		}
+	}
+	while (q > 0u) {
+		const uint32_t n = min(q, 32u);
+		q -= n;
+		test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
+		__syncwarp();
+	}
 }
 
 // LEAF1: every leaf holds one triangle (leaf size 1), so a hit leaf queues exactly one.
