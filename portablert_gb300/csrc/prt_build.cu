@@ -727,8 +727,8 @@ __global__ void __launch_bounds__(128)
 		if (empty_scene) { // a node without children
 			for (int c = 0; c < 8; ++c) {
 				Child8 ch;
-				ch.lo_x = ch.lo_y = ch.lo_z = 0.0f;
-				ch.hi_x = ch.hi_y = ch.hi_z = 0.0f;
+				ch.lo_x = ch.lo_y = ch.lo_z = __int_as_float(0x7FC00000);
+				ch.hi_x = ch.hi_y = ch.hi_z = __int_as_float(0x7FC00000);
 				ch.ref = kNone;
 				ch.pad = 0u;
 				nd->c[c] = ch;
@@ -740,7 +740,10 @@ __global__ void __launch_bounds__(128)
 		uint32_t k_inner = 0;
 #pragma unroll
 		for (int c = 0; c < 8; ++c) {
-			float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+			// An unused slot gets a NaN box: no slab test passes it.
+			float4 lo = make_float4(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000),
+			                        __int_as_float(0x7FC00000), 0.f),
+			       hi = lo;
 			uint32_t ref = kNone;
 			if (c < nc) {
 				const uint32_t r = C[c];

@@ -79,8 +79,9 @@ struct TravArgs {
 // area of the output records, which is read with 16-byte vector loads.
 struct alignas(16) WarpFixed {
 	unsigned long long key[32]; // best (t, primitive id) per slot
-	float ray[32][9];           // origin, direction, reciprocal per slot
-	int kind[32];
+	float4 ro[32];              // origin and kind (int bits) per slot
+	float4 rf[32];              // reciprocals per slot
+	float4 rd[32];              // direction per slot
 	SegDesc seg;                // the run the current 32 rays belong to
 	uint32_t batches;           // batches this warp has taken (kept here, not in a register)
 	uint32_t pad_[3];
@@ -125,16 +126,18 @@ __device__ __forceinline__ float byte_as_float(uint32_t w, int k) {
 
 __device__ __forceinline__ RayC slot_ray(const WarpFixed &S, uint32_t s) {
 	RayC r;
-	r.ox = S.ray[s][0];
-	r.oy = S.ray[s][1];
-	r.oz = S.ray[s][2];
-	r.dx = S.ray[s][3];
-	r.dy = S.ray[s][4];
-	r.dz = S.ray[s][5];
-	r.fx = S.ray[s][6];
-	r.fy = S.ray[s][7];
-	r.fz = S.ray[s][8];
-	r.kind = S.kind[s];
+	// Two 16-byte shared loads for the slab test (the direction is dead there).
+	const float4 o = S.ro[s], f = S.rf[s], d = S.rd[s];
+	r.ox = o.x;
+	r.oy = o.y;
+	r.oz = o.z;
+	r.dx = d.x;
+	r.dy = d.y;
+	r.dz = d.z;
+	r.fx = f.x;
+	r.fy = f.y;
+	r.fz = f.z;
+	r.kind = __float_as_int(o.w);
 	return r;
 }
 
@@ -170,7 +173,9 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 		float4 lo, hi;
 		ld_nc_256(&(static_cast<const Node8 *>(nodes) + node)->c[k], lo, hi);
 		const uint32_t ref = __float_as_uint(lo.w);
-		if (ref != kNone) {
+		// An unused slot has a NaN box, which the plain slab test never passes; the
+		// conservative test would, so only the general pass checks the reference.
+		if (REGULAR || ref != kNone) {
 			inner = !ref_is_leaf(ref);
 			hit = box_test<REGULAR>(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
 			child = inner ? ref : leaf_first(ref);
@@ -211,13 +216,13 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 }
 
 // Resident blocks per SM the register budget is set for, per node format (measured on
-// the 1M-triangle heightfield: FP32 nodes gain 3 % at 9 blocks of 4 warps = 56 registers
-// with a few spilled words; the compressed decode needs 64 registers, 8 blocks).
+// the 1M-triangle heightfield: 9 blocks of 4 warps = 56 registers, with a few spilled
+// words, is fastest for both formats).
 #ifndef PRT_TRAVERSE_MIN_BLOCKS_FP32
 #define PRT_TRAVERSE_MIN_BLOCKS_FP32 9
 #endif
 #ifndef PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED
-#define PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED 8
+#define PRT_TRAVERSE_MIN_BLOCKS_COMPRESSED 9
 #endif
 
 // The traversal of one batch of up to 32 rays (slots 0..nb-1 of S) through scene sd.
@@ -254,13 +259,13 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		}
 		const uint32_t take = min(top, (uint32_t)kItems);
 		top -= take;
+		// Groups without an item this step repeat the first one (same loads, no branch)
+		// and drop what they find.
 		const bool work = (uint32_t)g < take;
-		const uint32_t item = work ? pool[top + g] : 0u;
+		const uint32_t item = pool[top + (work ? g : 0)];
 		__syncwarp(); // the pops above are read before the pushes below overwrite them
 		const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
-		RayC r;
-		if (work)
-			r = slot_ray(S, slot);
+		const RayC r = slot_ray(S, slot);
 		if (COUNT && work && s == 0)
 			++n_visits;
 
@@ -272,9 +277,9 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 			inner[j] = false;
 			child[j] = 0;
 			leaf_n[j] = 0;
-			if (work)
-				test_child<FMT, REGULAR>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
-				                child[j], leaf_n[j]);
+			test_child<FMT, REGULAR>(nodes, r, node, s * kChildPerLane + j, hit[j], inner[j],
+			                         child[j], leaf_n[j]);
+			hit[j] = hit[j] && work;
 		}
 
 		// Push the hit inner children as new items (lane order, then child order).
@@ -304,7 +309,7 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		bool single = true;
 #pragma unroll
 		for (int j = 0; j < kChildPerLane; ++j) {
-			cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
+			cnt[j] = (hit[j] && !inner[j]) ? (LEAF1 ? 1u : leaf_n[j]) : 0u;
 			all_cnt += cnt[j];
 			single = single && cnt[j] <= 1u;
 		}
@@ -436,11 +441,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 				const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
 				r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
 			}
-			float *sr = S.ray[lane];
-			sr[0] = r.ox; sr[1] = r.oy; sr[2] = r.oz;
-			sr[3] = r.dx; sr[4] = r.dy; sr[5] = r.dz;
-			sr[6] = r.fx; sr[7] = r.fy; sr[8] = r.fz;
-			S.kind[lane] = r.kind;
+			S.ro[lane] = make_float4(r.ox, r.oy, r.oz, __int_as_float(r.kind));
+			S.rf[lane] = make_float4(r.fx, r.fy, r.fz, 0.0f);
+			S.rd[lane] = make_float4(r.dx, r.dy, r.dz, 0.0f);
 		}
 		S.key[lane] = kNoHit;
 		__syncwarp();
@@ -448,7 +451,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		if (sd.n_tris) {
 			// Nearly every batch has only rays with finite reciprocals.
 			const bool regular =
-			    __all_sync(0xFFFFFFFFu, (uint32_t)lane >= nb || S.kind[lane] == 0);
+			    __all_sync(0xFFFFFFFFu, (uint32_t)lane >= nb || __float_as_int(S.ro[lane].w) == 0);
 			if (PASS == 1 && !regular) {
 				if (lane == 0)
 					atomicAdd(a.deferred, 1u);
