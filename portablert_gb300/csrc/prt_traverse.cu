@@ -178,7 +178,9 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 		if (REGULAR || ref != kNone) {
 			inner = !ref_is_leaf(ref);
 			hit = box_test<REGULAR>(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-			child = inner ? ref : leaf_first(ref);
+			// A node index, or a leaf's first triangle: both below 2^27, under the
+			// leaf flag and count bits.
+			child = ref & kIndexMask;
 			leaf_n = inner ? 0u : leaf_count(ref);
 		}
 	} else {
