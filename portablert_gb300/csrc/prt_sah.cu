@@ -808,6 +808,25 @@ __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 			lo = src[2 * (size_t)(st.begin + lane)];
 			hi = src[2 * (size_t)(st.begin + lane) + 1];
 		}
+		if (m >= 3) {
+			// Each triangle's rank among the task's on each axis, by (centre, index),
+			// packed 5 bits per axis into the unused w of its box (it moves with the
+			// triangle when lanes are reordered).  A node's own order on an axis is then
+			// one OR over its lanes' rank bits and a population count.
+			uint32_t gr = 0;
+#pragma unroll
+			for (int a = 0; a < 3; ++a) {
+				const uint64_t key = (uint32_t)lane < m
+				                         ? (((uint64_t)f2ord(rec_c(lo, hi, a)) << 32) |
+				                            __float_as_uint(lo.w))
+				                         : ~0ull;
+				uint32_t rank = 0;
+				for (uint32_t j = 0; j < m; ++j)
+					rank += __shfl_sync(0xFFFFFFFFu, key, (int)j) < key;
+				gr |= min(rank, 31u) << (5 * a);
+			}
+			hi.w = __uint_as_float(gr);
+		}
 		if (m >= 2) {
 			uint32_t base = 0;
 			if (lane == 0 && m > 2)
@@ -848,13 +867,10 @@ __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 					uint64_t best = ~0ull;
 					uint32_t rank_best = 0;
 					for (int a = 0; a < 3; ++a) {
-						const uint64_t key =
-						    ((uint64_t)f2ord(rec_c(lo, hi, a)) << 32) | __float_as_uint(lo.w);
-						uint32_t rank = 0;
-						for (int j = f; j < f + cnt; ++j) {
-							const uint64_t kj = __shfl_sync(0xFFFFFFFFu, key, j);
-							rank += kj < key;
-						}
+						const uint32_t ga = (__float_as_uint(hi.w) >> (5 * a)) & 31u;
+						const uint32_t members =
+						    __reduce_or_sync(0xFFFFFFFFu, in ? (1u << ga) : 0u);
+						const uint32_t rank = __popc(members & ((1u << ga) - 1u));
 						// Boxes in sorted order: lane f + r holds the box of rank r.
 						if (in)
 							stage[f + rank] = make_float4(lo.x, lo.y, lo.z, hi.x);
@@ -868,8 +884,7 @@ __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 						}
 						__syncwarp();
 						Box6 p = sb, q = sb;
-#pragma unroll
-						for (int o = 1; o < 32; o <<= 1) {
+						for (int o = 1; o < cnt; o <<= 1) {
 							const Box6 pu = shfl_box(p, max(lane - o, 0));
 							const Box6 qd = shfl_box(q, min(lane + o, 31));
 							if (in && lane - o >= f)
