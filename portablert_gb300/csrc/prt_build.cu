@@ -1126,8 +1126,6 @@ static int lbvh_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch
 int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
                   cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg) {
 	const uint32_t S = plan.S, n = plan.n, n_int = plan.n_int;
-	const size_t ni = std::max<uint32_t>(n_int, 1);
-	const size_t nn = std::max<uint32_t>(n, 1);
 	if (plan.sah && !host_checks) {
 		msg = "the SAH build reads its level counters on the host";
 		return PRT_ERR_ARG;
