@@ -784,9 +784,11 @@ __global__ void __launch_bounds__(128) k_sah_mid(SahArgs A, int par) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Small tasks: one warp builds the subtree of up to 32 triangles, one per lane.  Each
-// node sorts its lanes' centres on each axis (rank by comparison), sweeps prefix and
-// suffix boxes and reorders its lanes by the best axis; the children are the two parts.
+// Small tasks: one warp builds the subtree of up to 32 triangles, one per lane.  The
+// triangles are ranked once per axis by (centre, index); each node orders its lanes on
+// each axis from those ranks (one OR of rank bits and a population count), sweeps prefix
+// and suffix boxes and reorders its lanes by the best axis; the children are the two
+// parts.
 
 __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 	__shared__ float4 stage_all[4][2 * 32];

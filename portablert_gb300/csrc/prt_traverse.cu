@@ -17,9 +17,15 @@
 //    pops one item and each of its 4 lanes loads and slab-tests 2 of the node's 8
 //    children: lane s takes children s and s + 4, so each of the two 256-bit loads of a
 //    group reads one 128-byte line of the node (children 2s and 2s + 1 would spread each
-//    load over two lines and double the L1 wavefronts: 15 % slower).  Hit inner children are pushed back as items and hit
-//    leaf triangles are appended to a triangle queue, at positions from ballots and
-//    popc.  Roots of new rays are admitted whenever fewer than 8 items are left.
+//    load over two lines and double the L1 wavefronts: 15 % slower).  Hit inner children
+//    are pushed back as items and hit leaf triangles are appended to a triangle queue,
+//    at positions from ballots and popc.  Roots of new rays are admitted whenever fewer
+//    than 8 items are left.  Unused child slots hold NaN boxes, which no plain slab test
+//    passes.
+//  * Each query is two launches: a regular pass over the batches whose 32 rays all have
+//    finite reciprocals (the plain slab test only), which counts and skips the others,
+//    and a deferred pass over those with the conservative test for zero direction
+//    components (it returns at once when there are none).
 //  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
 //    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
 //  * When the pool and the queue are empty the warp recomputes each slot's winning
