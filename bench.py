@@ -790,6 +790,39 @@ def run_gpu(args, world, rank):
     comp_node_size = b.stat("node_size")
     b.set_option("node_format", 0)
 
+    # Coherent and incoherent rays apart (the primary rays, the offset secondary rays),
+    # and the literal secondary rays (offset 0: they start on the surface they leave, and
+    # under the reference's semantics nearly all hit it again at t ~ 0).
+    def time_range(ptr, count, k=10):
+        for _ in range(3):
+            b.nearest_hits_dev(ptr, count, d_out.data_ptr(), TAGS, sptr)
+        b.sync()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(k)]
+        for s, e in evs:
+            flush.zero_()
+            s.record(stream)
+            b.nearest_hits_dev(ptr, count, d_out.data_ptr(), TAGS, sptr)
+            e.record(stream)
+        torch.cuda.synchronize()
+        return count / (sum(s.elapsed_time(e) for s, e in evs) / k) / 1e3
+
+    n_prim = len(prim)
+    coherence = {"primary": {"n": n_prim, "mrays_s": time_range(d_rays.data_ptr(), n_prim)},
+                 "secondary_offset": {"n": n - n_prim, "delta": DELTA,
+                                      "mrays_s": time_range(d_rays.data_ptr() + 24 * n_prim,
+                                                            n - n_prim)}}
+    if rank == 0:
+        hp = b.nearest_hits(prim, TAGS)
+        lit = workloads.secondary_rays(tris, prim, hp["valid"] != 0, hp["primitive_id"],
+                                       np.stack([hp["px"], hp["py"], hp["pz"]], 1),
+                                       N_SECONDARY, delta=0.0, seed=1)
+        d_lit = torch.from_numpy(np.ascontiguousarray(lit, dtype=np.float32)).cuda()
+        torch.cuda.synchronize()
+        coherence["secondary_literal"] = {"n": len(lit), "delta": 0.0,
+                                          "mrays_s": time_range(d_lit.data_ptr(), len(lit))}
+        del d_lit
+
     out = {"metric": METRIC, "value": mrays, "unit": "Mrays/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
@@ -821,6 +854,7 @@ def run_gpu(args, world, rank):
                               "nodes": lbvh_nodes}},
            "compressed": {"value": world * n * args.steps / (comp_ms / 1e3) / 1e6,
                           "unit": "Mrays/s", "node_bytes": comp_node_size},
+           "coherence": coherence,
            "clocks": clk}
     del d_rays, d_out, flush
     torch.cuda.empty_cache()
