@@ -436,10 +436,10 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 			                                       n, lay, d_out, cfg, ctx->d_work(),
 			                                       ctx->d_visits(), ctx->d_err(), ctx->stream,
 			                                       ctx->sms));
-			CAPI_TRY(ctx, cudaStreamSynchronize(ctx->stream));
 			if (ctx->count)
-				CAPI_TRY(ctx,
-				         cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
+				CAPI_TRY(ctx, cudaMemcpyAsync(ctx->visits, ctx->d_visits(), 16,
+				                              cudaMemcpyDeviceToHost, ctx->stream));
+			// One wait: the error word's copy is queued after the traversal.
 			return check_device_errors(ctx);
 		}
 	}
