@@ -86,6 +86,28 @@ def test_host_call_in_place_and_copied(gpu_backend, rays_mem, out_mem, direct):
             assert np.array_equal(got, want), (tags, shift)
 
 
+def test_host_call_with_device_buffers_runs_in_place(gpu_backend):
+    """Device memory handed to the host-buffer call is traversed where it is."""
+    import ctypes
+
+    import torch
+
+    tris = workloads.soup_tris(49, 3_000)
+    rays = workloads.soup_rays(50, 70_001)
+    gpu_backend.set_tris(tris)
+    lay = hitreg.layout(hitreg.TAGS)
+    want = _device_records(torch, gpu_backend, rays, hitreg.TAGS)
+    d_r = torch.from_numpy(rays).cuda()
+    d_o = torch.zeros(len(rays) * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    L = gpu_backend._L
+    gpu_backend._check(L.prt_b200_nearest_hits(
+        gpu_backend.ctx, ctypes.c_void_p(d_r.data_ptr()), len(rays), lay.mask, lay.size,
+        lay.offsets8(), ctypes.c_void_p(d_o.data_ptr())))
+    assert gpu_backend.stat("in_place") == 1.0
+    assert np.array_equal(d_o.cpu().numpy(), want)
+
+
 def test_chunked_host_call_pinned_buffers(gpu_backend):
     import ctypes
 
