@@ -1,6 +1,6 @@
 """The binned-SAH build (option build_sah): every field of every record equals the
 oracle's exhaustive search and the LBVH build's records, whatever the scene -- sizes at
-each boundary of the builder's tiers (32 and 1024 triangles, 2048-triangle chunks),
+each boundary of the builder's tiers (32 and 512 triangles, 2048-triangle chunks),
 identical triangles (no plane separates them), non-finite vertices and a scene whose
 planes would nest deeper than the depth guard -- and the tree needs fewer node visits
 than the LBVH on the heightfield and the soup."""
@@ -32,7 +32,8 @@ def sah(gpu_backend):
     gpu_backend.set_option("node_format", 0)
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 64, 1024, 1025, 2048, 2049, 5000, 40_000])
+@pytest.mark.parametrize("n", [1, 2, 3, 31, 32, 33, 64, 512, 513, 1024, 1025, 2048, 2049,
+                               5000, 40_000])
 def test_sizes_against_exhaustive_search(sah, oracle_lib, n):
     tris = W.soup_tris(9000 + n, n)
     rays = W.soup_rays(9100 + n, 4000)
