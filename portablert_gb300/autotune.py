@@ -98,11 +98,6 @@ def tune_batch(backend, d_tris_ptr: int, tri_off, queries, stream=None, reps: in
     Leaves the backend's options set to the winner.  `queries` is a list or ctypes
     array of prt_b200_query.  Returns {"config": {...}, "ms": best, "tried": [...],
     "cached": bool}."""
-    import torch
-
-    from .batch import Batch
-
-    stream = stream or torch.cuda.Stream()
     sig = signature(tri_off, queries)
     key = f"{backend.device_name()}|{sig}|{','.join(map(str, formats))}"
     data = _load(cache) if cache else {}
@@ -110,7 +105,12 @@ def tune_batch(backend, d_tris_ptr: int, tri_off, queries, stream=None, reps: in
         best = data[key]
         apply(backend, best["config"])
         return dict(best, cached=True)
+    import torch
+
     from . import _lib
+    from .batch import Batch
+
+    stream = stream or torch.cuda.Stream()
 
     qarr = queries if not isinstance(queries, list) else (_lib.Query * len(queries))(*queries)
     tried = []
