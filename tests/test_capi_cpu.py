@@ -82,3 +82,25 @@ def test_query_struct_layout_matches_header(tmp_path):
 def test_cpp_api_compiles_and_links():
     exe = build.build_cpp_test()
     assert os.path.exists(exe)
+
+
+def test_python_registry_mirrors_the_reference():
+    """portableRT's registry calls (backend.hpp:39-95, backend.cpp:50-56) in the Python
+    mirror: one backend named "B200", listed as available only where a device is, and
+    nearest_hits before select_backend is the reference's "Unknown backend" error."""
+    import numpy as np
+    import torch
+
+    from portablert_gb300 import backend
+
+    everything = backend.all_backends()
+    assert [b.name() for b in everything] == ["B200"]
+    avail = backend.available_backends()
+    if not torch.cuda.is_available():
+        assert avail == []
+    saved, backend.selected_backend = backend.selected_backend, None
+    try:
+        with pytest.raises(RuntimeError, match="Unknown backend"):
+            backend.nearest_hits(np.zeros((1, 6), np.float32))
+    finally:
+        backend.selected_backend = saved
