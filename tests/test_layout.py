@@ -87,3 +87,19 @@ def test_compat_header_layout_matches():
 def test_reference_header_layout_matches():
     got = _probe("/root/reference/include", extra=("-include", "cstdint", "-include", "iostream"))
     assert got == EXPECTED
+
+
+def test_batch_query_record_carries_the_layout():
+    """make_query fills a prt_b200_query with the HitReg layout of its tags (the C side
+    reads the same field mask, record size and offsets a single query would use)."""
+    from portablert_gb300 import hitreg
+    from portablert_gb300.batch import Batch, make_query
+
+    for tags in (hitreg.TAGS, ("valid",), ("t", "primitive_id", "uv", "valid")):
+        lay = hitreg.layout(tags)
+        q = make_query(7, 0x1000, 123, 0x2000, tags)
+        assert (q.scene, q.rays, q.n_rays, q.out) == (7, 0x1000, 123, 0x2000)
+        assert q.field_mask == lay.mask and q.rec_size == lay.size
+        assert list(q.offs) == list(lay.offsets8())
+    off, ptr, s = Batch._offsets([0, 5, 5, 12])
+    assert s == 3 and off.dtype.name == "uint64" and ptr[3] == 12
