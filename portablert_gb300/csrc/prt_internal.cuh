@@ -269,15 +269,6 @@ __device__ __forceinline__ void best_init(Best &b) {
 	b.pid = kNone;
 }
 
-__device__ __forceinline__ void best_offer(Best &b, float t, float u, float v, uint32_t pid) {
-	if (t < b.t || (t == b.t && t < INFINITY && pid < b.pid)) {
-		b.t = t;
-		b.u = u;
-		b.v = v;
-		b.pid = pid;
-	}
-}
-
 // Exact per-triangle test: the reference slab test on the triangle's own bounding
 // box (make_aabb, bvh.hpp:28-37, select semantics) and then Moller-Trumbore.  True
 // when the reference would accept the triangle (its t may still be +inf or NaN, which
@@ -293,17 +284,10 @@ __device__ __forceinline__ bool tri_test(const RayC &r, const float4 a, const fl
 	return ref_mt(r, a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, t, u, v);
 }
 
-__device__ __forceinline__ void test_triangle(const RayC &r, const float4 a, const float4 b,
-                                              const float4 c, Best &best) {
-	float t, u, v;
-	if (tri_test(r, a, b, c, t, u, v))
-		best_offer(best, t, u, v, __float_as_uint(a.w));
-}
-
 // The closest hit as one 64-bit key: order-preserving bits of t above the primitive
-// id, so the minimum key is the smallest t and, among equal t, the smallest id (the
-// same rule as best_offer).  -0 and +0 compare equal as floats, so both map to +0's
-// key; the hit itself is recomputed from the winning id.  kNoHit: nothing recorded.
+// id, so the minimum key is the smallest t and, among equal t, the smallest id (ties in
+// t go to the smaller id).  -0 and +0 compare equal as floats, so both map to +0's key;
+// the hit itself is recomputed from the winning id.  kNoHit: nothing recorded.
 constexpr unsigned long long kNoHit = ~0ull;
 
 __device__ __forceinline__ unsigned long long hit_key(float t, uint32_t pid) {
