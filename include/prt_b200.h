@@ -194,7 +194,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  place (pinned memory; pageable memory where the device reads it
  *                  through the host's page tables, as on Grace) traverses them there:
  *                  rays read and records written over the host link, no staging copies
- *                  (default 1); 0 = always the chunked copy pipeline below
+ *                  (default 1; rays not 8-byte aligned are copied); 0 = always the
+ *                  chunked copy pipeline below
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)

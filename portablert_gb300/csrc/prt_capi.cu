@@ -426,9 +426,13 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 	cfg.count = ctx->count;
 	// In place when the device can reach both buffers: the traversal reads each ray from
 	// host memory once and writes each record there once, over the host link, with no
-	// staging buffers and nothing to overlap.
+	// staging buffers and nothing to overlap.  The traversal reads rays as 8-byte pairs,
+	// so rays that are only 4-byte aligned (a float array at an odd index) are copied
+	// into the aligned staging buffer instead; records may have any alignment.
 	if (ctx->host_direct) {
 		const void *d_in = device_alias(ctx, rays6);
+		if (reinterpret_cast<uintptr_t>(d_in) % 8 != 0)
+			d_in = nullptr;
 		void *d_out = d_in ? device_alias(ctx, out_host) : nullptr;
 		ctx->last_in_place = d_in && d_out;
 		if (d_in && d_out) {

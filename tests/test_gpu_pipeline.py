@@ -108,6 +108,46 @@ def test_host_call_with_device_buffers_runs_in_place(gpu_backend):
     assert np.array_equal(d_o.cpu().numpy(), want)
 
 
+@pytest.mark.parametrize("rays_mem", ["pinned", "pageable"])
+def test_host_rays_at_a_four_byte_offset_are_copied(gpu_backend, rays_mem):
+    """Rays starting 4 bytes past an 8-byte boundary (a float array at an odd index) are
+    not traversed in place, since the traversal reads them in 8-byte pairs: the call
+    copies them into its aligned staging buffer and gives the same records; the same
+    rays 8-byte aligned are traversed in place."""
+    import ctypes
+
+    import torch
+
+    tris = workloads.soup_tris(51, 4_000)
+    rays = workloads.soup_rays(52, 40_001)
+    gpu_backend.set_tris(tris)
+    lay = hitreg.layout(hitreg.TAGS)
+    want = _device_records(torch, gpu_backend, rays, hitreg.TAGS)
+    flat = np.zeros(rays.size + 2, np.float32)
+    buf = torch.from_numpy(flat).pin_memory() if rays_mem == "pinned" else flat
+    base = buf.data_ptr() if rays_mem == "pinned" else flat.ctypes.data
+    assert base % 8 == 0
+    host = buf.numpy() if rays_mem == "pinned" else flat
+    size = len(rays) * lay.size
+    o = torch.zeros(size, dtype=torch.uint8).pin_memory() if rays_mem == "pinned" else \
+        np.zeros(size, np.uint8)
+    o_ptr = o.data_ptr() if rays_mem == "pinned" else o.ctypes.data
+    L = gpu_backend._L
+    for k in (1, 2):
+        host[:] = 0.0
+        host[k:k + rays.size] = rays.reshape(-1)
+        o[:] = 0
+        gpu_backend._check(L.prt_b200_nearest_hits(
+            gpu_backend.ctx, ctypes.c_void_p(base + 4 * k), len(rays), lay.mask, lay.size,
+            lay.offsets8(), ctypes.c_void_p(o_ptr)))
+        if k == 1:
+            assert gpu_backend.stat("in_place") == 0.0, rays_mem
+        elif rays_mem == "pinned":  # pageable memory is reachable only on some hosts
+            assert gpu_backend.stat("in_place") == 1.0
+        got = o.numpy() if rays_mem == "pinned" else o
+        assert np.array_equal(got, want), (k, rays_mem)
+
+
 def test_chunked_host_call_pinned_buffers(gpu_backend):
     import ctypes
 
