@@ -11,7 +11,6 @@
 // that scene alone (tested).
 #include <algorithm>
 #include <cstring>
-#include <functional>
 #include <string>
 #include <vector>
 
@@ -149,9 +148,10 @@ int launch_query(prt_b200_batch *b, Slot &s, const std::vector<prt::SegDesc> &se
 	return PRT_OK;
 }
 
-size_t graph_key(const float *d_tris, const uint64_t *tri_off, uint32_t S,
-                 const prt_b200_query *q, uint32_t nq, const prt_b200_ctx *ctx) {
-	std::hash<std::string> h;
+// Everything a captured graph bakes in (pointers, scene offsets, queries, options),
+// compared in full so that a replay never runs a graph made for other buffers.
+std::string graph_key(const float *d_tris, const uint64_t *tri_off, uint32_t S,
+                      const prt_b200_query *q, uint32_t nq, const prt_b200_ctx *ctx) {
 	std::string k(reinterpret_cast<const char *>(&d_tris), sizeof d_tris);
 	k.append(reinterpret_cast<const char *>(tri_off), sizeof(uint64_t) * (S + 1));
 	k.append(reinterpret_cast<const char *>(q), sizeof(prt_b200_query) * nq);
@@ -159,7 +159,7 @@ size_t graph_key(const float *d_tris, const uint64_t *tri_off, uint32_t S,
 	                     (int)ctx->count,     ctx->pool_depth,        (int)ctx->build_compressed,
 	                     (int)ctx->collapse_cost};
 	k.append(reinterpret_cast<const char *>(opts), sizeof opts);
-	return h(k);
+	return k;
 }
 
 void drop_graph(prt_b200_batch *b) {
@@ -169,7 +169,7 @@ void drop_graph(prt_b200_batch *b) {
 		cudaGraphDestroy(b->graph);
 	b->gexec = nullptr;
 	b->graph = nullptr;
-	b->graph_key = 0;
+	b->graph_key.clear();
 }
 
 } // namespace
@@ -343,7 +343,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 	std::lock_guard<std::mutex> lk(ctx->mu);
 	B_TRY(ctx, cudaSetDevice(ctx->device));
 	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-	const size_t key = graph_key(d_tris, tri_off, n_scenes, queries, n_queries, ctx);
+	std::string key = graph_key(d_tris, tri_off, n_scenes, queries, n_queries, ctx);
 	if (!b->gexec || key != b->graph_key) {
 		drop_graph(b);
 		b->built = false;
@@ -395,7 +395,7 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 			drop_graph(b);
 			return bcuda(ctx, ie, "batch run_graph: instantiate");
 		}
-		b->graph_key = key;
+		b->graph_key = std::move(key);
 	} else {
 		int rc = check_slot(b, b->gslot);
 		if (rc != PRT_OK)

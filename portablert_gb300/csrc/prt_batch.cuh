@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
 #include "prt_ctx.cuh"
@@ -40,7 +42,7 @@ struct prt_b200_batch {
 	// CUDA graph of build + query
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t gexec = nullptr;
-	size_t graph_key = 0;
+	std::string graph_key;
 	prt::BatchSlot gslot;
 	prt::BuildPlan gplan;
 	bool graph_dirty = false;   // arena stats not read back since the last replay
