@@ -9,14 +9,18 @@
 // Faces of n > 3 vertices are split as a fan (a, b_k, b_k+1) (tinyobjloader triangulates
 // too; its own split of polygons is not restated, the examples' meshes are triangle
 // meshes).  Every other line (vt, vn, o, g, s, usemtl, mtllib, comments) is skipped.
-// Numbers are parsed as double and rounded to float, as tinyobjloader does.
+// Numbers are parsed as double (independent of the C locale) and rounded to float, as
+// tinyobjloader does.
 #include <stdint.h>
 
 #include <algorithm>
 #include <cerrno>
+#include <charconv>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -34,6 +38,30 @@ const char *skip_space(const char *p, const char *e) {
 	while (p < e && is_space(*p))
 		++p;
 	return p;
+}
+
+// A decimal number in [p, e) (optional sign, digits, fraction, exponent, or inf/nan),
+// correctly rounded to double whatever the process's locale; the end of the number, or
+// null when none starts at p.
+const char *parse_number(const char *p, const char *e, double &out) {
+	const bool neg = p < e && *p == '-';
+	const char *q = (p < e && (*p == '+' || *p == '-')) ? p + 1 : p;
+	if (q < e && (*q == '+' || *q == '-'))
+		return nullptr;
+	const std::from_chars_result r = std::from_chars(q, e, out);
+	if (r.ec == std::errc::invalid_argument || r.ptr == q)
+		return nullptr;
+	if (r.ec == std::errc::result_out_of_range) {
+		// Beyond double's range: the nearest double, as the C library's strtod gives.
+		const char *x = q;
+		while (x < r.ptr && *x != 'e' && *x != 'E')
+			++x;
+		const bool tiny = x < r.ptr && x + 1 < r.ptr && x[1] == '-';
+		out = tiny ? 0.0 : HUGE_VAL;
+	}
+	if (neg)
+		out = -out;
+	return r.ptr;
 }
 
 // One vertex reference of an `f` line: the position index before any '/'.
@@ -55,7 +83,7 @@ bool parse_ref(const char *&p, const char *e, long long n_verts, uint32_t &out) 
 
 int parse(const std::vector<char> &buf, std::vector<float> &tris, std::string &err) {
 	std::vector<float> verts;
-	// buf ends with a NUL that is not part of the text (it stops strtod and strtoll).
+	// buf ends with a NUL that is not part of the text (it stops strtoll).
 	const char *p = buf.data(), *end = buf.data() + buf.size() - 1;
 	uint64_t line = 0;
 	std::vector<uint32_t> face;
@@ -69,9 +97,9 @@ int parse(const std::vector<char> &buf, std::vector<float> &tris, std::string &e
 			q += 2;
 			for (int k = 0; k < 3; ++k) {
 				q = skip_space(q, le);
-				char *ne = nullptr;
-				const double d = std::strtod(q, &ne);
-				if (ne == q || ne > le) {
+				double d = 0.0;
+				const char *ne = parse_number(q, le, d);
+				if (!ne) {
 					err = "obj line " + std::to_string(line) + ": bad vertex";
 					return PRT_ERR_ARG;
 				}
@@ -123,19 +151,29 @@ int prt_b200_obj_load(const char *path, float **tris9, uint64_t *n_tris) {
 		prt::set_global_error(std::string("obj_load: cannot open ") + path);
 		return PRT_ERR_ARG;
 	}
-	std::vector<char> buf;
-	char chunk[1 << 16];
-	size_t got;
-	while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0)
-		buf.insert(buf.end(), chunk, chunk + got);
-	std::fclose(f);
-	buf.push_back('\0');
+	// The file and the soup are held in host vectors: a file too large for host memory
+	// is an error status, not an exception through the C boundary.
 	std::vector<float> tris;
-	std::string err;
-	const int rc = parse(buf, tris, err);
-	if (rc != PRT_OK) {
-		prt::set_global_error(err);
-		return rc;
+	try {
+		std::vector<char> buf;
+		char chunk[1 << 16];
+		size_t got;
+		while ((got = std::fread(chunk, 1, sizeof chunk, f)) > 0)
+			buf.insert(buf.end(), chunk, chunk + got);
+		std::fclose(f);
+		f = nullptr;
+		buf.push_back('\0');
+		std::string err;
+		const int rc = parse(buf, tris, err);
+		if (rc != PRT_OK) {
+			prt::set_global_error(err);
+			return rc;
+		}
+	} catch (const std::bad_alloc &) {
+		if (f)
+			std::fclose(f);
+		prt::set_global_error("obj_load: out of host memory");
+		return PRT_ERR_OOM;
 	}
 	float *out = static_cast<float *>(std::malloc(std::max<size_t>(tris.size(), 1) * sizeof(float)));
 	if (!out) {

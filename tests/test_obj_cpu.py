@@ -20,7 +20,8 @@ def _py_parse(text):
         if not p:
             continue
         if p[0] == "v":
-            verts.append([np.float32(float(x)) for x in p[1:4]])
+            with np.errstate(over="ignore"):  # beyond float's range rounds to inf
+                verts.append([np.float32(float(x)) for x in p[1:4]])
         elif p[0] == "f":
             idx = []
             for r in p[1:]:
@@ -92,3 +93,37 @@ def test_examples_bunny():
         want = _py_parse(f.read())
     assert got.shape == (4968, 9)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+def test_number_forms_round_like_python(tmp_path):
+    """Signs, exponents, long mantissas (correct rounding to double, then to float),
+    values beyond double's range, inf and nan: each coordinate equals Python's float()
+    rounded to float32, whatever the process's C locale."""
+    nums = ["+1.5", "-2e3", "1E-2", ".5", "5.", "-0", "0.1000000000000000055511151231257827",
+            "3.4028235677973366e38", "3.4028236e38", "1.4e-45", "7e-46", "1e400", "-1e400",
+            "1e-400", "inf", "-INF", "Infinity", "123456789012345678901234567890",
+            "0.333333333333333333333333333333333333333333333", "nan"]
+    while len(nums) % 3:
+        nums.append("0")
+    lines = [f"v {nums[i]} {nums[i + 1]} {nums[i + 2]}" for i in range(0, len(nums), 3)]
+    nv = len(lines)
+    lines += [f"f {a + 1} {b + 1} {c + 1}" for a, b, c in
+              [(k, (k + 1) % nv, (k + 2) % nv) for k in range(nv)]]
+    text = "\n".join(lines) + "\n"
+    p = tmp_path / "n.obj"
+    p.write_text(text)
+    got = obj.load_obj(str(p))
+    want = _py_parse(text)
+    assert got.shape == want.shape
+    nan_g, nan_w = np.isnan(got), np.isnan(want)
+    assert np.array_equal(nan_g, nan_w)
+    assert np.array_equal(got[~nan_g].view(np.uint32), want[~nan_w].view(np.uint32))
+
+
+@pytest.mark.parametrize("text", ["v 1 2\n3 4 5\nf 1 1 1\n", "v 1 2 +-3\n", "v 1 2 -\n",
+                                  "v 1 2 e5\n"])
+def test_a_vertex_never_borrows_from_the_next_line_or_a_bad_number(tmp_path, text):
+    p = tmp_path / "bad.obj"
+    p.write_text(text)
+    with pytest.raises(PrtError):
+        obj.load_obj(str(p))
