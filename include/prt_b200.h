@@ -32,7 +32,7 @@ enum {
 	PRT_ERR_NO_DEVICE = 3,    /* no sm_103 device */
 	PRT_ERR_NO_SCENE = 4,     /* nearest_hits before set_tris */
 	PRT_ERR_DEVICE = 5,       /* a kernel reported an error (see last_error) */
-	PRT_ERR_OOM = 6,          /* device allocation failed */
+	PRT_ERR_OOM = 6,          /* device or host allocation failed (or a thread did not start) */
 	PRT_ERR_LIMIT = 7         /* a documented size limit was exceeded */
 };
 

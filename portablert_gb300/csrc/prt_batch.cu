@@ -245,58 +245,60 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 	if (!b)
 		return PRT_ERR_ARG;
 	prt_b200_ctx *ctx = b->ctx;
-	if (n_scenes == 0 || !tri_off || (tri_off[n_scenes] && !d_tris))
-		return bfail(ctx, PRT_ERR_ARG, "batch set_tris: need scenes, offsets and triangles");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	B_TRY(ctx, cudaSetDevice(ctx->device));
-	for (int i = 0; i < kSlots; ++i) {
-		int rc = check_slot(b, b->slots[i]);
+	return prt::guarded(&ctx->err, "batch set_tris", [&]() -> int {
+		if (n_scenes == 0 || !tri_off || (tri_off[n_scenes] && !d_tris))
+			return bfail(ctx, PRT_ERR_ARG, "batch set_tris: need scenes, offsets and triangles");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		B_TRY(ctx, cudaSetDevice(ctx->device));
+		for (int i = 0; i < kSlots; ++i) {
+			int rc = check_slot(b, b->slots[i]);
+			if (rc != PRT_OK)
+				return rc;
+		}
+		drop_graph(b);
+		b->built = false;
+		cudaEvent_t e0, e1;
+		B_TRY(ctx, cudaEventCreate(&e0));
+		B_TRY(ctx, cudaEventCreate(&e1));
+		cudaEventRecord(e0, ctx->stream);
+		std::string msg;
+		// Binned-SAH trees as set_tris builds them (option build_sah); a tree too deep for
+		// the collapse falls back to the LBVH.  Graph builds (run_graph) are always LBVH.
+		bool sah = ctx->build_sah;
+		int rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
+		                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg, sah,
+		                           ctx->collapse_cost);
+		if (sah && rc == PRT_ERR_LIMIT) {
+			sah = false;
+			msg.clear();
+			rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
+			                       b->arena, b->ws, ctx->stream, ctx->d_err(), msg, false,
+			                       ctx->collapse_cost);
+		}
+		b->built_sah = sah;
+		cudaEventRecord(e1, ctx->stream);
+		cudaEventSynchronize(e1);
+		float ms = 0.0f;
+		cudaEventElapsedTime(&ms, e0, e1);
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		b->build_ms = ms;
+		if (rc != PRT_OK)
+			return bfail(ctx, rc, msg);
+		uint32_t err_word = 0;
+		B_TRY(ctx, cudaMemcpy(&err_word, ctx->d_err(), 4, cudaMemcpyDeviceToHost));
+		if (err_word) {
+			cudaMemset(ctx->d_err(), 0, 4);
+			return bfail(ctx, PRT_ERR_DEVICE, "batch build: kernel reported an error");
+		}
+		if ((int)b->arena.depth > prt::traversal_stack_depth())
+			return bfail(ctx, PRT_ERR_LIMIT, "batch build: tree too deep for the traversal");
+		rc = scene_tables(b);
 		if (rc != PRT_OK)
 			return rc;
-	}
-	drop_graph(b);
-	b->built = false;
-	cudaEvent_t e0, e1;
-	B_TRY(ctx, cudaEventCreate(&e0));
-	B_TRY(ctx, cudaEventCreate(&e1));
-	cudaEventRecord(e0, ctx->stream);
-	std::string msg;
-	// Binned-SAH trees as set_tris builds them (option build_sah); a tree too deep for
-	// the collapse falls back to the LBVH.  Graph builds (run_graph) are always LBVH.
-	bool sah = ctx->build_sah;
-	int rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-	                           b->arena, b->ws, ctx->stream, ctx->d_err(), msg, sah,
-	                           ctx->collapse_cost);
-	if (sah && rc == PRT_ERR_LIMIT) {
-		sah = false;
-		msg.clear();
-		rc = prt::build_scenes(d_tris, tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed,
-		                       b->arena, b->ws, ctx->stream, ctx->d_err(), msg, false,
-		                       ctx->collapse_cost);
-	}
-	b->built_sah = sah;
-	cudaEventRecord(e1, ctx->stream);
-	cudaEventSynchronize(e1);
-	float ms = 0.0f;
-	cudaEventElapsedTime(&ms, e0, e1);
-	cudaEventDestroy(e0);
-	cudaEventDestroy(e1);
-	b->build_ms = ms;
-	if (rc != PRT_OK)
-		return bfail(ctx, rc, msg);
-	uint32_t err_word = 0;
-	B_TRY(ctx, cudaMemcpy(&err_word, ctx->d_err(), 4, cudaMemcpyDeviceToHost));
-	if (err_word) {
-		cudaMemset(ctx->d_err(), 0, 4);
-		return bfail(ctx, PRT_ERR_DEVICE, "batch build: kernel reported an error");
-	}
-	if ((int)b->arena.depth > prt::traversal_stack_depth())
-		return bfail(ctx, PRT_ERR_LIMIT, "batch build: tree too deep for the traversal");
-	rc = scene_tables(b);
-	if (rc != PRT_OK)
-		return rc;
-	b->built = true;
-	return PRT_OK;
+		b->built = true;
+		return PRT_OK;
+	});
 }
 
 int prt_b200_batch_query_dev(prt_b200_batch *b, const prt_b200_query *queries, uint32_t n_queries,
@@ -304,32 +306,34 @@ int prt_b200_batch_query_dev(prt_b200_batch *b, const prt_b200_query *queries, u
 	if (!b || (n_queries && !queries))
 		return b ? bfail(b->ctx, PRT_ERR_ARG, "batch query: null query list") : PRT_ERR_ARG;
 	prt_b200_ctx *ctx = b->ctx;
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	if (!b->built)
-		return bfail(ctx, PRT_ERR_NO_SCENE, "batch query: batch_set_tris has not succeeded");
-	if (ctx->node_format == PRT_NODES_COMPRESSED && !b->arena.has_cnodes)
-		return bfail(ctx, PRT_ERR_ARG, "batch query: compressed nodes were not built");
-	B_TRY(ctx, cudaSetDevice(ctx->device));
-	std::vector<prt::SegDesc> segs;
-	unsigned long long n_virtual = 0;
-	int rc = segments(b, queries, n_queries, segs, n_virtual);
-	if (rc != PRT_OK || segs.empty())
-		return rc;
-	Slot &s = b->slots[b->next_slot];
-	b->next_slot = (b->next_slot + 1) % kSlots;
-	rc = check_slot(b, s);
-	if (rc != PRT_OK)
-		return rc;
-	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-	B_TRY(ctx, s.segs.reserve(sizeof(prt::SegDesc) * segs.size()));
-	B_TRY(ctx, cudaMemcpyAsync(s.segs.p, segs.data(), sizeof(prt::SegDesc) * segs.size(),
-	                           cudaMemcpyHostToDevice, st));
-	rc = launch_query(b, s, segs, n_virtual, 0, b->arena.n_nodes, st);
-	if (rc != PRT_OK)
-		return rc;
-	B_TRY(ctx, cudaEventRecord(s.done, st));
-	s.pending = true;
-	return PRT_OK;
+	return prt::guarded(&ctx->err, "batch query", [&]() -> int {
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		if (!b->built)
+			return bfail(ctx, PRT_ERR_NO_SCENE, "batch query: batch_set_tris has not succeeded");
+		if (ctx->node_format == PRT_NODES_COMPRESSED && !b->arena.has_cnodes)
+			return bfail(ctx, PRT_ERR_ARG, "batch query: compressed nodes were not built");
+		B_TRY(ctx, cudaSetDevice(ctx->device));
+		std::vector<prt::SegDesc> segs;
+		unsigned long long n_virtual = 0;
+		int rc = segments(b, queries, n_queries, segs, n_virtual);
+		if (rc != PRT_OK || segs.empty())
+			return rc;
+		Slot &s = b->slots[b->next_slot];
+		b->next_slot = (b->next_slot + 1) % kSlots;
+		rc = check_slot(b, s);
+		if (rc != PRT_OK)
+			return rc;
+		cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+		B_TRY(ctx, s.segs.reserve(sizeof(prt::SegDesc) * segs.size()));
+		B_TRY(ctx, cudaMemcpyAsync(s.segs.p, segs.data(), sizeof(prt::SegDesc) * segs.size(),
+		                           cudaMemcpyHostToDevice, st));
+		rc = launch_query(b, s, segs, n_virtual, 0, b->arena.n_nodes, st);
+		if (rc != PRT_OK)
+			return rc;
+		B_TRY(ctx, cudaEventRecord(s.done, st));
+		s.pending = true;
+		return PRT_OK;
+	});
 }
 
 int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint64_t *tri_off,
@@ -338,75 +342,77 @@ int prt_b200_batch_run_graph(prt_b200_batch *b, const float *d_tris, const uint6
 	if (!b)
 		return PRT_ERR_ARG;
 	prt_b200_ctx *ctx = b->ctx;
-	if (n_scenes == 0 || !tri_off || (n_queries && !queries))
-		return bfail(ctx, PRT_ERR_ARG, "batch run_graph: bad arguments");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	B_TRY(ctx, cudaSetDevice(ctx->device));
-	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-	std::string key = graph_key(d_tris, tri_off, n_scenes, queries, n_queries, ctx);
-	if (!b->gexec || key != b->graph_key) {
-		drop_graph(b);
-		b->built = false;
-		int rc = check_slot(b, b->gslot);
-		if (rc != PRT_OK)
-			return rc;
-		std::string msg;
-		// Plan: reserve everything and upload the offset tables outside the graph.
-		rc = prt::build_plan(tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed, b->arena,
-		                     b->ws, ctx->stream, b->gplan, msg, false, ctx->collapse_cost);
-		if (rc != PRT_OK)
-			return bfail(ctx, rc, msg);
-		b->arena.has_cnodes = ctx->build_compressed;
-		b->arena.depth = (uint32_t)prt::traversal_stack_depth();
-		b->arena.n_nodes = b->gplan.node_cap;
-		rc = scene_tables(b);
-		if (rc != PRT_OK)
-			return rc;
-		std::vector<prt::SegDesc> segs;
-		unsigned long long n_virtual = 0;
-		rc = segments(b, queries, n_queries, segs, n_virtual);
-		if (rc != PRT_OK)
-			return rc;
-		B_TRY(ctx, b->gslot.segs.reserve(sizeof(prt::SegDesc) * std::max<size_t>(segs.size(), 1)));
-		if (!segs.empty())
-			B_TRY(ctx, cudaMemcpy(b->gslot.segs.p, segs.data(), sizeof(prt::SegDesc) * segs.size(),
-			                      cudaMemcpyHostToDevice));
-		B_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-		// Capture: the whole build (no host round-trips) and the query launch.
-		B_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-		rc = prt::build_enqueue(d_tris, b->gplan, b->arena, b->ws, ctx->stream, ctx->d_err(),
-		                        false, msg);
-		if (rc == PRT_OK && !segs.empty())
-			rc = launch_query(b, b->gslot, segs, n_virtual,
-			                  ctx->pool_depth ? ctx->pool_depth : prt::traversal_stack_depth(),
-			                  b->gplan.node_cap, ctx->stream);
-		cudaGraph_t g = nullptr;
-		cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
-		if (rc != PRT_OK) {
-			if (g)
-				cudaGraphDestroy(g);
-			return rc == PRT_ERR_CUDA ? rc : bfail(ctx, rc, msg.empty() ? ctx->err.get() : msg);
-		}
-		if (ce != cudaSuccess)
-			return bcuda(ctx, ce, "batch run_graph: capture");
-		b->graph = g;
-		cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
-		if (ie != cudaSuccess) {
+	return prt::guarded(&ctx->err, "batch run_graph", [&]() -> int {
+		if (n_scenes == 0 || !tri_off || (n_queries && !queries))
+			return bfail(ctx, PRT_ERR_ARG, "batch run_graph: bad arguments");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		B_TRY(ctx, cudaSetDevice(ctx->device));
+		cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+		std::string key = graph_key(d_tris, tri_off, n_scenes, queries, n_queries, ctx);
+		if (!b->gexec || key != b->graph_key) {
 			drop_graph(b);
-			return bcuda(ctx, ie, "batch run_graph: instantiate");
+			b->built = false;
+			int rc = check_slot(b, b->gslot);
+			if (rc != PRT_OK)
+				return rc;
+			std::string msg;
+			// Plan: reserve everything and upload the offset tables outside the graph.
+			rc = prt::build_plan(tri_off, n_scenes, ctx->leaf_size, ctx->build_compressed, b->arena,
+			                     b->ws, ctx->stream, b->gplan, msg, false, ctx->collapse_cost);
+			if (rc != PRT_OK)
+				return bfail(ctx, rc, msg);
+			b->arena.has_cnodes = ctx->build_compressed;
+			b->arena.depth = (uint32_t)prt::traversal_stack_depth();
+			b->arena.n_nodes = b->gplan.node_cap;
+			rc = scene_tables(b);
+			if (rc != PRT_OK)
+				return rc;
+			std::vector<prt::SegDesc> segs;
+			unsigned long long n_virtual = 0;
+			rc = segments(b, queries, n_queries, segs, n_virtual);
+			if (rc != PRT_OK)
+				return rc;
+			B_TRY(ctx, b->gslot.segs.reserve(sizeof(prt::SegDesc) * std::max<size_t>(segs.size(), 1)));
+			if (!segs.empty())
+				B_TRY(ctx, cudaMemcpy(b->gslot.segs.p, segs.data(), sizeof(prt::SegDesc) * segs.size(),
+				                      cudaMemcpyHostToDevice));
+			B_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+			// Capture: the whole build (no host round-trips) and the query launch.
+			B_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+			rc = prt::build_enqueue(d_tris, b->gplan, b->arena, b->ws, ctx->stream, ctx->d_err(),
+			                        false, msg);
+			if (rc == PRT_OK && !segs.empty())
+				rc = launch_query(b, b->gslot, segs, n_virtual,
+				                  ctx->pool_depth ? ctx->pool_depth : prt::traversal_stack_depth(),
+				                  b->gplan.node_cap, ctx->stream);
+			cudaGraph_t g = nullptr;
+			cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+			if (rc != PRT_OK) {
+				if (g)
+					cudaGraphDestroy(g);
+				return rc == PRT_ERR_CUDA ? rc : bfail(ctx, rc, msg.empty() ? ctx->err.get() : msg);
+			}
+			if (ce != cudaSuccess)
+				return bcuda(ctx, ce, "batch run_graph: capture");
+			b->graph = g;
+			cudaError_t ie = cudaGraphInstantiate(&b->gexec, g, 0);
+			if (ie != cudaSuccess) {
+				drop_graph(b);
+				return bcuda(ctx, ie, "batch run_graph: instantiate");
+			}
+			b->graph_key = std::move(key);
+		} else {
+			int rc = check_slot(b, b->gslot);
+			if (rc != PRT_OK)
+				return rc;
 		}
-		b->graph_key = std::move(key);
-	} else {
-		int rc = check_slot(b, b->gslot);
-		if (rc != PRT_OK)
-			return rc;
-	}
-	B_TRY(ctx, cudaGraphLaunch(b->gexec, st));
-	B_TRY(ctx, cudaEventRecord(b->gslot.done, st));
-	b->gslot.pending = true;
-	b->graph_dirty = true;
-	b->built = true;
-	return PRT_OK;
+		B_TRY(ctx, cudaGraphLaunch(b->gexec, st));
+		B_TRY(ctx, cudaEventRecord(b->gslot.done, st));
+		b->gslot.pending = true;
+		b->graph_dirty = true;
+		b->built = true;
+		return PRT_OK;
+	}, ctx->stream);
 }
 
 int prt_b200_batch_sync(prt_b200_batch *b) {

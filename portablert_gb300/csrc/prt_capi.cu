@@ -259,30 +259,34 @@ int prt_b200_device_name(prt_b200_ctx *ctx, char *buf, size_t len) {
 int prt_b200_set_tris(prt_b200_ctx *ctx, const float *tris9, uint64_t n) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	if (!tris9 && n)
-		return fail(ctx, PRT_ERR_ARG, "set_tris: null triangle pointer");
-	if (n > prt::kMaxTris)
-		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-	if (n) {
-		CAPI_TRY(ctx, ctx->tris_in.reserve(36ull * n));
-		CAPI_TRY(ctx, cudaMemcpyAsync(ctx->tris_in.p, tris9, 36ull * n, cudaMemcpyHostToDevice,
-		                              ctx->stream));
-	}
-	return do_build(ctx, ctx->tris_in.as<float>(), n);
+	return prt::guarded(&ctx->err, "set_tris", [&]() -> int {
+		if (!tris9 && n)
+			return fail(ctx, PRT_ERR_ARG, "set_tris: null triangle pointer");
+		if (n > prt::kMaxTris)
+			return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+		if (n) {
+			CAPI_TRY(ctx, ctx->tris_in.reserve(36ull * n));
+			CAPI_TRY(ctx, cudaMemcpyAsync(ctx->tris_in.p, tris9, 36ull * n, cudaMemcpyHostToDevice,
+			                              ctx->stream));
+		}
+		return do_build(ctx, ctx->tris_in.as<float>(), n);
+	});
 }
 
 int prt_b200_set_tris_dev(prt_b200_ctx *ctx, const float *d_tris9, uint64_t n) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	if (!d_tris9 && n)
-		return fail(ctx, PRT_ERR_ARG, "set_tris_dev: null triangle pointer");
-	if (n > prt::kMaxTris)
-		return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-	return do_build(ctx, d_tris9, n);
+	return prt::guarded(&ctx->err, "set_tris_dev", [&]() -> int {
+		if (!d_tris9 && n)
+			return fail(ctx, PRT_ERR_ARG, "set_tris_dev: null triangle pointer");
+		if (n > prt::kMaxTris)
+			return fail(ctx, PRT_ERR_LIMIT, "set_tris: at most 134217727 triangles per scene");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+		return do_build(ctx, d_tris9, n);
+	});
 }
 
 } // extern "C"
@@ -333,15 +337,17 @@ int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t 
                               void *d_out, void *stream) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	std::string why;
-	if (!layout_ok(field_mask, rec_size, offs, why))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
-	if (n && (!d_rays6 || !d_out))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
-	if (reinterpret_cast<uintptr_t>(d_rays6) % 8 != 0)
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: rays must be 8-byte aligned");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	return queue_query(ctx, d_rays6, n, field_mask, rec_size, offs, d_out, stream, nullptr);
+	return prt::guarded(&ctx->err, "nearest_hits_dev", [&]() -> int {
+		std::string why;
+		if (!layout_ok(field_mask, rec_size, offs, why))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
+		if (n && (!d_rays6 || !d_out))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
+		if (reinterpret_cast<uintptr_t>(d_rays6) % 8 != 0)
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: rays must be 8-byte aligned");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		return queue_query(ctx, d_rays6, n, field_mask, rec_size, offs, d_out, stream, nullptr);
+	});
 }
 
 int prt_b200_nearest_hits_camera(prt_b200_ctx *ctx, const prt_b200_camera *camera,
@@ -349,15 +355,17 @@ int prt_b200_nearest_hits_camera(prt_b200_ctx *ctx, const prt_b200_camera *camer
                                  void *d_out, void *stream) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	std::string why;
-	if (!prt::camera_ok(camera, why) || !layout_ok(field_mask, rec_size, offs, why))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: " + why);
-	if (!d_out)
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: null output");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	const prt_b200_camera cam = *camera;
-	return queue_query(ctx, nullptr, (uint64_t)cam.width * cam.height, field_mask, rec_size,
-	                   offs, d_out, stream, &cam);
+	return prt::guarded(&ctx->err, "nearest_hits_camera", [&]() -> int {
+		std::string why;
+		if (!prt::camera_ok(camera, why) || !layout_ok(field_mask, rec_size, offs, why))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: " + why);
+		if (!d_out)
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits_camera: null output");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		const prt_b200_camera cam = *camera;
+		return queue_query(ctx, nullptr, (uint64_t)cam.width * cam.height, field_mask, rec_size,
+		                   offs, d_out, stream, &cam);
+	});
 }
 
 int prt_b200_sync(prt_b200_ctx *ctx) {
@@ -403,118 +411,120 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
                           uint32_t rec_size, const uint8_t offs[8], void *out_host) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	std::string why;
-	if (!layout_ok(field_mask, rec_size, offs, why))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
-	if (n && (!rays6 || !out_host))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	if (!ctx->scene_set)
-		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
-	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits: compressed nodes were not built");
-	if (n == 0)
-		return PRT_OK;
-	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-	prt::OutLayout lay;
-	lay.mask = field_mask;
-	lay.rec_size = rec_size;
-	std::memcpy(lay.off, offs, 8);
-	prt::TravConfig cfg;
-	cfg.format = ctx->node_format;
-	cfg.block = ctx->block;
-	cfg.count = ctx->count;
-	// In place when the device can reach both buffers: the traversal reads each ray from
-	// host memory once and writes each record there once, over the host link, with no
-	// staging buffers and nothing to overlap.  The traversal reads rays as 8-byte pairs,
-	// so rays that are only 4-byte aligned (a float array at an odd index) are copied
-	// into the aligned staging buffer instead; records may have any alignment.
-	if (ctx->host_direct) {
-		const void *d_in = device_alias(ctx, rays6);
-		if (reinterpret_cast<uintptr_t>(d_in) % 8 != 0)
-			d_in = nullptr;
-		void *d_out = d_in ? device_alias(ctx, out_host) : nullptr;
-		ctx->last_in_place = d_in && d_out;
-		if (d_in && d_out) {
-			CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, static_cast<const float *>(d_in),
-			                                       n, lay, d_out, cfg, ctx->d_work(),
-			                                       ctx->d_visits(), ctx->d_err(), ctx->stream,
-			                                       ctx->sms));
-			if (ctx->count)
-				CAPI_TRY(ctx, cudaMemcpyAsync(ctx->visits, ctx->d_visits(), 16,
-				                              cudaMemcpyDeviceToHost, ctx->stream));
-			// One wait: the error word's copy is queued after the traversal.
-			return check_device_errors(ctx);
+	return prt::guarded(&ctx->err, "nearest_hits", [&]() -> int {
+		std::string why;
+		if (!layout_ok(field_mask, rec_size, offs, why))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: " + why);
+		if (n && (!rays6 || !out_host))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: null buffer");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		if (!ctx->scene_set)
+			return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits: set_tris has not succeeded");
+		if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits: compressed nodes were not built");
+		if (n == 0)
+			return PRT_OK;
+		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+		prt::OutLayout lay;
+		lay.mask = field_mask;
+		lay.rec_size = rec_size;
+		std::memcpy(lay.off, offs, 8);
+		prt::TravConfig cfg;
+		cfg.format = ctx->node_format;
+		cfg.block = ctx->block;
+		cfg.count = ctx->count;
+		// In place when the device can reach both buffers: the traversal reads each ray from
+		// host memory once and writes each record there once, over the host link, with no
+		// staging buffers and nothing to overlap.  The traversal reads rays as 8-byte pairs,
+		// so rays that are only 4-byte aligned (a float array at an odd index) are copied
+		// into the aligned staging buffer instead; records may have any alignment.
+		if (ctx->host_direct) {
+			const void *d_in = device_alias(ctx, rays6);
+			if (reinterpret_cast<uintptr_t>(d_in) % 8 != 0)
+				d_in = nullptr;
+			void *d_out = d_in ? device_alias(ctx, out_host) : nullptr;
+			ctx->last_in_place = d_in && d_out;
+			if (d_in && d_out) {
+				CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, static_cast<const float *>(d_in),
+				                                       n, lay, d_out, cfg, ctx->d_work(),
+				                                       ctx->d_visits(), ctx->d_err(), ctx->stream,
+				                                       ctx->sms));
+				if (ctx->count)
+					CAPI_TRY(ctx, cudaMemcpyAsync(ctx->visits, ctx->d_visits(), 16,
+					                              cudaMemcpyDeviceToHost, ctx->stream));
+				// One wait: the error word's copy is queued after the traversal.
+				return check_device_errors(ctx);
+			}
 		}
-	}
-	ctx->last_in_place = false;
-	CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
-	CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
-	// Chunks: pipe_chunks of them (fewer when a chunk would hold under pipe_min_rays), one
-	// when the visit counters are on (each launch would reset them).  With pipe_ramp the
-	// sizes ramp up and down (weights 1, 2, 4, 8, ..., 8, 4, 2, 1), so the copy-in of the
-	// first chunk and the copy-out of the last, which nothing overlaps, are short.  Chunk
-	// c is copied in on s_in, traversed on stream c % 2 (so a chunk's last blocks overlap
-	// the next chunk's first) and copied out on s_out.  Every chunk has its own rays,
-	// records and events; the two compute streams have their own ray counters.
-	int nc = ctx->count ? 1 : ctx->pipe_chunks;
-	if (nc > 1 && n / (uint64_t)nc < ctx->pipe_min_rays)
-		nc = (int)std::max<uint64_t>(1, n / ctx->pipe_min_rays);
-	uint64_t bnd[prt_b200_ctx::kPipe + 1];
-	{
-		uint32_t w[prt_b200_ctx::kPipe], total = 0;
-		for (int i = 0; i < nc; ++i) {
-			w[i] = ctx->pipe_ramp ? 1u << std::min(std::min(i, nc - 1 - i), 3) : 1u;
-			total += w[i];
+		ctx->last_in_place = false;
+		CAPI_TRY(ctx, ctx->rays_buf.reserve(24ull * n));
+		CAPI_TRY(ctx, ctx->out_buf.reserve((uint64_t)rec_size * n));
+		// Chunks: pipe_chunks of them (fewer when a chunk would hold under pipe_min_rays), one
+		// when the visit counters are on (each launch would reset them).  With pipe_ramp the
+		// sizes ramp up and down (weights 1, 2, 4, 8, ..., 8, 4, 2, 1), so the copy-in of the
+		// first chunk and the copy-out of the last, which nothing overlaps, are short.  Chunk
+		// c is copied in on s_in, traversed on stream c % 2 (so a chunk's last blocks overlap
+		// the next chunk's first) and copied out on s_out.  Every chunk has its own rays,
+		// records and events; the two compute streams have their own ray counters.
+		int nc = ctx->count ? 1 : ctx->pipe_chunks;
+		if (nc > 1 && n / (uint64_t)nc < ctx->pipe_min_rays)
+			nc = (int)std::max<uint64_t>(1, n / ctx->pipe_min_rays);
+		uint64_t bnd[prt_b200_ctx::kPipe + 1];
+		{
+			uint32_t w[prt_b200_ctx::kPipe], total = 0;
+			for (int i = 0; i < nc; ++i) {
+				w[i] = ctx->pipe_ramp ? 1u << std::min(std::min(i, nc - 1 - i), 3) : 1u;
+				total += w[i];
+			}
+			bnd[0] = 0;
+			uint64_t cum = 0;
+			for (int i = 0; i < nc; ++i) {
+				cum += w[i];
+				bnd[i + 1] = (i + 1 == nc) ? n : ((unsigned __int128)n * cum / total) & ~31ull;
+			}
 		}
-		bnd[0] = 0;
-		uint64_t cum = 0;
-		for (int i = 0; i < nc; ++i) {
-			cum += w[i];
-			bnd[i + 1] = (i + 1 == nc) ? n : ((unsigned __int128)n * cum / total) & ~31ull;
+		cudaStream_t ks[2] = {ctx->stream, ctx->s_k2};
+		uint32_t *ctr[2] = {ctx->d_work(), ctx->d_work() + 8};
+		// Earlier work of the context's stream (a _dev call) finishes before the chunks start.
+		CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[0], ctx->stream));
+		for (cudaStream_t st : {ctx->s_in, ctx->s_out, ctx->s_k2})
+			CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_k[0], 0));
+		const uint8_t *rin = reinterpret_cast<const uint8_t *>(rays6);
+		uint8_t *rout = static_cast<uint8_t *>(out_host);
+		for (int c = 0; c <= nc; ++c) {
+			if (c < nc) {
+				const uint64_t b = bnd[c], m = bnd[c + 1] - bnd[c];
+				CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.as<uint8_t>() + 24 * b, rin + 24 * b,
+				                              24 * m, cudaMemcpyHostToDevice, ctx->s_in));
+				CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[c], ctx->s_in));
+				cudaStream_t st = ks[c & 1];
+				CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_in[c], 0));
+				CAPI_TRY(ctx, prt::launch_nearest_hits(
+				                  ctx->scene, ctx->rays_buf.as<float>() + 6 * b, m, lay,
+				                  ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b, cfg, ctr[c & 1],
+				                  ctx->d_visits(), ctx->d_err(), st, ctx->sms));
+				CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[c], st));
+			}
+			// The copy-out of the chunk before is queued after this chunk's copy-in, so that
+			// with pageable host memory (where the copy calls return only when done) the
+			// copy-in still overlaps the traversal.
+			if (c > 0) {
+				const uint64_t b = bnd[c - 1], m = bnd[c] - bnd[c - 1];
+				CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->s_out, ctx->ev_k[c - 1], 0));
+				CAPI_TRY(ctx, cudaMemcpyAsync(rout + (uint64_t)rec_size * b,
+				                              ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b,
+				                              (uint64_t)rec_size * m, cudaMemcpyDeviceToHost,
+				                              ctx->s_out));
+			}
 		}
-	}
-	cudaStream_t ks[2] = {ctx->stream, ctx->s_k2};
-	uint32_t *ctr[2] = {ctx->d_work(), ctx->d_work() + 8};
-	// Earlier work of the context's stream (a _dev call) finishes before the chunks start.
-	CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[0], ctx->stream));
-	for (cudaStream_t st : {ctx->s_in, ctx->s_out, ctx->s_k2})
-		CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_k[0], 0));
-	const uint8_t *rin = reinterpret_cast<const uint8_t *>(rays6);
-	uint8_t *rout = static_cast<uint8_t *>(out_host);
-	for (int c = 0; c <= nc; ++c) {
-		if (c < nc) {
-			const uint64_t b = bnd[c], m = bnd[c + 1] - bnd[c];
-			CAPI_TRY(ctx, cudaMemcpyAsync(ctx->rays_buf.as<uint8_t>() + 24 * b, rin + 24 * b,
-			                              24 * m, cudaMemcpyHostToDevice, ctx->s_in));
-			CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[c], ctx->s_in));
-			cudaStream_t st = ks[c & 1];
-			CAPI_TRY(ctx, cudaStreamWaitEvent(st, ctx->ev_in[c], 0));
-			CAPI_TRY(ctx, prt::launch_nearest_hits(
-			                  ctx->scene, ctx->rays_buf.as<float>() + 6 * b, m, lay,
-			                  ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b, cfg, ctr[c & 1],
-			                  ctx->d_visits(), ctx->d_err(), st, ctx->sms));
-			CAPI_TRY(ctx, cudaEventRecord(ctx->ev_k[c], st));
-		}
-		// The copy-out of the chunk before is queued after this chunk's copy-in, so that
-		// with pageable host memory (where the copy calls return only when done) the
-		// copy-in still overlaps the traversal.
-		if (c > 0) {
-			const uint64_t b = bnd[c - 1], m = bnd[c] - bnd[c - 1];
-			CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->s_out, ctx->ev_k[c - 1], 0));
-			CAPI_TRY(ctx, cudaMemcpyAsync(rout + (uint64_t)rec_size * b,
-			                              ctx->out_buf.as<uint8_t>() + (uint64_t)rec_size * b,
-			                              (uint64_t)rec_size * m, cudaMemcpyDeviceToHost,
-			                              ctx->s_out));
-		}
-	}
-	// s_out waited for every chunk's traversal; the context's stream waits for s_out.
-	CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[0], ctx->s_out));
-	CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[0], 0));
-	CAPI_TRY(ctx, cudaStreamSynchronize(ctx->s_out));
-	if (ctx->count)
-		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
-	return check_device_errors(ctx);
+		// s_out waited for every chunk's traversal; the context's stream waits for s_out.
+		CAPI_TRY(ctx, cudaEventRecord(ctx->ev_in[0], ctx->s_out));
+		CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->stream, ctx->ev_in[0], 0));
+		CAPI_TRY(ctx, cudaStreamSynchronize(ctx->s_out));
+		if (ctx->count)
+			CAPI_TRY(ctx, cudaMemcpy(ctx->visits, ctx->d_visits(), 16, cudaMemcpyDeviceToHost));
+		return check_device_errors(ctx);
+	});
 }
 
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {

@@ -4,7 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <exception>
 #include <mutex>
+#include <new>
 #include <string>
 #include <utility>
 #include <vector>
@@ -95,6 +97,39 @@ namespace prt {
 // first use): record ->ev on the stream after the work, and set_tris waits for it.
 // Caller holds the context's lock.
 int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out);
+
+// Runs the body of a C entry point and turns a C++ exception (host memory exhausted, a
+// thread that could not start) into PRT_ERR_OOM with a message in *err, so that no
+// exception crosses the C boundary.  When `capture` is a stream the body left
+// capturing, the capture is ended and its graph dropped, so the stream stays usable.
+template <class F>
+int guarded(ErrorText *err, const char *what, F &&body, cudaStream_t capture = nullptr) noexcept {
+	const char *why = "out of host memory";
+	try {
+		return body();
+	} catch (const std::bad_alloc &) {
+	} catch (const std::exception &ex) {
+		why = ex.what();
+	} catch (...) {
+		why = "unexpected exception";
+	}
+	if (capture) {
+		cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+		if (cudaStreamIsCapturing(capture, &cs) == cudaSuccess &&
+		    cs != cudaStreamCaptureStatusNone) {
+			cudaGraph_t g = nullptr;
+			if (cudaStreamEndCapture(capture, &g) == cudaSuccess && g)
+				cudaGraphDestroy(g);
+		}
+		cudaGetLastError();
+	}
+	try {
+		if (err)
+			*err = std::string(what) + ": " + why;
+	} catch (...) {
+	}
+	return PRT_ERR_OOM;
+}
 
 // Validates a HitReg layout descriptor.
 inline bool layout_ok(uint32_t mask, uint32_t rec, const uint8_t *off, std::string &why) {

@@ -31,8 +31,10 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <memory>
 #include <mutex>
+#include <new>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -318,6 +320,26 @@ void completer(prt_b200_server *s, Lane *L) {
 	}
 }
 
+// Frees a lane's stream, event and buffers (its threads have stopped).
+void release_lane(Lane &L) {
+	if (L.st)
+		cudaStreamSynchronize(L.st);
+	L.segs.release();
+	L.work.release();
+	if (L.h_segs)
+		cudaFreeHost(L.h_segs);
+	if (L.h_err)
+		cudaFreeHost(L.h_err);
+	if (L.ev)
+		cudaEventDestroy(L.ev);
+	if (L.st)
+		cudaStreamDestroy(L.st);
+	L.h_segs = nullptr;
+	L.h_err = nullptr;
+	L.ev = nullptr;
+	L.st = nullptr;
+}
+
 void shutdown(prt_b200_server *s) {
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
@@ -375,7 +397,11 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 	if (e == cudaSuccess)
 		e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
 	for (uint32_t i = 0; i < n_lanes && e == cudaSuccess; ++i) {
-		std::unique_ptr<Lane> L(new Lane());
+		std::unique_ptr<Lane> L(new (std::nothrow) Lane());
+		if (!L) {
+			e = cudaErrorMemoryAllocation;
+			break;
+		}
 		// Lane 0 of several is the express lane: the highest stream priority.
 		e = cudaStreamCreateWithPriority(&L->st, cudaStreamNonBlocking,
 		                                 (i == 0 && n_lanes > 1) ? greatest : least);
@@ -391,7 +417,16 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 			e = cudaMallocHost(&L->h_segs, sizeof(prt::SegDesc) * kMaxWaveRequests);
 		if (e == cudaSuccess)
 			e = cudaMallocHost(&L->h_err, 16);
-		s->lanes.push_back(std::move(L));
+		// A wave holds at most kMaxWaveRequests requests: with the room reserved here the
+		// scheduler thread never allocates to fill one.
+		try {
+			L->wave.reserve(kMaxWaveRequests);
+			s->lanes.push_back(std::move(L));
+		} catch (const std::bad_alloc &) {
+			if (L) // not yet owned by the server: free what it holds
+				release_lane(*L);
+			e = cudaErrorMemoryAllocation;
+		}
 	}
 	if (e != cudaSuccess) {
 		std::lock_guard<std::mutex> lk(ctx->mu);
@@ -400,9 +435,19 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		return e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA;
 	}
 	prt_b200_server *sp = s.get();
-	for (auto &l : sp->lanes)
-		l->completer = std::thread(completer, sp, l.get());
-	sp->sched = std::thread(scheduler, sp);
+	try {
+		for (auto &l : sp->lanes)
+			l->completer = std::thread(completer, sp, l.get());
+		sp->sched = std::thread(scheduler, sp);
+	} catch (const std::exception &ex) {
+		// A thread that could not start: stop those that did and free everything.
+		{
+			std::lock_guard<std::mutex> lk(ctx->mu);
+			ctx->err = std::string("server create: ") + ex.what();
+		}
+		prt_b200_server_destroy(s.release());
+		return PRT_ERR_OOM;
+	}
 	*out = s.release();
 	return PRT_OK;
 }
@@ -412,20 +457,8 @@ void prt_b200_server_destroy(prt_b200_server *s) {
 		return;
 	shutdown(s);
 	cudaSetDevice(s->ctx->device);
-	for (auto &l : s->lanes) {
-		if (l->st)
-			cudaStreamSynchronize(l->st);
-		l->segs.release();
-		l->work.release();
-		if (l->h_segs)
-			cudaFreeHost(l->h_segs);
-		if (l->h_err)
-			cudaFreeHost(l->h_err);
-		if (l->ev)
-			cudaEventDestroy(l->ev);
-		if (l->st)
-			cudaStreamDestroy(l->st);
-	}
+	for (auto &l : s->lanes)
+		release_lane(*l);
 	for (auto &kv : s->reqs)
 		delete kv.second;
 	s->region.release();
@@ -465,16 +498,30 @@ int prt_b200_server_submit(prt_b200_server *s, uint32_t scene, const float *rays
 		return sfail(s, PRT_ERR_ARG, "server submit: server is stopping");
 	if (n && !s->alloc.fits_ever(r->bytes))
 		return sfail(s, PRT_ERR_LIMIT, "server submit: request larger than the memory budget");
-	r->id = s->next_id++;
+	// Host memory for the ticket table or the queue may run out: the request is then
+	// neither queued nor given a ticket, and the call returns PRT_ERR_OOM.
+	r->id = s->next_id;
 	r->t_submit = Clock::now();
+	try {
+		auto ins = s->reqs.emplace(r->id, r.get());
+		if (n) {
+			try {
+				s->waiting.push_back(r.get());
+			} catch (...) {
+				s->reqs.erase(ins.first);
+				throw;
+			}
+		}
+	} catch (const std::bad_alloc &) {
+		return sfail(s, PRT_ERR_OOM, "server submit: out of host memory");
+	}
+	++s->next_id;
 	*ticket = r->id;
 	Request *rp = r.release();
-	s->reqs[rp->id] = rp;
 	if (n == 0) {
 		rp->t_done = rp->t_submit;
 		rp->done = true;
 	} else {
-		s->waiting.push_back(rp);
 		s->cv_sched.notify_one();
 	}
 	return PRT_OK;
