@@ -104,3 +104,39 @@ def test_python_registry_mirrors_the_reference():
             backend.nearest_hits(np.zeros((1, 6), np.float32))
     finally:
         backend.selected_backend = saved
+
+
+def test_exceptions_become_statuses(tmp_path):
+    """The guard every C entry point runs its body under (prt_ctx.cuh): a body that runs
+    out of host memory, or throws anything else, returns PRT_ERR_OOM with a message
+    instead of letting the exception cross the C boundary; a body that returns passes
+    its status through.  Host code only (no CUDA call is made)."""
+    from portablert_gb300 import build as b
+
+    src = tmp_path / "g.cu"
+    src.write_text(
+        '#include <cstdio>\n#include <new>\n#include <stdexcept>\n'
+        f'#include "{os.path.join(ROOT, "portablert_gb300", "csrc", "prt_ctx.cuh")}"\n'
+        'int main() {\n'
+        '  prt::ErrorText err;\n'
+        '  int a = prt::guarded(&err, "one", [&]() -> int { throw std::bad_alloc(); });\n'
+        '  std::string ma = err.get();\n'
+        '  int b = prt::guarded(&err, "two", [&]() -> int { throw std::runtime_error("x"); });\n'
+        '  std::string mb = err.get();\n'
+        '  int c = prt::guarded(&err, "three", [&]() -> int { throw 7; });\n'
+        '  std::string mc = err.get();\n'
+        '  int d = prt::guarded(&err, "four", [&]() -> int { return PRT_ERR_LIMIT; });\n'
+        '  int e = prt::guarded(nullptr, "five", [&]() -> int { throw std::bad_alloc(); });\n'
+        '  std::printf("%d %d %d %d %d|%s|%s|%s\\n", a, b, c, d, e, ma.c_str(), mb.c_str(),'
+        ' mc.c_str());\n'
+        '  return 0;\n}\n')
+    exe = tmp_path / "g"
+    r = subprocess.run([b.nvcc(), "-std=c++17", str(src), "-o", str(exe)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.strip()
+    codes, ma, mb, mc = out.split("|")
+    assert codes.split() == ["6", "6", "6", "7", "6"]
+    assert ma == "one: out of host memory"
+    assert mb == "two: x"
+    assert mc == "three: unexpected exception"
