@@ -74,6 +74,23 @@ int check_device_errors(prt_b200_ctx *ctx) {
 	return PRT_OK;
 }
 
+// The record layout of a call, and the traversal settings of the context's options.
+prt::OutLayout out_layout(uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8]) {
+	prt::OutLayout lay;
+	lay.mask = field_mask;
+	lay.rec_size = rec_size;
+	std::memcpy(lay.off, offs, 8);
+	return lay;
+}
+
+prt::TravConfig trav_config(const prt_b200_ctx *ctx) {
+	prt::TravConfig cfg;
+	cfg.format = ctx->node_format;
+	cfg.block = ctx->block;
+	cfg.count = ctx->count;
+	return cfg;
+}
+
 int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	// Queries still reading the old scene on callers' streams finish before the
 	// rebuild overwrites its arrays.
@@ -305,14 +322,8 @@ int queue_query(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n, uint32_t fi
 	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
 	if (n == 0)
 		return PRT_OK;
-	prt::OutLayout lay;
-	lay.mask = field_mask;
-	lay.rec_size = rec_size;
-	std::memcpy(lay.off, offs, 8);
-	prt::TravConfig cfg;
-	cfg.format = ctx->node_format;
-	cfg.block = ctx->block;
-	cfg.count = ctx->count;
+	const prt::OutLayout lay = out_layout(field_mask, rec_size, offs);
+	const prt::TravConfig cfg = trav_config(ctx);
 	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
 	prt_b200_ctx::QueryStream *qs = nullptr;
 	if (st != ctx->stream) {
@@ -425,14 +436,8 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 		if (n == 0)
 			return PRT_OK;
 		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-		prt::OutLayout lay;
-		lay.mask = field_mask;
-		lay.rec_size = rec_size;
-		std::memcpy(lay.off, offs, 8);
-		prt::TravConfig cfg;
-		cfg.format = ctx->node_format;
-		cfg.block = ctx->block;
-		cfg.count = ctx->count;
+		const prt::OutLayout lay = out_layout(field_mask, rec_size, offs);
+		const prt::TravConfig cfg = trav_config(ctx);
 		// In place when the device can reach both buffers: the traversal reads each ray from
 		// host memory once and writes each record there once, over the host link, with no
 		// staging buffers and nothing to overlap.  The traversal reads rays as 8-byte pairs,
@@ -706,14 +711,8 @@ extern "C" int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *ray
 	cudaStream_t st = ctx->stream;
 	CAPI_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoallocWork, st));
 	CAPI_TRY(ctx, cudaMemcpyAsync(d_rays, rays6, 24ull * n, cudaMemcpyHostToDevice, st));
-	prt::OutLayout lay;
-	lay.mask = field_mask;
-	lay.rec_size = rec_size;
-	std::memcpy(lay.off, offs, 8);
-	prt::TravConfig cfg;
-	cfg.format = ctx->node_format;
-	cfg.block = ctx->block;
-	cfg.count = ctx->count;
+	const prt::OutLayout lay = out_layout(field_mask, rec_size, offs);
+	const prt::TravConfig cfg = trav_config(ctx);
 	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays, n, lay, d_out, cfg, d_work,
 	                                       d_visits, d_err, st, ctx->sms));
 	CAPI_TRY(ctx, cudaMemcpyAsync(out_host, d_out, (uint64_t)rec_size * n, cudaMemcpyDeviceToHost,
