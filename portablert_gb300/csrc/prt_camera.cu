@@ -157,52 +157,54 @@ int prt_b200_shade_lambert(prt_b200_ctx *ctx, const prt_b200_camera *camera,
                            uint8_t *d_rgba, void *stream) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	std::string why;
-	if (!prt::layout_ok(field_mask, rec_size, offs, why))
-		return cfail(ctx, PRT_ERR_ARG, "shade_lambert: " + why);
-	if ((field_mask & (PRT_FIELD_T | PRT_FIELD_PRIMITIVE_ID)) !=
-	    (PRT_FIELD_T | PRT_FIELD_PRIMITIVE_ID))
-		return cfail(ctx, PRT_ERR_ARG, "shade_lambert: records need t and primitive_id");
-	if (camera) {
-		if (!camera_ok(camera, why))
+	return prt::guarded(&ctx->err, "shade_lambert", [&]() -> int {
+		std::string why;
+		if (!prt::layout_ok(field_mask, rec_size, offs, why))
 			return cfail(ctx, PRT_ERR_ARG, "shade_lambert: " + why);
-		n = (uint64_t)camera->width * camera->height;
-	} else if (n && !d_rays6) {
-		return cfail(ctx, PRT_ERR_ARG, "shade_lambert: no camera and no rays");
-	}
-	if (n && (!d_records || !d_rgba))
-		return cfail(ctx, PRT_ERR_ARG, "shade_lambert: null buffer");
-	if (reinterpret_cast<uintptr_t>(d_rgba) % 4 != 0 ||
-	    reinterpret_cast<uintptr_t>(d_records) % 4 != 0)
-		return cfail(ctx, PRT_ERR_ARG, "shade_lambert: buffers must be 4-byte aligned");
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	if (!ctx->scene_set)
-		return cfail(ctx, PRT_ERR_NO_SCENE, "shade_lambert: set_tris has not succeeded");
-	cudaError_t e = cudaSetDevice(ctx->device);
-	if (e != cudaSuccess || n == 0)
-		return e == cudaSuccess ? PRT_OK : cuda_fail(ctx, e, "shade_lambert");
-	cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
-	prt_b200_camera c{};
-	if (camera)
-		c = *camera;
-	const prt::SceneGPU &sc = ctx->scene;
-	k_lambert<<<grid_for(n, ctx->sms), 256, 0, st>>>(
-	    sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), sc.n_tris, c, camera ? 1u : 0u, d_rays6, n,
-	    static_cast<const uint8_t *>(d_records), rec_size, offs[PRT_OFF_T], offs[PRT_OFF_PID],
-	    reinterpret_cast<uchar4 *>(d_rgba));
-	e = cudaGetLastError();
-	if (e != cudaSuccess)
-		return cuda_fail(ctx, e, "shade_lambert");
-	if (st != ctx->stream) { // a rebuild waits for this read of the scene
-		prt_b200_ctx::QueryStream *qs = nullptr;
-		const int rc = prt::query_stream(ctx, st, &qs);
-		if (rc != PRT_OK)
-			return rc;
-		e = cudaEventRecord(qs->ev, st);
+		if ((field_mask & (PRT_FIELD_T | PRT_FIELD_PRIMITIVE_ID)) !=
+		    (PRT_FIELD_T | PRT_FIELD_PRIMITIVE_ID))
+			return cfail(ctx, PRT_ERR_ARG, "shade_lambert: records need t and primitive_id");
+		if (camera) {
+			if (!camera_ok(camera, why))
+				return cfail(ctx, PRT_ERR_ARG, "shade_lambert: " + why);
+			n = (uint64_t)camera->width * camera->height;
+		} else if (n && !d_rays6) {
+			return cfail(ctx, PRT_ERR_ARG, "shade_lambert: no camera and no rays");
+		}
+		if (n && (!d_records || !d_rgba))
+			return cfail(ctx, PRT_ERR_ARG, "shade_lambert: null buffer");
+		if (reinterpret_cast<uintptr_t>(d_rgba) % 4 != 0 ||
+		    reinterpret_cast<uintptr_t>(d_records) % 4 != 0)
+			return cfail(ctx, PRT_ERR_ARG, "shade_lambert: buffers must be 4-byte aligned");
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		if (!ctx->scene_set)
+			return cfail(ctx, PRT_ERR_NO_SCENE, "shade_lambert: set_tris has not succeeded");
+		cudaError_t e = cudaSetDevice(ctx->device);
+		if (e != cudaSuccess || n == 0)
+			return e == cudaSuccess ? PRT_OK : cuda_fail(ctx, e, "shade_lambert");
+		cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+		prt_b200_camera c{};
+		if (camera)
+			c = *camera;
+		const prt::SceneGPU &sc = ctx->scene;
+		k_lambert<<<grid_for(n, ctx->sms), 256, 0, st>>>(
+		    sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), sc.n_tris, c, camera ? 1u : 0u, d_rays6, n,
+		    static_cast<const uint8_t *>(d_records), rec_size, offs[PRT_OFF_T], offs[PRT_OFF_PID],
+		    reinterpret_cast<uchar4 *>(d_rgba));
+		e = cudaGetLastError();
 		if (e != cudaSuccess)
 			return cuda_fail(ctx, e, "shade_lambert");
-	}
-	return PRT_OK;
+		if (st != ctx->stream) { // a rebuild waits for this read of the scene
+			prt_b200_ctx::QueryStream *qs = nullptr;
+			const int rc = prt::query_stream(ctx, st, &qs);
+			if (rc != PRT_OK)
+				return rc;
+			e = cudaEventRecord(qs->ev, st);
+			if (e != cudaSuccess)
+				return cuda_fail(ctx, e, "shade_lambert");
+		}
+		return PRT_OK;
+	});
 }
 
 } // extern "C"
