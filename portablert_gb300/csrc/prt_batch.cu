@@ -257,10 +257,9 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 		}
 		drop_graph(b);
 		b->built = false;
-		cudaEvent_t e0, e1;
-		B_TRY(ctx, cudaEventCreate(&e0));
-		B_TRY(ctx, cudaEventCreate(&e1));
-		cudaEventRecord(e0, ctx->stream);
+		prt::EventPair ev;
+		B_TRY(ctx, ev.create());
+		cudaEventRecord(ev.a, ctx->stream);
 		std::string msg;
 		// Binned-SAH trees as set_tris builds them (option build_sah); a tree too deep for
 		// the collapse falls back to the LBVH.  Graph builds (run_graph) are always LBVH.
@@ -276,13 +275,8 @@ int prt_b200_batch_set_tris_dev(prt_b200_batch *b, const float *d_tris, const ui
 			                       ctx->collapse_cost);
 		}
 		b->built_sah = sah;
-		cudaEventRecord(e1, ctx->stream);
-		cudaEventSynchronize(e1);
-		float ms = 0.0f;
-		cudaEventElapsedTime(&ms, e0, e1);
-		cudaEventDestroy(e0);
-		cudaEventDestroy(e1);
-		b->build_ms = ms;
+		cudaEventRecord(ev.b, ctx->stream);
+		b->build_ms = ev.elapsed_ms();
 		if (rc != PRT_OK)
 			return bfail(ctx, rc, msg);
 		uint32_t err_word = 0;

@@ -96,10 +96,9 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	// rebuild overwrites its arrays.
 	for (auto &q : ctx->query_streams)
 		CAPI_TRY(ctx, cudaStreamWaitEvent(ctx->stream, q.ev, 0));
-	cudaEvent_t e0, e1;
-	CAPI_TRY(ctx, cudaEventCreate(&e0));
-	CAPI_TRY(ctx, cudaEventCreate(&e1));
-	cudaEventRecord(e0, ctx->stream);
+	prt::EventPair ev;
+	CAPI_TRY(ctx, ev.create());
+	cudaEventRecord(ev.a, ctx->stream);
 	std::string msg;
 	bool sah = ctx->build_sah;
 	int rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
@@ -112,13 +111,8 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 		                      ctx->ws, ctx->stream, ctx->d_err(), msg, false, ctx->collapse_cost);
 	}
 	ctx->last_build_sah = sah;
-	cudaEventRecord(e1, ctx->stream);
-	cudaEventSynchronize(e1);
-	float ms = 0.0f;
-	cudaEventElapsedTime(&ms, e0, e1);
-	cudaEventDestroy(e0);
-	cudaEventDestroy(e1);
-	ctx->build_ms = ms;
+	cudaEventRecord(ev.b, ctx->stream);
+	ctx->build_ms = ev.elapsed_ms();
 	ctx->scene_set = false;
 	if (rc != PRT_OK)
 		return fail(ctx, rc, msg);
@@ -145,6 +139,8 @@ int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream *
 			*out = &q;
 			return PRT_OK;
 		}
+	// Room first: a failed host allocation then leaves no event or counter behind.
+	ctx->query_streams.reserve(ctx->query_streams.size() + 1);
 	prt_b200_ctx::QueryStream q{st, nullptr, nullptr};
 	CAPI_TRY(ctx, cudaEventCreateWithFlags(&q.ev, cudaEventDisableTiming));
 	cudaError_t e = cudaMalloc(&q.counter, 64);

@@ -98,6 +98,31 @@ namespace prt {
 // Caller holds the context's lock.
 int query_stream(prt_b200_ctx *ctx, cudaStream_t st, prt_b200_ctx::QueryStream **out);
 
+// Two timing events around work queued on a stream, destroyed however the scope ends.
+struct EventPair {
+	cudaEvent_t a = nullptr, b = nullptr;
+	cudaError_t create() {
+		cudaError_t e = cudaEventCreate(&a);
+		return e == cudaSuccess ? cudaEventCreate(&b) : e;
+	}
+	// Milliseconds between the two (after b has been recorded), 0 if unavailable.
+	float elapsed_ms() const {
+		float ms = 0.0f;
+		if (cudaEventSynchronize(b) != cudaSuccess || cudaEventElapsedTime(&ms, a, b) != cudaSuccess)
+			ms = 0.0f;
+		return ms;
+	}
+	EventPair() = default;
+	EventPair(const EventPair &) = delete;
+	EventPair &operator=(const EventPair &) = delete;
+	~EventPair() {
+		if (a)
+			cudaEventDestroy(a);
+		if (b)
+			cudaEventDestroy(b);
+	}
+};
+
 // Runs the body of a C entry point and turns a C++ exception (host memory exhausted, a
 // thread that could not start) into PRT_ERR_OOM with a message in *err, so that no
 // exception crosses the C boundary.  When `capture` is a stream the body left
