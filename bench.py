@@ -770,6 +770,9 @@ def run_gpu(args, world, rank):
     achieved = n * b_ray / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
     traffic = committed_profile("dram_bytes_per_launch")
+    # What DRAM itself carries: the profiled bytes of one launch over its live duration
+    # (node fetches the L2 serves are in the algorithmic bytes, not here).
+    dram = traffic / per_launch_s / 1e9 if traffic else None
     # The bytes a ray must move at least (its 24-byte ray in, its record out).
     io_floor = n * (24 + lay.size) / per_launch_s / 1e9
 
@@ -844,6 +847,7 @@ def run_gpu(args, world, rank):
                         "bytes_per_ray": b_ray, "node_visits_per_ray": v_nodes,
                         "tri_tests_per_ray": v_tris, "node_bytes": node_size,
                         "io_floor_gbs": io_floor, "io_floor_frac": io_floor / peak,
+                        "dram_gbs": dram, "dram_frac": dram / peak if dram else None,
                         "l2_hit_rate_pct": committed_profile("l2_hit_rate_pct")},
            "build": {"mtris_s_device": len(tris) / build_dev_ms / 1e3,
                      "mtris_s_e2e": len(tris) / build_e2e_ms / 1e3,
