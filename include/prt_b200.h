@@ -94,9 +94,10 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n,
                           uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
                           void *out_host);
 
-/* Device-resident variant: d_rays6 and d_out are device pointers; the work is queued
- * on `stream` (a cudaStream_t, NULL = the context's stream) and the call returns
- * without waiting.  prt_b200_sync waits and reports kernel-side errors. */
+/* Device-resident variant: d_rays6 and d_out are device pointers (d_rays6 8-byte
+ * aligned, else PRT_ERR_ARG; d_out any alignment); the work is queued on `stream` (a
+ * cudaStream_t, NULL = the context's stream) and the call returns without waiting.
+ * prt_b200_sync waits and reports kernel-side errors. */
 int prt_b200_nearest_hits_dev(prt_b200_ctx *ctx, const float *d_rays6, uint64_t n,
                               uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
                               void *d_out, void *stream);
