@@ -70,7 +70,7 @@ int prt_b200_create(int device, prt_b200_ctx **out);
 void prt_b200_destroy(prt_b200_ctx *ctx);
 
 /* Message of the last failing call on ctx ("" if none).  With ctx == NULL: the last
- * failure of prt_b200_create or prt_b200_obj_load in this thread.  The string is the
+ * failure of prt_b200_create, prt_b200_obj_load or prt_b200_gltf_load in this thread.  The string is the
  * calling thread's copy, valid until its next call of this function. */
 const char *prt_b200_last_error(const prt_b200_ctx *ctx);
 
@@ -288,6 +288,15 @@ int prt_b200_shade_lambert(prt_b200_ctx *ctx, const prt_b200_camera *camera,
  * *tris9 is allocated by the library (free it with prt_b200_free); errors are reported
  * by prt_b200_last_error(NULL).  Host only: needs no device. */
 int prt_b200_obj_load(const char *path, float **tris9, uint64_t *n_tris);
+
+/* Triangles of a glTF 2.0 file (.gltf with file or base64 data: buffers, or .glb), as
+ * the sponza example reads its scene for set_tris (examples/sponza/main.cpp:35-101):
+ * every mesh in order, each TRIANGLES primitive with POSITION and indices (others
+ * skipped), triangles of consecutive index triples, mesh-space positions.  byteStride
+ * is followed; an index or accessor out of range, a non-float VEC3 position, sparse
+ * accessors and required extensions are errors.  Allocation, errors and freeing as
+ * prt_b200_obj_load.  Host only: needs no device. */
+int prt_b200_gltf_load(const char *path, float **tris9, uint64_t *n_tris);
 void prt_b200_free(void *p);
 
 /* Seeded synthetic workloads written straight into device memory (no counterpart in

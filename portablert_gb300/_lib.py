@@ -24,7 +24,7 @@ EXPORTS = (
     "prt_b200_server_create", "prt_b200_server_destroy", "prt_b200_server_submit",
     "prt_b200_server_wait", "prt_b200_server_stat", "prt_b200_server_last_error",
     "prt_b200_nearest_hits_camera", "prt_b200_camera_rays", "prt_b200_shade_lambert",
-    "prt_b200_obj_load", "prt_b200_free",
+    "prt_b200_obj_load", "prt_b200_gltf_load", "prt_b200_free",
 )
 
 
@@ -120,6 +120,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_obj_load.restype = c_int
     L.prt_b200_obj_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.POINTER(ctypes.c_float)),
                                     ctypes.POINTER(c_u64)]
+    L.prt_b200_gltf_load.restype = c_int
+    L.prt_b200_gltf_load.argtypes = L.prt_b200_obj_load.argtypes
     L.prt_b200_free.restype = None
     L.prt_b200_free.argtypes = [vp]
     cp = ctypes.POINTER(Camera)

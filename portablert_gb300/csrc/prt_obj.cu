@@ -180,7 +180,8 @@ int prt_b200_obj_load(const char *path, float **tris9, uint64_t *n_tris) {
 		prt::set_global_error("obj_load: out of host memory");
 		return PRT_ERR_OOM;
 	}
-	std::memcpy(out, tris.data(), tris.size() * sizeof(float));
+	if (!tris.empty())
+		std::memcpy(out, tris.data(), tris.size() * sizeof(float));
 	*tris9 = out;
 	*n_tris = tris.size() / 9;
 	return PRT_OK;

@@ -12,10 +12,16 @@ from . import _lib
 
 def load_obj(path: str) -> np.ndarray:
     """n x 9 float32 triangles of every face (polygons as fans), in file order."""
+    return load_soup("prt_b200_obj_load", path)
+
+
+def load_soup(entry: str, path: str) -> np.ndarray:
+    """n x 9 float32 triangles from one of the library's mesh readers (`entry`: its C
+    name), copied out of the library's array, which is then freed."""
     L = _lib.load()
     p = ctypes.POINTER(ctypes.c_float)()
     n = ctypes.c_uint64()
-    rc = L.prt_b200_obj_load(str(path).encode(), ctypes.byref(p), ctypes.byref(n))
+    rc = getattr(L, entry)(str(path).encode(), ctypes.byref(p), ctypes.byref(n))
     _lib.check(rc, None, L)
     try:
         out = np.ctypeslib.as_array(p, shape=(n.value * 9,)).copy() if n.value else \
