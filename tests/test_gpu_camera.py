@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from parity import compare
-from portablert_gb300 import hitreg, obj
+from portablert_gb300 import gltf, hitreg, obj
 from portablert_gb300._lib import Camera
 
 pytestmark = pytest.mark.gpu
@@ -126,6 +126,41 @@ def test_fused_camera_traversal_and_shading(gpu_backend, oracle_lib, blob, big_b
                                           rays_ptr=d_rays.data_ptr(), n=n)
             gpu_backend.sync()
             assert np.array_equal(rgba.cpu().numpy().reshape(n, 4), want_rgba), (d, use_cam)
+
+
+def test_sponza_setup_on_a_gltf_scene(gpu_backend, oracle_lib, tmp_path):
+    """The sponza example's path end to end on a .glb scene: the glTF reader's soup,
+    set_tris, the rotating camera (form 2) fused into the traversal, and the Lambert
+    image -- records and pixels equal the oracle's on the same soup."""
+    import torch
+
+    v, f = obj.blob_mesh(40, 48, centre=(0.0, 0.0, 3.0), radius=1.0)
+    p = tmp_path / "scene.glb"
+    gltf.write_gltf(str(p), v, f, "u32", "glb")
+    mesh = gltf.load_gltf(str(p))
+    assert np.array_equal(mesh, v.astype(np.float32)[f].reshape(-1, 9))
+    gpu_backend.set_tris(mesh)
+    bvh = oracle_lib.BVH(mesh)
+    lay = hitreg.layout(TAGS)
+    d = _front_cameras(160, 100)[1]
+    n = d["width"] * d["height"]
+    cam = _ccam(d)
+    rec = torch.zeros(n * lay.size, dtype=torch.uint8, device="cuda")
+    rgba = torch.zeros(n * 4, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    gpu_backend.nearest_hits_camera(cam, rec.data_ptr(), TAGS)
+    gpu_backend.shade_lambert(rec.data_ptr(), TAGS, rgba.data_ptr(), cam=cam)
+    gpu_backend.sync()
+    got = rec.cpu().numpy().view(lay.numpy_dtype())
+    rays = _ocam(oracle_lib, d)
+    want = bvh.nearest_hits(rays)
+    assert (want["valid"] != 0).sum() > n // 50
+    rep = compare(got, want, TAGS, mesh, rays, oracle_lib)
+    assert rep["n_bad"] == 0, rep["bad"][:10]
+    hits = np.zeros(n, oracle_lib.HIT_DTYPE)
+    for k in ("t", "primitive_id", "valid"):
+        hits[k] = got[k]
+    assert np.array_equal(rgba.cpu().numpy().reshape(n, 4), oracle_lib.lambert(mesh, rays, hits))
 
 
 def test_camera_arguments_checked(gpu_backend):
