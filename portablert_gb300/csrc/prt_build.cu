@@ -4,18 +4,21 @@
 // Replaces the single-threaded binned-SAH build of portableRT (bvh.hpp:58-193).  The
 // tree's shape does not affect the answers (every triangle whose own box passes the
 // reference slab test is examined; see prt_traverse.cu), only how many boxes a ray
-// passes: set_tris builds its binary tree with binned SAH (prt_sah.cu, steps 1-5
-// replaced), batches use this fast LBVH.  Several scenes are built in the same
-// launches: scene s owns the input triangles [tri_off[s], tri_off[s+1]), its sort key
-// carries the scene index above the Morton code, its binary nodes are the range
-// [int_off[s], int_off[s+1]) and its 8-wide root is node s.
+// passes: set_tris, batch builds and servers build their binary trees with binned SAH
+// by default (prt_sah.cu, steps 1-5 replaced); graph-captured batch builds and the
+// option build_sah = 0 use this LBVH, about 3x faster to build.  Several scenes are
+// built in the same launches: scene s owns the input triangles [tri_off[s],
+// tri_off[s+1]), its sort key carries the scene index above the Morton code, its binary
+// nodes are the range [int_off[s], int_off[s+1]) and its 8-wide root is node s.
 //   1. centroid bounds per scene  (k_centroid_bounds; warp reduce + ordered-int atomics)
 //   2. 30-bit Morton codes        (k_morton; 10 bits per axis, centroids normalised)
 //   3. onesweep radix sort        (prt_sort.cu; 4 digit passes, +1 or 2 for the scene)
 //   4. Karras hierarchy           (k_karras; Karras 2012 within each scene's range)
 //   5. bottom-up refit            (k_leaf_boxes + k_refit; atomic arrival counters)
-//   6. collapse to 8-wide nodes   (k_collapse, one launch per level, per-level counters,
-//                                  so the host checks progress only every few levels)
+//   6. collapse to 8-wide nodes   (k_collapse_cost: bottom-up least expected cost per
+//                                  ray, which subtrees become nodes and which leaves;
+//                                  then k_collapse, one launch per level, per-level
+//                                  counters, so the host checks progress every few levels)
 //   7. triangle re-layout         (k_relayout; each node's leaf triangles contiguous)
 //   8. optional 8-bit encoding    (k_compress; outward-rounded child boxes)
 // A triangle with a non-finite vertex gets the box [-FLT_MAX, FLT_MAX]^3 in the tree,
