@@ -55,7 +55,7 @@ enum {
 #define PRT_OFF_PZ 7
 
 /* Acceleration-structure node formats (option "node_format"). */
-#define PRT_NODES_FP32 0       /* 8-wide nodes, FP32 child boxes (224 B) */
+#define PRT_NODES_FP32 0       /* 8-wide nodes, FP32 child boxes (256 B) */
 #define PRT_NODES_COMPRESSED 1 /* 8-wide nodes, 8-bit child boxes rounded outward (96 B) */
 
 /* Replaces CPUBackend::is_available (portableRT src/intersect_cpu.cpp:9) for this

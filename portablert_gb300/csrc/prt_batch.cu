@@ -1,6 +1,7 @@
 // prt_batch.cu - many scenes built together and queried by one persistent launch.
 //
-// A batch holds S scenes in one arena (built by the same kernels, prt_build.cu) and
+// A batch holds S scenes in one arena (built by the same kernels as one scene: binned
+// SAH, prt_sah.cu, by default; the LBVH of prt_build.cu inside a captured graph) and
 // answers a list of queries (scene, rays, output, record layout) with one launch of the
 // traversal kernel over all their rays (prt_traverse.cu, segment tables).  The build
 // and the query can be captured together in a CUDA graph and replayed.

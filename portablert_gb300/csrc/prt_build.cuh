@@ -1,4 +1,5 @@
-// prt_build.cuh - device scenes and the LBVH build pipeline (prt_build.cu).
+// prt_build.cuh - device scenes and the build pipelines (binned SAH or LBVH, then the
+// shared collapse, re-layout and compression: prt_sah.cu, prt_build.cu).
 #pragma once
 
 #include <cuda_runtime.h>

@@ -3,8 +3,9 @@
 // Data layout in HBM for one scene (n triangles):
 //   tri4   float4[3n]  triangle records in leaf order: (v0.xyz, primitive id bits),
 //                      (v1.xyz, 0), (v2.xyz, 0); 48 B per triangle.
-//   nodes  Node8[]     8-wide nodes, 224 B each, root at index 0.
-//   cnodes CNode8[]    the same tree with 8-bit child boxes, 80 B each (optional).
+//   nodes  Node8[]     8-wide nodes, 256 B each (eight 32-B child records: box and
+//                      reference), root at index 0.
+//   cnodes CNode8[]    the same tree with 8-bit child boxes, 96 B each (optional).
 //
 // A child reference is 32 bits: 0xFFFFFFFF = empty slot; bit 31 clear = index of a
 // child node; bit 31 set = leaf holding triangles [first, first + count) of tri4 with
@@ -35,7 +36,7 @@ enum : uint32_t {
 };
 
 // One child of an 8-wide FP32 node: its box and its reference, 32 B, so the lane that
-// tests child c reads it with two 16-byte loads and a node's 8 children are 256
+// tests child c reads it with one 32-byte load and a node's 8 children are 256
 // contiguous bytes.
 struct alignas(16) Child8 {
 	float lo_x, lo_y, lo_z;
