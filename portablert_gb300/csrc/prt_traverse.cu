@@ -22,10 +22,11 @@
 //    at positions from ballots and popc.  Roots of new rays are admitted whenever fewer
 //    than 8 items are left.  Unused child slots hold NaN boxes, which no plain slab test
 //    passes.
-//  * Each query is two launches: a regular pass over the batches whose 32 rays all have
-//    finite reciprocals (the plain slab test only), which counts and skips the others,
-//    and a deferred pass over those with the conservative test for zero direction
-//    components (it returns at once when there are none).
+//  * A query of ray buffers is two launches: a regular pass over the batches whose 32
+//    rays all have finite reciprocals (the plain slab test only), which counts and skips
+//    the others, and a deferred pass over those with the conservative test for zero
+//    direction components (it returns at once when there are none).  Camera queries and
+//    counting runs are one general launch.
 //  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
 //    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
 //  * When the pool and the queue are empty the warp recomputes each slot's winning
