@@ -534,7 +534,7 @@ struct Document {
 			return false;
 		}
 		const Json &b = root.get("buffers")->arr[i];
-		if (!b.get("uri") && bin) {
+		if (i == 0 && !b.get("uri") && bin) { // a GLB's BIN chunk is its buffer 0
 			p = bin;
 			len = bin_len;
 		} else {
@@ -678,7 +678,7 @@ bool load_document(const std::string &path, Document &doc, std::vector<uint8_t> 
 				return false;
 			}
 			have = doc.buffers[i].size();
-		} else if (doc.bin) {
+		} else if (i == 0 && doc.bin) {
 			have = doc.bin_len;
 		}
 		if (have < len) {

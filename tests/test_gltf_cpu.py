@@ -160,6 +160,26 @@ def test_glb_with_two_buffers(tmp_path):
     assert _same(gltf.load_gltf(str(p)), _expected(doc, [b0, b1]))
 
 
+def test_only_buffer_0_of_a_glb_is_its_bin_chunk(tmp_path):
+    """A second buffer without a URI does not alias the BIN chunk: it has no bytes, so
+    its byteLength is an error."""
+    v, f = obj.blob_mesh(6, 8)
+    p = tmp_path / "g.glb"
+    gltf.write_gltf(str(p), v, f, "u16", "glb")
+    data = p.read_bytes()
+    js_len = struct.unpack_from("<I", data, 12)[0]
+    doc = json.loads(data[20:20 + js_len])
+    doc["buffers"].append({"byteLength": 16})
+    js = json.dumps(doc).encode()
+    js += b" " * (-len(js) % 4)
+    rest = data[20 + js_len:]
+    body = struct.pack("<II", len(js), 0x4E4F534A) + js + rest
+    q = tmp_path / "h.glb"
+    q.write_bytes(struct.pack("<III", 0x46546C67, 2, 12 + len(body)) + body)
+    with pytest.raises(PrtError, match="buffer 1: shorter than its byteLength"):
+        gltf.load_gltf(str(q))
+
+
 def test_empty_documents(tmp_path):
     for i, doc in enumerate([{"asset": {"version": "2.0"}},
                              {"asset": {"version": "2.0"}, "meshes": []},
