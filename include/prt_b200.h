@@ -197,6 +197,10 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  rays read and records written over the host link, no staging copies
  *                  (default 1; rays not 8-byte aligned are copied); 0 = always the
  *                  chunked copy pipeline below
+ *   "fail_alloc_after" test hook: n > 0 makes the n-th device buffer growth from now
+ *                  on (in any context of the process) fail as if the device were out of
+ *                  memory, once; the call that meets it returns PRT_ERR_OOM and the
+ *                  context stays usable.  0 disarms (default 0)
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)

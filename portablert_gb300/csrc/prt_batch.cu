@@ -173,6 +173,33 @@ void drop_graph(prt_b200_batch *b) {
 	b->graph_key.clear();
 }
 
+// Frees every device and host resource of a batch (its work is finished; the caller
+// holds the context's lock).
+void release_batch(prt_b200_batch *b) {
+	drop_graph(b);
+	for (Slot *s : {&b->gslot}) {
+		s->segs.release();
+		s->work.release();
+		if (s->done)
+			cudaEventDestroy(s->done);
+		s->done = nullptr;
+	}
+	for (int i = 0; i < kSlots; ++i) {
+		b->slots[i].segs.release();
+		b->slots[i].work.release();
+		if (b->slots[i].done)
+			cudaEventDestroy(b->slots[i].done);
+		b->slots[i].done = nullptr;
+	}
+	b->arena.release();
+	b->ws.release();
+	b->scenes_fp32.release();
+	b->scenes_comp.release();
+	if (b->h_words)
+		cudaFreeHost(b->h_words);
+	b->h_words = nullptr;
+}
+
 } // namespace
 
 extern "C" {
@@ -202,8 +229,9 @@ int prt_b200_batch_create(prt_b200_ctx *ctx, prt_b200_batch **out) {
 	if (e == cudaSuccess)
 		e = cudaEventCreateWithFlags(&b->gslot.done, cudaEventDisableTiming);
 	if (e != cudaSuccess) {
+		// Whatever was created before the failure is freed (the lock is held here).
 		int rc = bcuda(ctx, e, "batch create");
-		b->ctx = nullptr;
+		release_batch(b);
 		delete b;
 		return rc;
 	}
@@ -218,25 +246,7 @@ void prt_b200_batch_destroy(prt_b200_batch *b) {
 		std::lock_guard<std::mutex> lk(b->ctx->mu);
 		cudaSetDevice(b->ctx->device);
 		cudaDeviceSynchronize();
-		drop_graph(b);
-		for (Slot *s : {&b->gslot}) {
-			s->segs.release();
-			s->work.release();
-			if (s->done)
-				cudaEventDestroy(s->done);
-		}
-		for (int i = 0; i < kSlots; ++i) {
-			b->slots[i].segs.release();
-			b->slots[i].work.release();
-			if (b->slots[i].done)
-				cudaEventDestroy(b->slots[i].done);
-		}
-		b->arena.release();
-		b->ws.release();
-		b->scenes_fp32.release();
-		b->scenes_comp.release();
-		if (b->h_words)
-			cudaFreeHost(b->h_words);
+		release_batch(b);
 	}
 	delete b;
 }

@@ -24,6 +24,7 @@
 // A triangle with a non-finite vertex gets the box [-FLT_MAX, FLT_MAX]^3 in the tree,
 // which every finite ray passes, so the exact per-triangle test still sees it.
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstddef>
@@ -34,6 +35,20 @@
 #include "prt_sah.cuh"
 
 namespace prt {
+
+namespace {
+std::atomic<int64_t> g_alloc_failure{0}; // growths left before the injected failure
+} // namespace
+
+void arm_alloc_failure(int64_t n) { g_alloc_failure.store(n > 0 ? n : 0); }
+
+bool alloc_failure_due() {
+	int64_t v = g_alloc_failure.load(std::memory_order_relaxed);
+	while (v > 0)
+		if (g_alloc_failure.compare_exchange_weak(v, v - 1))
+			return v == 1;
+	return false;
+}
 
 void BuildScratch::release() {
 	DevBuf *all[] = {&keys,        &vals,     &keys2,      &vals2,    &scene_of,   &int_off,

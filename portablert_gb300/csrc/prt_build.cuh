@@ -14,6 +14,14 @@
 namespace prt {
 
 // Grow-only device allocation.
+// Host-side fault injection for tests (option "fail_alloc_after"): after
+// arm_alloc_failure(n), the n-th device buffer growth from then on, in any context,
+// fails with cudaErrorMemoryAllocation without calling the allocator, as a device out of
+// memory would; n = 0 disarms.  Nothing reaches the GPU: every caller checks the status
+// before it launches anything.
+void arm_alloc_failure(int64_t n);
+bool alloc_failure_due();
+
 struct DevBuf {
 	void *p = nullptr;
 	size_t bytes = 0;
@@ -24,6 +32,8 @@ struct DevBuf {
 			cudaFree(p);
 		p = nullptr;
 		bytes = 0;
+		if (alloc_failure_due())
+			return cudaErrorMemoryAllocation;
 		cudaError_t e = cudaMalloc(&p, b);
 		if (e == cudaSuccess)
 			bytes = b;

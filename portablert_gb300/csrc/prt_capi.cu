@@ -573,6 +573,10 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 		ctx->collapse_cost = v != 0;
 	} else if (k == "host_direct") {
 		ctx->host_direct = v != 0;
+	} else if (k == "fail_alloc_after") {
+		if (v < 0)
+			return fail(ctx, PRT_ERR_ARG, "fail_alloc_after must be >= 0");
+		prt::arm_alloc_failure(v);
 	} else {
 		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
 	}
