@@ -75,16 +75,25 @@ def test_set_tris_fails_at_each_allocation_then_recovers():
 
 def test_host_call_staging_fails_then_recovers():
     tris = workloads.soup_tris(63, 2000)
-    rays = workloads.soup_rays(64, 50_001)
+    rays = workloads.soup_rays(64, 100_003)
+    ref = _fresh()
+    try:
+        ref.set_tris(tris)
+        want = ref.nearest_hits(rays).view(np.uint8)  # 32-byte records, one per ray
+    finally:
+        ref.shutdown()
     b = _fresh()
     try:
         b.set_tris(tris)
-        want = b.nearest_hits(rays).view(np.uint8)  # in place: allocates nothing
-        b.set_option("host_direct", 0)              # the copy pipeline stages rays, records
-        for k in (1, 2):
+        # The copy pipeline from the first query on.  A call grows the rays' staging
+        # buffer, then the records', when its batch is larger than any before: round 1
+        # fails the first growth, round 2 (twice the rays) the second.
+        b.set_option("host_direct", 0)
+        for k, m in ((1, 50_001), (2, 100_003)):
             with Armed(b, k):
-                assert not _attempt(lambda: b.nearest_hits(rays))
-            assert np.array_equal(b.nearest_hits(rays).view(np.uint8), want), k
+                assert not _attempt(lambda: b.nearest_hits(rays[:m])), k
+            got = b.nearest_hits(rays[:m]).view(np.uint8)
+            assert np.array_equal(got, want[:32 * m]), k
     finally:
         b.shutdown()
 
