@@ -429,7 +429,8 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		}
 	}
 	if (e != cudaSuccess) {
-		std::lock_guard<std::mutex> lk(ctx->mu);
+		// No lock is held here: destroying the server destroys its batch, which takes the
+		// context's lock (ctx->err has a lock of its own).
 		ctx->err = std::string("server create: ") + cudaGetErrorString(e);
 		prt_b200_server_destroy(s.release());
 		return e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA;
@@ -441,10 +442,7 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		sp->sched = std::thread(scheduler, sp);
 	} catch (const std::exception &ex) {
 		// A thread that could not start: stop those that did and free everything.
-		{
-			std::lock_guard<std::mutex> lk(ctx->mu);
-			ctx->err = std::string("server create: ") + ex.what();
-		}
+		ctx->err = std::string("server create: ") + ex.what();
 		prt_b200_server_destroy(s.release());
 		return PRT_ERR_OOM;
 	}

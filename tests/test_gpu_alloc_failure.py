@@ -10,7 +10,9 @@ import pytest
 from portablert_gb300 import backend, batch, hitreg, serve, workloads
 from portablert_gb300._lib import PrtError
 
-pytestmark = pytest.mark.gpu
+# A blocked call (the server's creation once deadlocked on the context's lock when an
+# allocation failed) ends the run with every thread's stack instead of hanging it.
+pytestmark = [pytest.mark.gpu, pytest.mark.timeout(300, method="thread")]
 
 OOM, NO_SCENE = 6, 4
 
