@@ -212,7 +212,12 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree
  *   is an SAH tree), "in_place" (1 = the last host-buffer nearest_hits traversed the
  *   caller's buffers in place), "node_bytes", "tri_bytes",
- *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms". */
+ *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms".
+ * Every option can also be set for each new context from the environment:
+ *   PRT_B200_<OPTION> (the name in upper case), e.g. PRT_B200_LEAF_SIZE=4 or
+ *   PRT_B200_BUILD_SAH=0, so programs that use the backend through portableRT's API are
+ *   tuned without a change.  A value that is not a decimal integer makes
+ *   prt_b200_create fail with PRT_ERR_ARG; one out of range, with the option's error. */
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t value);
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value);
 

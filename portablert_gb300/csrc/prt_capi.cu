@@ -8,10 +8,15 @@
 // turns a status into std::runtime_error, the reference's exception type for an
 // unusable backend (include/portableRT/nearest_hits_impl.hpp:31-32).
 #include <algorithm>
+#include <cctype>
+#include <cerrno>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
@@ -72,6 +77,37 @@ int check_device_errors(prt_b200_ctx *ctx) {
 		return fail(ctx, PRT_ERR_DEVICE, m);
 	}
 	return PRT_OK;
+}
+
+// Every option prt_b200_set_option accepts.  PRT_B200_<KEY> in the environment (the
+// name in upper case, e.g. PRT_B200_LEAF_SIZE=4) sets option <key> of each new context,
+// so programs that use the backend through portableRT's API can be tuned unchanged.
+const char *const kOptionKeys[] = {"leaf_size",        "node_format",   "block",
+                                   "pipe_chunks",      "pipe_ramp",     "pipe_min_rays",
+                                   "serve_batches_per_warp", "pool_depth", "count_visits",
+                                   "build_compressed", "build_sah",     "collapse_cost",
+                                   "host_direct",      "fail_alloc_after"};
+
+// The overrides set in the environment, as (key, value); false with a message when a
+// value is not a decimal integer.
+bool env_overrides(std::vector<std::pair<const char *, int64_t>> &out, std::string &err) {
+	for (const char *key : kOptionKeys) {
+		std::string name = "PRT_B200_";
+		for (const char *c = key; *c; ++c)
+			name += (char)std::toupper((unsigned char)*c);
+		const char *text = std::getenv(name.c_str());
+		if (!text)
+			continue;
+		char *end = nullptr;
+		errno = 0;
+		const long long v = std::strtoll(text, &end, 10);
+		if (end == text || *end != '\0' || errno) {
+			err = name + "=" + text + ": not a decimal integer";
+			return false;
+		}
+		out.emplace_back(key, (int64_t)v);
+	}
+	return true;
 }
 
 // The record layout of a call, and the traversal settings of the context's options.
@@ -175,6 +211,13 @@ int prt_b200_create(int device, prt_b200_ctx **out) {
 		return PRT_ERR_ARG;
 	}
 	*out = nullptr;
+	// Environment overrides are read first, so a malformed one is reported on any machine.
+	std::vector<std::pair<const char *, int64_t>> env;
+	std::string env_err;
+	if (!env_overrides(env, env_err)) {
+		g_create_error = env_err;
+		return PRT_ERR_ARG;
+	}
 	int n = 0;
 	if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n || !cc_ok(device)) {
 		cudaGetLastError();
@@ -213,6 +256,14 @@ int prt_b200_create(int device, prt_b200_ctx **out) {
 		g_create_error = std::string("create: ") + cudaGetErrorString(e);
 		prt_b200_destroy(ctx);
 		return e == cudaErrorMemoryAllocation ? PRT_ERR_OOM : PRT_ERR_CUDA;
+	}
+	for (const auto &kv : env) {
+		const int rc = prt_b200_set_option(ctx, kv.first, kv.second);
+		if (rc != PRT_OK) {
+			g_create_error = "environment override: " + ctx->err.get();
+			prt_b200_destroy(ctx);
+			return rc;
+		}
 	}
 	*out = ctx;
 	return PRT_OK;

@@ -4,6 +4,7 @@ import ctypes
 import os
 import re
 import subprocess
+import sys
 
 import pytest
 
@@ -140,3 +141,58 @@ def test_exceptions_become_statuses(tmp_path):
     assert ma == "one: out of host memory"
     assert mb == "two: x"
     assert mc == "three: unexpected exception"
+
+
+def _option_lists():
+    src = open(os.path.join(ROOT, "portablert_gb300", "csrc", "prt_capi.cu")).read()
+    body = src[src.index("int prt_b200_set_option("):src.index("int prt_b200_get_stat(")]
+    accepted = re.findall(r'k == "(\w+)"', body)
+    table = src[src.index("kOptionKeys[] = {"):]
+    table = table[:table.index("};")]
+    env_keys = re.findall(r'"(\w+)"', table)
+    hdr = open(HEADER).read()
+    documented = re.findall(r'^ \*   "(\w+)"', hdr, re.M)
+    return accepted, env_keys, documented
+
+
+def test_every_option_is_documented_and_settable_from_the_environment():
+    accepted, env_keys, documented = _option_lists()
+    assert sorted(accepted) == sorted(env_keys)
+    assert set(accepted) <= set(documented), set(accepted) - set(documented)
+
+
+def _create_in_child(env_extra):
+    """prt_b200_create(0) in a fresh process with extra environment: (status, message)."""
+    code = (
+        "import ctypes, sys\n"
+        "from portablert_gb300 import _lib\n"
+        "L = _lib.load()\n"
+        "h = ctypes.c_void_p()\n"
+        "rc = L.prt_b200_create(0, ctypes.byref(h))\n"
+        "print(rc)\n"
+        "print((L.prt_b200_last_error(None) or b'').decode())\n"
+        "if h.value: L.prt_b200_destroy(h)\n")
+    env = dict(os.environ, **env_extra)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env,
+                       cwd=ROOT, timeout=300)
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.split("\n")
+    return int(lines[0]), lines[1]
+
+
+@pytest.mark.parametrize("value", ["abc", "", "4x", "1.5", "99999999999999999999"])
+def test_malformed_environment_override_is_an_argument_error(lib, value):
+    rc, msg = _create_in_child({"PRT_B200_LEAF_SIZE": value})
+    assert rc == 1 and "PRT_B200_LEAF_SIZE" in msg, (rc, msg)
+
+
+def test_wellformed_environment_override_passes_the_syntax_check(lib):
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present (the GPU tests apply the override)")
+    except ImportError:
+        pass
+    rc, msg = _create_in_child({"PRT_B200_LEAF_SIZE": " 4", "PRT_B200_BUILD_SAH": "-0"})
+    assert rc == 3 and "10.3" in msg, (rc, msg)  # reached the device check
