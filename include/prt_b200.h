@@ -116,7 +116,9 @@ int prt_b200_sync(prt_b200_ctx *ctx);
  * address up (cudaGetSymbolAddress), so make that first call before any stream capture.
  * All calls share the array: they are synchronous and serialised by a process-wide
  * lock; GPU work of two calls that overlapped would race.  The context and the scene
- * must already exist (prt_b200_create, prt_b200_set_tris allocate). */
+ * must already exist (prt_b200_create, prt_b200_set_tris allocate).  Kernel errors are
+ * reported as prt_b200_nearest_hits reports them: this call's own, and any that earlier
+ * asynchronous calls on the context (the _dev calls) left pending. */
 int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *rays6, uint64_t n,
                                   uint32_t field_mask, uint32_t rec_size, const uint8_t offs[8],
                                   void *out_host);
@@ -200,7 +202,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "fail_alloc_after" test hook: n > 0 makes the n-th device buffer growth from now
  *                  on (in any context of the process) fail as if the device were out of
  *                  memory, once; the call that meets it returns PRT_ERR_OOM and the
- *                  context stays usable.  0 disarms (default 0)
+ *                  context stays usable.  0 disarms (default 0).  Only this call sets
+ *                  it; it has no environment override
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
@@ -213,7 +216,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   is an SAH tree), "in_place" (1 = the last host-buffer nearest_hits traversed the
  *   caller's buffers in place), "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms".
- * Every option can also be set for each new context from the environment:
+ * Every option but the test hook can also be set for each new context from the
+ * environment:
  *   PRT_B200_<OPTION> (the name in upper case), e.g. PRT_B200_LEAF_SIZE=4 or
  *   PRT_B200_BUILD_SAH=0, so programs that use the backend through portableRT's API are
  *   tuned without a change.  A value that is not a decimal integer makes

@@ -81,7 +81,7 @@ def build_cpp_test(verbose: bool = False) -> str:
     """Compiles the portableRT C++ API (compat headers + B200Backend) into a test
     program linked against libprt_b200.so."""
     lib = build_library()
-    srcs = [os.path.join(PKG, "src", "b200_api_test.cpp"),
+    srcs = [os.path.join(ROOT, "tests", "cpp", "b200_api_test.cpp"),
             os.path.join(PKG, "src", "intersect_b200.cpp"),
             os.path.join(PKG, "compat", "backend.cpp")]
     deps = srcs + [lib, os.path.join(ROOT, "include", "portableRT", "intersect_b200.hpp")]

@@ -79,14 +79,17 @@ int check_device_errors(prt_b200_ctx *ctx) {
 	return PRT_OK;
 }
 
-// Every option prt_b200_set_option accepts.  PRT_B200_<KEY> in the environment (the
-// name in upper case, e.g. PRT_B200_LEAF_SIZE=4) sets option <key> of each new context,
-// so programs that use the backend through portableRT's API can be tuned unchanged.
+// Every tuning option prt_b200_set_option accepts.  PRT_B200_<KEY> in the environment
+// (the name in upper case, e.g. PRT_B200_LEAF_SIZE=4) sets option <key> of each new
+// context, so programs that use the backend through portableRT's API can be tuned
+// unchanged.  The test hook "fail_alloc_after" is deliberately not among them: it arms
+// a process-wide allocation-failure injector, which no environment variable of a
+// production program should be able to reach.
 const char *const kOptionKeys[] = {"leaf_size",        "node_format",   "block",
                                    "pipe_chunks",      "pipe_ramp",     "pipe_min_rays",
                                    "serve_batches_per_warp", "pool_depth", "count_visits",
                                    "build_compressed", "build_sah",     "collapse_cost",
-                                   "host_direct",      "fail_alloc_after"};
+                                   "host_direct"};
 
 // The overrides set in the environment, as (key, value); false with a message when a
 // value is not a decimal integer.
@@ -582,95 +585,99 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 	if (!ctx || !key)
 		return PRT_ERR_ARG;
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	std::string k(key);
-	if (k == "leaf_size") {
-		if (v < 1 || v > prt::kMaxLeaf)
-			return fail(ctx, PRT_ERR_ARG, "leaf_size must be in [1, 8]");
-		ctx->leaf_size = (int)v;
-	} else if (k == "node_format") {
-		if (v != PRT_NODES_FP32 && v != PRT_NODES_COMPRESSED)
-			return fail(ctx, PRT_ERR_ARG, "node_format must be 0 or 1");
-		ctx->node_format = (int)v;
-	} else if (k == "block") {
-		if (v < 32 || v > 128 || v % 32)
-			return fail(ctx, PRT_ERR_ARG, "block must be 32, 64, 96 or 128");
-		ctx->block = (int)v;
-	} else if (k == "pipe_chunks") {
-		if (v < 1 || v > prt_b200_ctx::kPipe)
-			return fail(ctx, PRT_ERR_ARG, "pipe_chunks must be in [1, 16]");
-		ctx->pipe_chunks = (int)v;
-	} else if (k == "pipe_ramp") {
-		ctx->pipe_ramp = v != 0;
-	} else if (k == "pipe_min_rays") {
-		if (v < 32 || v > (1ll << 30) || v % 32)
-			return fail(ctx, PRT_ERR_ARG, "pipe_min_rays must be a multiple of 32 in [32, 2^30]");
-		ctx->pipe_min_rays = (uint32_t)v;
-	} else if (k == "serve_batches_per_warp") {
-		if (v < 0 || v > (1 << 20))
-			return fail(ctx, PRT_ERR_ARG, "serve_batches_per_warp must be in [0, 2^20]");
-		ctx->serve_batches_per_warp = (int)v;
-	} else if (k == "pool_depth") {
-		if (v < 0 || v > prt::traversal_stack_depth())
-			return fail(ctx, PRT_ERR_ARG, "pool_depth must be in [0, 32]");
-		ctx->pool_depth = (int)v;
-	} else if (k == "count_visits") {
-		ctx->count = v != 0;
-	} else if (k == "build_compressed") {
-		ctx->build_compressed = v != 0;
-	} else if (k == "build_sah") {
-		ctx->build_sah = v != 0;
-	} else if (k == "collapse_cost") {
-		ctx->collapse_cost = v != 0;
-	} else if (k == "host_direct") {
-		ctx->host_direct = v != 0;
-	} else if (k == "fail_alloc_after") {
-		if (v < 0)
-			return fail(ctx, PRT_ERR_ARG, "fail_alloc_after must be >= 0");
-		prt::arm_alloc_failure(v);
-	} else {
-		return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
-	}
-	return PRT_OK;
+	return prt::guarded(&ctx->err, "set_option", [&]() -> int {
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		std::string k(key);
+		if (k == "leaf_size") {
+			if (v < 1 || v > prt::kMaxLeaf)
+				return fail(ctx, PRT_ERR_ARG, "leaf_size must be in [1, 8]");
+			ctx->leaf_size = (int)v;
+		} else if (k == "node_format") {
+			if (v != PRT_NODES_FP32 && v != PRT_NODES_COMPRESSED)
+				return fail(ctx, PRT_ERR_ARG, "node_format must be 0 or 1");
+			ctx->node_format = (int)v;
+		} else if (k == "block") {
+			if (v < 32 || v > 128 || v % 32)
+				return fail(ctx, PRT_ERR_ARG, "block must be 32, 64, 96 or 128");
+			ctx->block = (int)v;
+		} else if (k == "pipe_chunks") {
+			if (v < 1 || v > prt_b200_ctx::kPipe)
+				return fail(ctx, PRT_ERR_ARG, "pipe_chunks must be in [1, 16]");
+			ctx->pipe_chunks = (int)v;
+		} else if (k == "pipe_ramp") {
+			ctx->pipe_ramp = v != 0;
+		} else if (k == "pipe_min_rays") {
+			if (v < 32 || v > (1ll << 30) || v % 32)
+				return fail(ctx, PRT_ERR_ARG, "pipe_min_rays must be a multiple of 32 in [32, 2^30]");
+			ctx->pipe_min_rays = (uint32_t)v;
+		} else if (k == "serve_batches_per_warp") {
+			if (v < 0 || v > (1 << 20))
+				return fail(ctx, PRT_ERR_ARG, "serve_batches_per_warp must be in [0, 2^20]");
+			ctx->serve_batches_per_warp = (int)v;
+		} else if (k == "pool_depth") {
+			if (v < 0 || v > prt::traversal_stack_depth())
+				return fail(ctx, PRT_ERR_ARG, "pool_depth must be in [0, 32]");
+			ctx->pool_depth = (int)v;
+		} else if (k == "count_visits") {
+			ctx->count = v != 0;
+		} else if (k == "build_compressed") {
+			ctx->build_compressed = v != 0;
+		} else if (k == "build_sah") {
+			ctx->build_sah = v != 0;
+		} else if (k == "collapse_cost") {
+			ctx->collapse_cost = v != 0;
+		} else if (k == "host_direct") {
+			ctx->host_direct = v != 0;
+		} else if (k == "fail_alloc_after") {
+			if (v < 0)
+				return fail(ctx, PRT_ERR_ARG, "fail_alloc_after must be >= 0");
+			prt::arm_alloc_failure(v);
+		} else {
+			return fail(ctx, PRT_ERR_ARG, "unknown option " + k);
+		}
+		return PRT_OK;
+	});
 }
 
 int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
 	if (!ctx || !key || !value)
 		return PRT_ERR_ARG;
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	std::string k(key);
-	const prt::SceneGPU &s = ctx->scene;
-	if (k == "n_tris")
-		*value = (double)s.n_tris;
-	else if (k == "n_nodes")
-		*value = s.n_nodes;
-	else if (k == "depth")
-		*value = s.depth;
-	else if (k == "build_ms")
-		*value = ctx->build_ms;
-	else if (k == "build_sah")
-		*value = ctx->last_build_sah ? 1.0 : 0.0;
-	else if (k == "in_place")
-		*value = ctx->last_in_place ? 1.0 : 0.0;
-	else if (k == "node_bytes")
-		*value = (double)s.n_nodes *
-		         (ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8) : sizeof(prt::Node8));
-	else if (k == "node_size")
-		*value = (double)(ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8)
-		                                                            : sizeof(prt::Node8));
-	else if (k == "tri_bytes")
-		*value = 48.0 * (double)s.n_tris;
-	else if (k == "visits_nodes")
-		*value = (double)ctx->visits[0];
-	else if (k == "visits_tris")
-		*value = (double)ctx->visits[1];
-	else if (k == "sms")
-		*value = ctx->sms;
-	else if (k == "leaf_size")
-		*value = s.leaf_size;
-	else
-		return fail(ctx, PRT_ERR_ARG, "unknown statistic " + k);
-	return PRT_OK;
+	return prt::guarded(&ctx->err, "get_stat", [&]() -> int {
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		std::string k(key);
+		const prt::SceneGPU &s = ctx->scene;
+		if (k == "n_tris")
+			*value = (double)s.n_tris;
+		else if (k == "n_nodes")
+			*value = s.n_nodes;
+		else if (k == "depth")
+			*value = s.depth;
+		else if (k == "build_ms")
+			*value = ctx->build_ms;
+		else if (k == "build_sah")
+			*value = ctx->last_build_sah ? 1.0 : 0.0;
+		else if (k == "in_place")
+			*value = ctx->last_in_place ? 1.0 : 0.0;
+		else if (k == "node_bytes")
+			*value = (double)s.n_nodes *
+			         (ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8) : sizeof(prt::Node8));
+		else if (k == "node_size")
+			*value = (double)(ctx->node_format == PRT_NODES_COMPRESSED ? sizeof(prt::CNode8)
+			                                                            : sizeof(prt::Node8));
+		else if (k == "tri_bytes")
+			*value = 48.0 * (double)s.n_tris;
+		else if (k == "visits_nodes")
+			*value = (double)ctx->visits[0];
+		else if (k == "visits_tris")
+			*value = (double)ctx->visits[1];
+		else if (k == "sms")
+			*value = ctx->sms;
+		else if (k == "leaf_size")
+			*value = s.leaf_size;
+		else
+			return fail(ctx, PRT_ERR_ARG, "unknown statistic " + k);
+		return PRT_OK;
+	});
 }
 
 } // extern "C"
@@ -732,48 +739,53 @@ extern "C" int prt_b200_nearest_hits_noalloc(prt_b200_ctx *ctx, const float *ray
                                              const uint8_t offs[8], void *out_host) {
 	if (!ctx)
 		return PRT_ERR_ARG;
-	std::string why;
-	if (!layout_ok(field_mask, rec_size, offs, why))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: " + why);
-	if (n > kNoallocMaxRays)
-		return fail(ctx, PRT_ERR_LIMIT,
-		            "nearest_hits_noalloc: at most 65536 rays per call (" + std::to_string(n) +
-		                " given); split the batch or use prt_b200_nearest_hits");
-	if (n && (!rays6 || !out_host))
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: null buffer");
-	std::lock_guard<std::mutex> glk(g_noalloc_mu);
-	std::lock_guard<std::mutex> lk(ctx->mu);
-	if (!ctx->scene_set)
-		return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits_noalloc: set_tris has not succeeded");
-	if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
-		return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: compressed nodes were not built");
-	if (n == 0)
-		return PRT_OK;
-	CAPI_TRY(ctx, cudaSetDevice(ctx->device));
-	unsigned char *scratch = nullptr;
-	int rc = noalloc_scratch(ctx, ctx->device, &scratch);
-	if (rc != PRT_OK)
-		return rc;
-	uint32_t *d_work = reinterpret_cast<uint32_t *>(scratch);
-	uint32_t *d_err = d_work + 1;
-	unsigned long long *d_visits = reinterpret_cast<unsigned long long *>(scratch + 16);
-	float *d_rays = reinterpret_cast<float *>(scratch + kNoallocWork);
-	void *d_out = scratch + kNoallocWork + kNoallocRayBytes;
-	cudaStream_t st = ctx->stream;
-	CAPI_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoallocWork, st));
-	CAPI_TRY(ctx, cudaMemcpyAsync(d_rays, rays6, 24ull * n, cudaMemcpyHostToDevice, st));
-	const prt::OutLayout lay = out_layout(field_mask, rec_size, offs);
-	const prt::TravConfig cfg = trav_config(ctx);
-	CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays, n, lay, d_out, cfg, d_work,
-	                                       d_visits, d_err, st, ctx->sms));
-	CAPI_TRY(ctx, cudaMemcpyAsync(out_host, d_out, (uint64_t)rec_size * n, cudaMemcpyDeviceToHost,
-	                              st));
-	uint32_t err_word = 0;
-	CAPI_TRY(ctx, cudaMemcpyAsync(&err_word, d_err, 4, cudaMemcpyDeviceToHost, st));
-	CAPI_TRY(ctx, cudaStreamSynchronize(st));
-	if (ctx->count)
-		CAPI_TRY(ctx, cudaMemcpy(ctx->visits, d_visits, 16, cudaMemcpyDeviceToHost));
-	if (err_word)
-		return fail(ctx, PRT_ERR_DEVICE, "nearest_hits_noalloc: kernel reported an error");
-	return PRT_OK;
+	return prt::guarded(&ctx->err, "nearest_hits_noalloc", [&]() -> int {
+		std::string why;
+		if (!layout_ok(field_mask, rec_size, offs, why))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: " + why);
+		if (n > kNoallocMaxRays)
+			return fail(ctx, PRT_ERR_LIMIT,
+			            "nearest_hits_noalloc: at most 65536 rays per call (" + std::to_string(n) +
+			                " given); split the batch or use prt_b200_nearest_hits");
+		if (n && (!rays6 || !out_host))
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: null buffer");
+		std::lock_guard<std::mutex> glk(g_noalloc_mu);
+		std::lock_guard<std::mutex> lk(ctx->mu);
+		if (!ctx->scene_set)
+			return fail(ctx, PRT_ERR_NO_SCENE, "nearest_hits_noalloc: set_tris has not succeeded");
+		if (ctx->node_format == PRT_NODES_COMPRESSED && !ctx->scene.has_cnodes && ctx->scene.n_tris)
+			return fail(ctx, PRT_ERR_ARG, "nearest_hits_noalloc: compressed nodes were not built");
+		if (n == 0)
+			return PRT_OK;
+		CAPI_TRY(ctx, cudaSetDevice(ctx->device));
+		unsigned char *scratch = nullptr;
+		int rc = noalloc_scratch(ctx, ctx->device, &scratch);
+		if (rc != PRT_OK)
+			return rc;
+		uint32_t *d_work = reinterpret_cast<uint32_t *>(scratch);
+		uint32_t *d_err = d_work + 1;
+		unsigned long long *d_visits = reinterpret_cast<unsigned long long *>(scratch + 16);
+		float *d_rays = reinterpret_cast<float *>(scratch + kNoallocWork);
+		void *d_out = scratch + kNoallocWork + kNoallocRayBytes;
+		cudaStream_t st = ctx->stream;
+		CAPI_TRY(ctx, cudaMemsetAsync(scratch, 0, kNoallocWork, st));
+		CAPI_TRY(ctx, cudaMemcpyAsync(d_rays, rays6, 24ull * n, cudaMemcpyHostToDevice, st));
+		const prt::OutLayout lay = out_layout(field_mask, rec_size, offs);
+		const prt::TravConfig cfg = trav_config(ctx);
+		CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, d_rays, n, lay, d_out, cfg, d_work,
+		                                       d_visits, d_err, st, ctx->sms));
+		CAPI_TRY(ctx, cudaMemcpyAsync(out_host, d_out, (uint64_t)rec_size * n, cudaMemcpyDeviceToHost,
+		                              st));
+		uint32_t err_word = 0;
+		CAPI_TRY(ctx, cudaMemcpyAsync(&err_word, d_err, 4, cudaMemcpyDeviceToHost, st));
+		CAPI_TRY(ctx, cudaStreamSynchronize(st));
+		if (ctx->count)
+			CAPI_TRY(ctx, cudaMemcpy(ctx->visits, d_visits, 16, cudaMemcpyDeviceToHost));
+		if (err_word)
+			return fail(ctx, PRT_ERR_DEVICE, "nearest_hits_noalloc: kernel reported an error");
+		// Errors that earlier asynchronous calls on this context (the _dev calls) left in the
+		// context's own error word are reported here too, as prt_b200_nearest_hits reports
+		// them; reading it copies 4 bytes into the context's pinned word, no allocation.
+		return check_device_errors(ctx);
+	});
 }

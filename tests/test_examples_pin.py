@@ -11,6 +11,7 @@ import numpy as np
 import pytest
 
 from conftest import GOLDEN, ROOT
+from oracle.refdir import reference_path
 
 F32 = np.float32
 REF_EXAMPLES = os.path.join(ROOT, "oracle", "_ref")
@@ -42,7 +43,7 @@ def test_oracle_equals_bunny_program(oracle_lib):
     assert hashlib.sha256(mask.tobytes()).hexdigest() == str(z["sha256"])
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/examples"),
+@pytest.mark.skipif(not os.path.isdir(reference_path("examples")),
                     reason="the reference's example sources are not present")
 def test_fixtures_match_the_programs_run_now():
     sys.path.insert(0, ROOT)

@@ -10,9 +10,10 @@ import subprocess
 import pytest
 
 from conftest import ROOT
+from oracle.refdir import REFERENCE_DIR
 from portablert_gb300 import build
 
-REF = "/root/reference"
+REF = REFERENCE_DIR
 PATCH = os.path.join(ROOT, "portablert_gb300", "integration", "portableRT-b200.patch")
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src")),

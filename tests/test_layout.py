@@ -7,6 +7,7 @@ import tempfile
 import pytest
 
 from conftest import ROOT
+from oracle.refdir import reference_path
 from portablert_gb300 import hitreg
 
 # Measured with offsetof on portableRT's hitreg.hpp (g++ 13, x86-64):
@@ -82,10 +83,10 @@ def test_compat_header_layout_matches():
     assert got == EXPECTED
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/include"),
+@pytest.mark.skipif(not os.path.isdir(reference_path("include")),
                     reason="portableRT sources not present")
 def test_reference_header_layout_matches():
-    got = _probe("/root/reference/include", extra=("-include", "cstdint", "-include", "iostream"))
+    got = _probe(reference_path("include"), extra=("-include", "cstdint", "-include", "iostream"))
     assert got == EXPECTED
 
 

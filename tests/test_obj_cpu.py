@@ -6,10 +6,11 @@ import os
 import numpy as np
 import pytest
 
+from oracle.refdir import reference_path
 from portablert_gb300 import obj
 from portablert_gb300._lib import PrtError
 
-BUNNY = "/root/reference/examples/common/bunny.obj"
+BUNNY = reference_path("examples", "common", "bunny.obj")
 
 
 def _py_parse(text):

@@ -35,16 +35,32 @@ def test_noalloc_matches_allocating_call_twice():
         _lib.check(L.prt_b200_set_tris(ctx, tris.ctypes.data, len(tris)), ctx, L)
         cases = [(hitreg.TAGS, workloads.soup_rays(21, 50_000)),
                  (("t", "primitive_id", "valid"), workloads.soup_rays(22, MAX_RAYS))]
-        for tags, rays in cases:  # two calls in a row, different sizes and layouts
+        wants = []
+        for tags, rays in cases:
             lay = hitreg.layout(tags)
             rc_a, want = _call(L, L.prt_b200_nearest_hits, ctx, rays, lay)
             _lib.check(rc_a, ctx, L)
-            rc_b, got = _call(L, L.prt_b200_nearest_hits_noalloc, ctx, rays, lay)
-            _lib.check(rc_b, ctx, L)
-            # The parity tolerance of this project is bit equality.
-            assert np.array_equal(got, want)
-            rec = got.view(lay.numpy_dtype())
-            assert (rec["valid"] != 0).sum() > 0
+            wants.append(want)
+        # From here on the first device buffer growth anywhere in the process fails (the
+        # library's host-side allocation-failure injector).  The no-alloc calls must not
+        # meet it, and it must still be armed after them.
+        _lib.check(L.prt_b200_set_option(ctx, b"fail_alloc_after", 1), ctx, L)
+        try:
+            for (tags, rays), want in zip(cases, wants):  # two calls in a row
+                lay = hitreg.layout(tags)
+                rc_b, got = _call(L, L.prt_b200_nearest_hits_noalloc, ctx, rays, lay)
+                _lib.check(rc_b, ctx, L)
+                # The parity tolerance of this project is bit equality.
+                assert np.array_equal(got, want)
+                rec = got.view(lay.numpy_dtype())
+                assert (rec["valid"] != 0).sum() > 0
+            # Still armed: a set_tris that must grow its triangle buffer meets it.
+            bigger = workloads.soup_tris(13, 8192)
+            rc = L.prt_b200_set_tris(ctx, bigger.ctypes.data, len(bigger))
+            assert rc == 6, rc  # PRT_ERR_OOM: the no-alloc calls made no growth
+        finally:
+            L.prt_b200_set_option(ctx, b"fail_alloc_after", 0)
+        _lib.check(L.prt_b200_set_tris(ctx, tris.ctypes.data, len(tris)), ctx, L)
         too_many = workloads.soup_rays(23, MAX_RAYS + 1)
         rc, _ = _call(L, L.prt_b200_nearest_hits_noalloc, ctx, too_many,
                       hitreg.layout(hitreg.TAGS))
