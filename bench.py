@@ -47,17 +47,67 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def committed_profile(key: str):
-    """A figure (DRAM bytes per launch, L2 hit rate) from the committed ncu summary of the
-    heightfield traversal, if it exists."""
-    p = os.path.join(ROOT, "profiles", "traverse_heightfield_traffic.txt")
+PROFILE = os.path.join("profiles", "traverse_heightfield_traffic.txt")
+
+
+def committed_profile(key: str, text: bool = False):
+    """A figure (DRAM bytes, warp instructions per launch, L2 hit rate, the commit it was
+    captured at) from the committed ncu summary of the heightfield traversal, if any."""
+    p = os.path.join(ROOT, PROFILE)
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for line in f:
             if line.startswith(key + ":"):
-                return float(line.split(":", 1)[1])
+                v = line.split(":", 1)[1].strip()
+                return v if text else float(v)
     return None
+
+
+def traversal_rooflines(n, per_launch_s, b_ray, v_nodes, v_tris, node_size, rec_size, peak,
+                        peak_kind, l2_peak, sms, sm_mhz):
+    """The regular traversal pass against each resource that could bound it; `bound` is
+    the one it comes closest to.
+
+    * issue: warp instructions per launch (ncu, committed summary) over the launch time,
+      against 4 issue slots per SM per cycle at the median SM clock of the timed region;
+    * l2: the node and triangle bytes the traversal requests (visits x 256 B + tests x
+      48 B per ray) against the read bandwidth of its own 32-byte loads from an
+      L2-resident buffer (prt_b200_probe_read, measured in this run);
+    * hbm: DRAM bytes per launch (ncu, committed summary) against the measured HBM peak;
+      beside it the per-ray algorithmic bytes (24 B ray + record + node and triangle
+      fetches) against the same peak, which exceeds 1 because L2 serves most fetches."""
+    traffic = committed_profile("dram_bytes_per_launch")
+    inst = committed_profile("warp_instructions_per_launch")
+    at = committed_profile("captured_at", text=True)
+    src = f"{PROFILE} (ncu, traversal of commit {at})"
+    alg = n * b_ray / per_launch_s / 1e9
+    fetch = n * (v_nodes * node_size + v_tris * 48) / per_launch_s / 1e9
+    res = {
+        "issue": {"achieved": inst / per_launch_s / 1e9 if inst else None,
+                  "peak": sms * 4 * sm_mhz * 1e6 / 1e9, "unit": "G warp-instructions/s",
+                  "warp_instructions_per_ray": inst / n if inst else None,
+                  "warp_instructions_per_node_visit": inst / n / v_nodes if inst else None,
+                  "source": src, "sm_mhz": sm_mhz, "sms": sms},
+        "l2": {"achieved": fetch, "peak": l2_peak, "unit": "GB/s",
+               "bytes_per_ray": v_nodes * node_size + v_tris * 48,
+               "peak_source": "prt_b200_probe_read: 32-byte loads over a 48 MiB buffer, "
+                              "this run"},
+        "hbm": {"achieved": traffic / per_launch_s / 1e9 if traffic else None, "peak": peak,
+                "unit": "GB/s", "traffic": traffic, "traffic_source": src,
+                "peak_source": peak_kind, "l2_hit_rate_pct": committed_profile("l2_hit_rate_pct"),
+                "algorithmic": {"achieved": alg, "frac": alg / peak, "bytes_per_ray": b_ray,
+                                "node_visits_per_ray": v_nodes, "tri_tests_per_ray": v_tris,
+                                "node_bytes": node_size,
+                                "io_floor_frac": n * (24 + rec_size) / per_launch_s / 1e9 / peak}},
+    }
+    for r in res.values():
+        r["frac"] = r["achieved"] / r["peak"] if r["achieved"] and r["peak"] else None
+    bound = max((k for k in res if res[k]["frac"] is not None), key=lambda k: res[k]["frac"])
+    top = res[bound]
+    return {"bound": bound, "achieved": top["achieved"], "peak": top["peak"],
+            "unit": top["unit"], "frac": top["frac"], "traffic": traffic,
+            "traffic_source": src, **res}
 
 
 class ClockSampler:
@@ -165,12 +215,36 @@ def aggregate_mrays(world: int, n_per_rank: int, steps: int, max_total_ms: float
     return world * n_per_rank * steps / (max_total_ms / 1e3) / 1e6
 
 
+BUILD_BYTES_PER_TRI = 432  # the canonical LBVH pipeline's algorithmic bytes per triangle
+NODE_BYTES_WRITTEN = 256 + 96  # each 8-wide node in FP32 and in compressed form
+
+
+def build_roofline(n_tris, n_nodes, ms, lbvh_ms, lbvh_nodes, peak, peak_kind):
+    """The build against HBM bandwidth: algorithmic bytes = 432 B per triangle (scene
+    bounds, Morton codes, four radix passes, hierarchy, refit, collapse, re-layout) plus
+    the 8-wide nodes written in both formats, over the device-timed build."""
+    def one(nodes, t_ms):
+        byt = BUILD_BYTES_PER_TRI * n_tris + NODE_BYTES_WRITTEN * nodes
+        ach = byt / (t_ms / 1e3) / 1e9
+        return {"bytes": byt, "bytes_per_tri": byt / n_tris, "ms": t_ms, "achieved": ach,
+                "frac": ach / peak}
+    r = {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_kind}
+    r.update(one(n_nodes, ms))
+    r["lbvh"] = one(lbvh_nodes, lbvh_ms)
+    return r
+
+
 # --------------------------------------------------------------------------- CPU side
 
-def cpu_baseline(tris, rays, sample_rays: int, seed: int = 0):
+def cpu_baseline(tris, rays, sample_rays: int, seed: int = 0, got=None, tags=TAGS):
     """The oracle port of the reference CPU backend on this host: SAH build (1 thread,
-    as the reference) and nearest_hits on all online cores over a ray sample."""
+    as the reference) and nearest_hits on all online cores over a ray sample.
+
+    With `got` (the GPU's records of the whole batch) the oracle then answers every ray
+    of the batch (untimed) and the parity rules (oracle/parity.py) are applied to all of
+    them: the third value returned is that report."""
     from oracle import cpu as orc
+    from oracle import parity
 
     rng = np.random.default_rng(seed)
     idx = np.sort(rng.choice(len(rays), size=min(sample_rays, len(rays)), replace=False))
@@ -182,10 +256,18 @@ def cpu_baseline(tris, rays, sample_rays: int, seed: int = 0):
     t0 = time.perf_counter()
     bvh.nearest_hits(sample, threads=cores)
     q = time.perf_counter() - t0
+    rep = None
+    if got is not None:
+        t0 = time.perf_counter()
+        want = bvh.nearest_hits(rays, threads=cores)
+        rep = parity.check(got, want, tags, tris, rays, orc, threads=cores)
+        rep["checked_against"] = ("oracle port of the reference CPU backend (pinned bit for "
+                                  "bit to the reference's golden records), every ray")
+        rep["check_s"] = time.perf_counter() - t0
     return bvh, {"value": len(sample) / q / 1e6, "unit": "Mrays/s", "cores": cores,
                  "kind": "port", "build_mtris_s": len(tris) / build_s / 1e6,
                  "sample": f"{len(sample):,} rays drawn uniformly from the batch; SAH build of "
-                           f"all {len(tris):,} tris on 1 thread ({build_s:.1f} s)"}
+                           f"all {len(tris):,} tris on 1 thread ({build_s:.1f} s)"}, rep
 
 
 def run_reference(args, world, rank):
@@ -372,7 +454,29 @@ def leg_batch(b, stream, steps, n_scenes=4096, log=None):
     return res
 
 
-def leg_precision(b, stream, steps):
+def precision_parity(d_t, d_r, d_out, n_t, n_r, lay, k, seed=5):
+    """The CPU leg's check of the clustered soup: k rays drawn uniformly from the batch,
+    answered by the oracle's exhaustive search over all triangles (the reference's
+    answer up to ties and tree-dependent rays, which the parity rules handle) and
+    compared with the GPU's records of those rays."""
+    from oracle import cpu as orc
+    from oracle import parity
+
+    t0 = time.perf_counter()
+    idx = np.sort(np.random.default_rng(seed).choice(n_r, size=k, replace=False))
+    tris = d_t.cpu().numpy().reshape(n_t, 9)
+    rays = np.ascontiguousarray(d_r.cpu().numpy().reshape(n_r, 6)[idx])
+    got = d_out.cpu().numpy().view(lay.numpy_dtype()).reshape(-1)[idx]
+    cores = os.cpu_count() or 1
+    want = orc.brute_force(tris, rays, threads=cores)
+    rep = parity.check(got, want, lay.tags, tris, rays, orc, threads=cores)
+    rep["checked_against"] = (f"oracle exhaustive search over all {n_t:,} triangles, "
+                              f"{k:,} rays drawn uniformly from the batch")
+    rep["check_s"] = time.perf_counter() - t0
+    return rep
+
+
+def leg_precision(b, stream, steps, check_rays=0):
     """The clustered soup: 8,388,608 tris in 256 Gaussian clusters, 16,777,216 random
     rays, tags uv/t/primitive_id/valid; FP32 against compressed nodes (records must be
     byte-identical) and the FP64 t error of the answers."""
@@ -412,6 +516,8 @@ def leg_precision(b, stream, steps):
     sc = b.t_error(d_t.data_ptr(), n_t, d_r.data_ptr(), n_r, outs[0].data_ptr(), C0_TAGS)
     res["t_error_vs_fp64"] = sc
     res["compressed_over_fp32"] = res["compressed"]["mrays_s"] / res["fp32"]["mrays_s"]
+    if check_rays:
+        res["parity"] = precision_parity(d_t, d_r, outs[0], n_t, n_r, lay, check_rays)
     del d_t, d_r, outs
     torch.cuda.empty_cache()
     return res
@@ -708,6 +814,9 @@ def run_gpu(args, world, rank):
     b.sync()
     clk = clocks.stop()
     ms = [s.elapsed_time(e) for s, e in ev]
+    # The records of the timed steps: checked against the oracle (every ray, CPU leg),
+    # against the host-buffer call and against compressed nodes below.
+    fp32_out = d_out.clone()
     total_ms = max_over_ranks(float(sum(ms)), world)
     torch.cuda.synchronize()
     mrays = aggregate_mrays(world, n, args.steps, total_ms)
@@ -735,6 +844,8 @@ def run_gpu(args, world, rank):
     e2e = n / float(np.median(e2e_t)) / 1e6
     in_place = b.stat("in_place") == 1.0
     assert rec["valid"].sum() > 0
+    got_host = fp32_out.cpu()
+    e2e_identical = bool(torch.equal(h_out, got_host))
 
     def timed(f, k):
         f()
@@ -764,17 +875,18 @@ def run_gpu(args, world, rank):
     e2e_pageable_copy = timed(e2e_pageable_step, max(1, min(args.steps, 5)))
     b.set_option("host_direct", 1)
 
-    # Roofline of the traversal kernel (algorithmic bytes per launch / launch time).
+    # Rooflines of the traversal kernel: issue, L2 and HBM (traversal_rooflines).
     b_ray = 24 + lay.size + v_nodes * node_size + v_tris * 48
     per_launch_s = total_ms / 1e3 / args.steps
-    achieved = n * b_ray / per_launch_s / 1e9
     peak, peak_kind = measured_peaks()
-    traffic = committed_profile("dram_bytes_per_launch")
-    # What DRAM itself carries: the profiled bytes of one launch over its live duration
-    # (node fetches the L2 serves are in the algorithmic bytes, not here).
-    dram = traffic / per_launch_s / 1e9 if traffic else None
-    # The bytes a ray must move at least (its 24-byte ray in, its record out).
-    io_floor = n * (24 + lay.size) / per_launch_s / 1e9
+    probe = torch.empty(48 << 20, dtype=torch.uint8, device="cuda")
+    probe.random_(0, 256)
+    torch.cuda.synchronize()
+    l2_peak = max(b.probe_read_gbs(probe.data_ptr(), probe.numel(), 50) for _ in range(3))
+    del probe
+    sm_mhz = clk["sm_mhz"] or 2070.0
+    roof = traversal_rooflines(n, per_launch_s, b_ray, v_nodes, v_tris, node_size, lay.size,
+                               peak, peak_kind, l2_peak, b.stat("sms"), sm_mhz)
 
     # Compressed nodes on the same batch (same hits; checked in the tests).
     b.set_option("node_format", 1)
@@ -791,6 +903,8 @@ def run_gpu(args, world, rank):
     b.sync()
     comp_ms = float(sum(s.elapsed_time(e) for s, e in ev2))
     comp_node_size = b.stat("node_size")
+    comp_identical = bool(torch.equal(d_out, fp32_out))
+    del fp32_out
     b.set_option("node_format", 0)
 
     # Coherent and incoherent rays apart (the primary rays, the offset secondary rays),
@@ -838,18 +952,14 @@ def run_gpu(args, world, rank):
                    "copy_pipeline_value": e2e_copy,
                    "pageable_value": e2e_pageable,
                    "pageable_path": "in place" if pg_in_place else "chunked copy pipeline",
-                   "pageable_copy_pipeline_value": e2e_pageable_copy},
+                   "pageable_copy_pipeline_value": e2e_pageable_copy,
+                   "records_identical_to_device_run": e2e_identical},
            # per step: the regular pass and the deferred pass of k_trace8
            "gpu_launches": 2 * args.steps,
-           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                        "frac": achieved / peak, "traffic": traffic,
-                        "peak_source": peak_kind,
-                        "bytes_per_ray": b_ray, "node_visits_per_ray": v_nodes,
-                        "tri_tests_per_ray": v_tris, "node_bytes": node_size,
-                        "io_floor_gbs": io_floor, "io_floor_frac": io_floor / peak,
-                        "dram_gbs": dram, "dram_frac": dram / peak if dram else None,
-                        "l2_hit_rate_pct": committed_profile("l2_hit_rate_pct")},
-           "build": {"mtris_s_device": len(tris) / build_dev_ms / 1e3,
+           "roofline": roof,
+           "build": {"roofline": build_roofline(len(tris), b.stat("n_nodes"), build_dev_ms,
+                                                lbvh_ms, lbvh_nodes, peak, peak_kind),
+                     "mtris_s_device": len(tris) / build_dev_ms / 1e3,
                      "mtris_s_e2e": len(tris) / build_e2e_ms / 1e3,
                      "ms_device": build_dev_ms, "nodes": b.stat("n_nodes"),
                      "depth": b.stat("depth"),
@@ -857,7 +967,8 @@ def run_gpu(args, world, rank):
                      "lbvh": {"ms_device": lbvh_ms, "mtris_s_device": len(tris) / lbvh_ms / 1e3,
                               "nodes": lbvh_nodes}},
            "compressed": {"value": world * n * args.steps / (comp_ms / 1e3) / 1e6,
-                          "unit": "Mrays/s", "node_bytes": comp_node_size},
+                          "unit": "Mrays/s", "node_bytes": comp_node_size,
+                          "records_identical_to_fp32": comp_identical},
            "coherence": coherence,
            "clocks": clk}
     del d_rays, d_out, flush
@@ -868,7 +979,8 @@ def run_gpu(args, world, rank):
     if "small" in legs:
         out["small"] = leg_small(b, stream, min(args.steps, 20))
     if "precision" in legs:
-        out["precision"] = leg_precision(b, stream, min(args.steps, 10))
+        out["precision"] = leg_precision(b, stream, min(args.steps, 10),
+                                         check_rays=0 if args.no_cpu else 512)
     if "batch" in legs:
         out["batch"] = leg_batch(b, stream, min(args.steps, 10), log=log)
     if "serving" in legs:
@@ -876,8 +988,10 @@ def run_gpu(args, world, rank):
     if "camera" in legs:
         out["camera"] = leg_camera(b, stream, min(args.steps, 10), log=log)
     if rank == 0 and not args.no_cpu:
-        _, cb = cpu_baseline(tris, rays, sample_rays=131_072)
+        got = got_host.numpy().view(lay.numpy_dtype()).reshape(-1)
+        _, cb, rep = cpu_baseline(tris, rays, sample_rays=131_072, got=got)
         out["cpu_baseline"] = cb
+        out["parity"] = rep
     if rank == 0:
         print(json.dumps(out), flush=True)
     b.shutdown()

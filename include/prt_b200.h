@@ -324,6 +324,15 @@ void prt_b200_free(void *p);
 int prt_b200_generate(prt_b200_ctx *ctx, int kind, uint64_t seed, uint64_t n, double param,
                       void *d_out, void *stream);
 
+/* Measurement helper (no counterpart in the reference): *ms = device time of `passes`
+ * read passes over the device buffer d_buf (bytes, 32-byte aligned, >= 128 KiB) with the
+ * traversal's own 32-byte read-only loads, after one untimed pass; each pass a block
+ * reads a different slice than before, so L1 does not serve it.  A buffer under the
+ * L2 capacity gives the L2 -> SM read bandwidth (bytes x passes / time), a larger one
+ * HBM's.  Synchronous, on the context's stream. */
+int prt_b200_probe_read(prt_b200_ctx *ctx, const void *d_buf, uint64_t bytes, int passes,
+                        float *ms);
+
 /* FP64 scorer of t (no counterpart in portableRT; measurement only).  For every valid
  * record of a nearest_hits result (device buffers; the records need t, primitive_id and
  * valid), recomputes t by the Möller-Trumbore formula of core.hpp:27-65 in double on the

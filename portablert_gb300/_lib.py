@@ -24,7 +24,7 @@ EXPORTS = (
     "prt_b200_server_create", "prt_b200_server_destroy", "prt_b200_server_submit",
     "prt_b200_server_wait", "prt_b200_server_stat", "prt_b200_server_last_error",
     "prt_b200_nearest_hits_camera", "prt_b200_camera_rays", "prt_b200_shade_lambert",
-    "prt_b200_obj_load", "prt_b200_gltf_load", "prt_b200_free",
+    "prt_b200_obj_load", "prt_b200_gltf_load", "prt_b200_free", "prt_b200_probe_read",
 )
 
 
@@ -135,6 +135,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
     L.prt_b200_t_error.restype = c_int
     L.prt_b200_t_error.argtypes = [vp, vp, c_u64, vp, c_u64, vp, c_u32, c_u32, ctypes.c_char_p,
                                    ctypes.POINTER(ctypes.c_double)]
+    L.prt_b200_probe_read.restype = c_int
+    L.prt_b200_probe_read.argtypes = [vp, vp, c_u64, c_int, ctypes.POINTER(ctypes.c_float)]
     L.prt_b200_set_option.restype = c_int
     L.prt_b200_set_option.argtypes = [vp, ctypes.c_char_p, ctypes.c_int64]
     L.prt_b200_get_stat.restype = c_int

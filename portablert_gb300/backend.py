@@ -129,6 +129,15 @@ class B200Backend:
         return {"max_abs": r[0], "max_rel": r[1], "mean_abs": r[2], "scored": int(r[3]),
                 "exact": int(r[4]), "unscored": int(r[5])}
 
+    def probe_read_gbs(self, buf_ptr: int, nbytes: int, passes: int = 50) -> float:
+        """Read bandwidth (GB/s) of the traversal's 32-byte loads over a device buffer
+        (prt_b200_probe_read): under the L2 capacity the L2 -> SM bandwidth."""
+        self._need()
+        ms = ctypes.c_float()
+        self._check(self._L.prt_b200_probe_read(self.ctx, buf_ptr, nbytes, passes,
+                                                ctypes.byref(ms)))
+        return nbytes * passes / (ms.value / 1e3) / 1e9
+
     # -- tuning and statistics ----------------------------------------------------------
     def set_option(self, key: str, value: int) -> None:
         self._need()

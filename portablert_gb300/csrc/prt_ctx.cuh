@@ -49,8 +49,9 @@ struct prt_b200_ctx {
 	prt::BuildScratch ws;
 	prt::DevBuf tris_in;
 	prt::DevBuf rays_buf, out_buf;
-	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [16..31] visit counters,
-	                  // [32..35] ray counter of the second compute stream
+	prt::DevBuf work; // [0..3] ray counter, [4..7] error word, [8..15] deferred-pass
+	                  // words, [16..31] visit counters, [32..47] ray counter and deferred
+	                  // words of the second compute stream, [48..51] the read probe's sink
 	// The host-buffer call splits large batches into chunks and overlaps the copy-in of a
 	// chunk, the traversal of the one before and the copy-out of the one before that.
 	static constexpr int kPipe = 16; // most chunks of one call

@@ -24,6 +24,20 @@ def load_golden(name):
     return out
 
 
+def load_c0_golden(tris, rays):
+    """The reference's records for the small configuration (4,096-triangle soup, 65,536
+    rays, seed 0; tags t, primitive_id, uv, valid).  The inputs are regenerated by the
+    seeded generator; their SHA-256 must match the one stored with the records."""
+    import hashlib
+
+    from oracle.cpu import HIT_DTYPE
+
+    z = np.load(os.path.join(GOLDEN, "c0_soup.npz"))
+    assert hashlib.sha256(np.ascontiguousarray(tris).tobytes()).hexdigest() == str(z["tris_sha256"])
+    assert hashlib.sha256(np.ascontiguousarray(rays).tobytes()).hexdigest() == str(z["rays_sha256"])
+    return {"full": z["full"].reshape(-1).view(HIT_DTYPE), "tags": tuple(z["tags"].tolist())}
+
+
 GOLDEN_SETS = ("kat", "axis_grid", "inside_soup", "duplicates", "one_tri", "two_tris",
                "zero_tris", "soup_small")
 

@@ -125,9 +125,35 @@ SETS = {
 }
 
 
+C0_TAGS = ("t", "primitive_id", "uv", "valid")
+
+
+def c0_soup():
+    """The small configuration exactly: 4,096-triangle soup and 65,536 rays (seed 0).
+    Inputs are not stored (the seeded generator rebuilds them; their SHA-256 pins it);
+    of the reference's records only the configuration's tags are kept (p is zeroed, as
+    are u, v and primitive_id of misses, which the reference leaves unwritten)."""
+    import hashlib
+
+    tris, rays = W.soup(seed=0, n_tris=4096, n_rays=65536)
+    full, _, _ = cpu.run_reference(tris, rays)
+    full = full.copy()
+    for f in ("px", "py", "pz"):
+        full[f] = 0
+    miss = full["valid"] == 0
+    for f in ("u", "v", "primitive_id"):
+        full[f][miss] = 0
+    np.savez_compressed(os.path.join(HERE, "c0_soup.npz"),
+                        full=full.view(np.uint8).reshape(-1, 32), tags=np.array(C0_TAGS),
+                        tris_sha256=hashlib.sha256(tris.tobytes()).hexdigest(),
+                        rays_sha256=hashlib.sha256(rays.tobytes()).hexdigest())
+    print("c0_soup", tris.shape[0], rays.shape[0], int((~miss).sum()), "hits")
+
+
 def main():
     if not cpu.ref_available():
         raise SystemExit("build oracle/_ref/ref_oracle first (make -C oracle ref)")
+    c0_soup()
     for name, fn in SETS.items():
         tris, rays = fn()
         combos = name == "soup_small"

@@ -1,94 +1,3 @@
-"""Parity rules between a backend's hit records and the reference's.
-
-* ``valid`` and ``primitive_id`` bit-exact; t, u, v, p bit-exact (the kernels use the
-  reference's operation order without FMA, so no ulp tolerance is needed: TOL_ULP = 0).
-* A ray whose closest accepted triangles tie in t may report any of them: such rays
-  are listed, and checked by equal t and by re-running the reference arithmetic on the
-  reported triangle (it must be accepted with exactly that t, u and v).
-* Misses: only t (= +inf) and valid are compared; the reference leaves u, v and
-  primitive_id unwritten there.
-"""
-from __future__ import annotations
-
-import numpy as np
-
-TOL_ULP = 0
-
-
-def _bits(a):
-    return np.ascontiguousarray(a).view(np.uint32)
-
-
-def _same_float(a, b):
-    """Bit-identical, treating every NaN as equal (NaN payloads differ by platform)."""
-    a = np.ascontiguousarray(a, np.float32)
-    b = np.ascontiguousarray(b, np.float32)
-    both_nan = np.isnan(a) & np.isnan(b)
-    return (_bits(a) == _bits(b)) | both_nan
-
-
-def tri_box_pass(tri, ray):
-    """The reference slab test (bvh.hpp:195-222) on one triangle's own box, in numpy
-    float32 with the select min/max."""
-    t = np.asarray(tri, np.float32).reshape(3, 3)
-    o = np.asarray(ray[:3], np.float32)
-    d = np.asarray(ray[3:], np.float32)
-
-    def rmin(a, b):
-        return b if b < a else a
-
-    def rmax(a, b):
-        return b if a < b else a
-
-    lo = [rmin(t[0, k], rmin(t[1, k], t[2, k])) for k in range(3)]
-    hi = [rmax(t[0, k], rmax(t[1, k], t[2, k])) for k in range(3)]
-    with np.errstate(all="ignore"):
-        f = [np.float32(1.0) / d[k] for k in range(3)]
-        ts = [np.float32((np.float32(lo[k]) - o[k]) * f[k]) for k in range(3)] + \
-             [np.float32((np.float32(hi[k]) - o[k]) * f[k]) for k in range(3)]
-    t1, t3, t5, t2, t4, t6 = ts
-    tmin = rmax(rmax(rmin(t1, t2), rmin(t3, t4)), rmin(t5, t6))
-    tmax = rmin(rmin(rmax(t1, t2), rmax(t3, t4)), rmax(t5, t6))
-    return not (tmax < 0) and not (tmin > tmax)
-
-
-def compare(got, want, tags, tris, rays, oracle=None):
-    """Checks `got` (structured array, fields per `tags`) against `want` (the reference's
-    full records).  Returns a report dict; report['bad'] lists failing ray indices."""
-    tags = set(tags)
-    n = len(want)
-    wv = want["valid"] != 0
-    ok = np.ones(n, bool)
-    if "valid" in tags:
-        ok &= (got["valid"] != 0) == wv
-    if "t" in tags:
-        ok &= _same_float(got["t"], want["t"]) | (~wv & np.isinf(got["t"]) & (got["t"] > 0))
-    same_pid = np.ones(n, bool)
-    if "primitive_id" in tags:
-        same_pid = got["primitive_id"] == want["primitive_id"]
-    exact = np.ones(n, bool)
-    if "uv" in tags:
-        exact &= _same_float(got["u"], want["u"]) & _same_float(got["v"], want["v"])
-    if "p" in tags:
-        for f in ("px", "py", "pz"):
-            exact &= _same_float(got[f], want[f])
-    hit_ok = same_pid & exact
-    ties = []
-    if "primitive_id" in tags:
-        for i in np.flatnonzero(wv & ~hit_ok):
-            # A different triangle is allowed only on an exact tie in t.
-            pid = int(got["primitive_id"][i])
-            if oracle is None or pid >= len(tris):
-                continue
-            acc, t, u, v = oracle.intersect_tri(tris[pid], rays[i])
-            if acc and tri_box_pass(tris[pid], rays[i]) and \
-                    np.float32(t) == np.float32(want["t"][i]):
-                if "uv" in tags and not (np.float32(u) == got["u"][i] and
-                                         np.float32(v) == got["v"][i]):
-                    continue
-                hit_ok[i] = True
-                ties.append(int(i))
-    ok &= ~wv | hit_ok
-    bad = np.flatnonzero(~ok)
-    return {"n": n, "hits": int(wv.sum()), "ties": ties, "bad": bad.tolist(),
-            "n_bad": int(bad.size)}
+"""The parity rules (oracle/parity.py), under the name the tests import."""
+from oracle.parity import (TOL_ULP, _same_float, check, compare, exact_vs_leaf_only,  # noqa: F401
+                           tree_dependent_rays, tri_box_pass)

@@ -14,8 +14,8 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_SETS, ROOT, load_golden
-from parity import _same_float, compare
+from conftest import GOLDEN_SETS, ROOT, load_c0_golden, load_golden
+from parity import _same_float, check, compare, exact_vs_leaf_only
 from portablert_gb300 import hitreg, workloads
 
 pytestmark = pytest.mark.gpu
@@ -24,49 +24,13 @@ FULL_TAGS = hitreg.TAGS
 
 
 def _exact_vs_leaf_only(got, bf, tags=FULL_TAGS):
-    """Bit-exact agreement with the order-independent leaf-only answer (ties -> lower
-    primitive id), which is what the kernels compute by construction."""
-    v = bf["valid"] != 0
-    bad = np.zeros(len(bf), bool)
-    if "valid" in tags:
-        bad |= (got["valid"] != 0) != v
-    if "t" in tags:
-        bad |= ~_same_float(got["t"], bf["t"])
-    if "primitive_id" in tags:
-        bad |= v & (got["primitive_id"] != bf["primitive_id"])
-    if "uv" in tags:
-        bad |= v & ~(_same_float(got["u"], bf["u"]) & _same_float(got["v"], bf["v"]))
-    if "p" in tags:
-        for f in ("px", "py", "pz"):
-            bad |= v & ~_same_float(got[f], bf[f])
-    return np.flatnonzero(bad)
-
-
-def _tree_dependent(tris, rays, oracle):
-    """Tree-dependent rays (see oracle.cpu.tree_dependent); only rays whose x
-    reciprocal is infinite can be, so only those are searched exhaustively."""
-    with np.errstate(divide="ignore"):
-        cand = np.flatnonzero(np.isinf(np.float32(1.0) / rays[:, 3]))
-    dep = np.zeros(len(rays), bool)
-    bf = np.zeros(len(rays), oracle.HIT_DTYPE)
-    if cand.size:
-        d, a, _ = oracle.tree_dependent(tris, rays[cand])
-        dep[cand] = d
-        bf[cand] = a
-    return dep, bf
+    return exact_vs_leaf_only(got, bf, tags)
 
 
 def _check_against_reference(got, ref, tris, rays, oracle, tags=FULL_TAGS):
-    dep, bf = _tree_dependent(tris, rays, oracle)
-    rep = compare(got, ref, tags, tris, rays, oracle)
-    bad = [i for i in rep["bad"] if not dep[i]]
-    assert rep["n_bad"] - sum(1 for i in rep["bad"] if dep[i]) == len(bad)
-    assert not bad, f"{len(bad)} rays differ from the reference, e.g. {bad[:5]}"
-    # Tree-dependent rays: ours must be the leaf-only answer exactly.
-    idx = np.flatnonzero(dep)
-    if idx.size:
-        assert _exact_vs_leaf_only(got[idx], bf[idx], tags).size == 0
-    return rep, int(dep.sum())
+    rep = check(got, ref, tags, tris, rays, oracle)
+    assert rep["n_bad"] == 0, f"{rep['n_bad']} rays differ from the reference, e.g. {rep['bad'][:5]}"
+    return rep, rep["tree_dependent"]
 
 
 @pytest.mark.parametrize("name", GOLDEN_SETS)
@@ -101,6 +65,10 @@ def test_soup_small_config_bit_exact(gpu_backend, oracle_lib):
     ref = oracle_lib.BVH(tris).nearest_hits(rays)
     rep, _ = _check_against_reference(got, ref, tris, rays, oracle_lib, tags)
     assert rep["hits"] > 30000
+    # And against the reference's own records for exactly these inputs (golden fixture).
+    g = load_c0_golden(tris, rays)
+    rep, _ = _check_against_reference(got, g["full"], tris, rays, oracle_lib, tags)
+    assert rep["hits"] == int((g["full"]["valid"] != 0).sum())
 
 
 @pytest.mark.parametrize("tags", hitreg.TAG_COMBOS, ids=hitreg.hitreg_name)

@@ -30,6 +30,25 @@ def test_restated_oracle_matches_reference_golden(oracle_lib, name):
     _assert_same_full(mine, g["full"])
 
 
+def test_restated_oracle_matches_reference_small_config(oracle_lib):
+    """The small configuration exactly (4,096 triangles, 65,536 rays): the restatement
+    equals the reference's records on its tags t, primitive_id, uv, valid."""
+    from conftest import load_c0_golden
+
+    tris, rays = workloads.soup(seed=0, n_tris=4096, n_rays=65536)
+    g = load_c0_golden(tris, rays)
+    ref = g["full"]
+    mine = oracle_lib.BVH(tris).nearest_hits(rays, threads=4)
+    v = ref["valid"] != 0
+    assert g["tags"] == ("t", "primitive_id", "uv", "valid")
+    assert v.sum() > 30000
+    assert np.array_equal(mine["valid"], ref["valid"])
+    assert _same_float(mine["t"], ref["t"]).all()
+    assert np.array_equal(mine["primitive_id"][v], ref["primitive_id"][v])
+    for f in ("u", "v"):
+        assert _same_float(mine[f][v], ref[f][v]).all(), f
+
+
 def test_kat_values(oracle_lib):
     # examples/validation/main.cpp:66-111: t=1, u=0.3, v=0.5, id 0, p=(0.1,0,0) +-1e-4.
     g = load_golden("kat")
