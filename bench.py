@@ -660,26 +660,24 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
     return res
 
 
+BUNNY_OBJ = os.path.join(ROOT, "tests", "golden", "bunny.obj")
+
+
 def leg_camera(b, stream, steps, size=4096, log=None):
     """The examples' bunny set-up (4096 x 4096 pinhole sensor rays from (0, -0.02, -0.3),
-    sensor 0.05 wide at 0.05) on a bunny-sized synthetic mesh read back through the OBJ
-    reader (the bunny file is not part of this repository): rays built inside the
-    traversal (no ray buffer) against the same rays from a buffer, the Lambert shading
-    pass, and a frame rendered to pinned host memory (camera -> hits -> RGBA8 -> host).
-    At this scale the examples' Lambert leaves normals unnormalised (|N| < 0.001) and
-    the image is black, as the reference's would be; the cost is the same."""
-    import tempfile
-
+    sensor 0.05 wide at 0.05) on the examples' own bunny mesh (tests/golden/bunny.obj,
+    4,968 triangles) read through the OBJ reader: rays built inside the traversal (no ray
+    buffer) against the same rays from a buffer, the Lambert shading pass, and a frame
+    rendered to pinned host memory (camera -> hits -> RGBA8 -> host).  The valid mask is
+    compared with the one the bunny program writes (tests/golden/bunny_mesh.npz).  At
+    this scale the examples' Lambert leaves normals unnormalised (|N| < 0.001) and the
+    image is black, as the reference's would be; the cost is the same."""
     import torch
 
     from portablert_gb300 import obj
     from portablert_gb300._lib import Camera
 
-    v, f = obj.blob_mesh(60, 84)
-    with tempfile.TemporaryDirectory() as td:
-        path = os.path.join(td, "blob.obj")
-        obj.write_obj(path, v, f)
-        tris = obj.load_obj(path)
+    tris = obj.load_obj(BUNNY_OBJ)
     b.set_tris(tris)
     cam = Camera()
     cam.width = cam.height = size
@@ -706,7 +704,7 @@ def leg_camera(b, stream, steps, size=4096, log=None):
         shade()
         h_rgba.copy_(rgba, non_blocking=True)
 
-    res = {"workload": f"{len(tris):,}-tri bunny-sized mesh (OBJ), {size}x{size} pinhole "
+    res = {"workload": f"the examples' bunny ({len(tris):,} tris, OBJ), {size}x{size} pinhole "
                        "sensor rays of the examples' bunny set-up; tags t, primitive_id, valid",
            "n_tris": len(tris), "n_rays": n}
     for name, fn in (("fused_camera", fused), ("ray_buffer", buffered), ("shade", shade)):
@@ -727,8 +725,14 @@ def leg_camera(b, stream, steps, size=4096, log=None):
     fms = 1e3 * (time.perf_counter() - t0) / k
     res["frame_to_host"] = {"ms": fms, "fps": 1e3 / fms, "mrays_s": n / fms / 1e3,
                             "d2h_bytes": 4 * n}
+    fused()
+    torch.cuda.synchronize()
     recs = rec.cpu().numpy().view(lay.numpy_dtype())
     res["hit_pixels"] = int((recs["valid"] != 0).sum())
+    if size == 4096:
+        z = np.load(os.path.join(ROOT, "tests", "golden", "bunny_mesh.npz"))
+        res["mask_equals_bunny_program"] = bool(
+            np.array_equal(np.packbits(recs["valid"] != 0), z["mask_bits"]))
     del rec, rays, rgba, h_rgba
     torch.cuda.empty_cache()
     return res

@@ -8,12 +8,16 @@ stb), on a generated bunny-sized mesh:
 * camera_validation.npz: the validation program's 1,048,576 rays -- the SHA-256 of their
   bytes and every 1021st ray;
 * bunny_blob.npz: the mesh's triangles (as read through the OBJ reader) and the valid
-  mask the bunny program writes for its 4096 x 4096 camera, bit-packed, with its SHA-256.
+  mask the bunny program writes for its 4096 x 4096 camera, bit-packed, with its SHA-256;
+* bunny.obj: the examples' own mesh (examples/common/bunny.obj, 4,968 triangles), copied
+  as test data, and bunny_mesh.npz: the valid mask the bunny program writes for it (the
+  program run unmodified on that file), bit-packed, with the SHA-256 of mask and file.
 
     python tests/golden/make_examples_golden.py      (needs the reference tree)
 """
 import hashlib
 import os
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -24,6 +28,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
 
+from oracle.refdir import reference_path  # noqa: E402
 from portablert_gb300 import obj  # noqa: E402
 
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
@@ -46,6 +51,21 @@ def main():
         subprocess.run([os.path.join(REF_BIN, "bunny_example")], env=env, cwd=td, check=True,
                        input=b"0\n", stdout=subprocess.DEVNULL)
         mask = np.fromfile(mask_path, np.uint8)
+    bunny_src = reference_path("examples", "common", "bunny.obj")
+    bunny_dst = os.path.join(HERE, "bunny.obj")
+    shutil.copyfile(bunny_src, bunny_dst)
+    with tempfile.TemporaryDirectory() as td:
+        env = dict(os.environ, PRT_STUB_OBJ=bunny_dst,
+                   PRT_STUB_IMAGE=os.path.join(td, "mask.bin"))
+        subprocess.run([os.path.join(REF_BIN, "bunny_example")], env=env, cwd=td, check=True,
+                       input=b"0\n", stdout=subprocess.DEVNULL)
+        bmask = np.fromfile(os.path.join(td, "mask.bin"), np.uint8)
+    with open(bunny_dst, "rb") as f:
+        obj_sha = hashlib.sha256(f.read()).hexdigest()
+    np.savez_compressed(os.path.join(HERE, "bunny_mesh.npz"),
+                        mask_bits=np.packbits(bmask != 0), n=len(bmask),
+                        sha256=hashlib.sha256(bmask.tobytes()).hexdigest(), obj_sha256=obj_sha)
+    print(f"bunny.obj: mask {len(bmask)} ({int((bmask != 0).sum())} lit)")
     idx = np.arange(0, len(rays), 1021)
     np.savez_compressed(os.path.join(HERE, "camera_validation.npz"),
                         sha256=hashlib.sha256(rays.tobytes()).hexdigest(), n=len(rays),

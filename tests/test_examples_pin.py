@@ -43,6 +43,23 @@ def test_oracle_equals_bunny_program(oracle_lib):
     assert hashlib.sha256(mask.tobytes()).hexdigest() == str(z["sha256"])
 
 
+def test_oracle_equals_bunny_program_on_the_bunny(oracle_lib):
+    """The examples' own bunny mesh (tests/golden/bunny.obj) through the OBJ reader, the
+    oracle's camera and traversal: the bunny program's valid mask bit for bit."""
+    from portablert_gb300 import obj
+
+    z = np.load(os.path.join(GOLDEN, "bunny_mesh.npz"))
+    path = os.path.join(GOLDEN, "bunny.obj")
+    with open(path, "rb") as f:
+        assert hashlib.sha256(f.read()).hexdigest() == str(z["obj_sha256"])
+    tris = obj.load_obj(path)
+    rays = oracle_lib.camera_rays(*bunny_camera_args())
+    hits = oracle_lib.BVH(tris).nearest_hits(rays)
+    mask = np.where(hits["valid"] != 0, 255, 0).astype(np.uint8)
+    assert np.array_equal(np.packbits(mask != 0), z["mask_bits"])
+    assert hashlib.sha256(mask.tobytes()).hexdigest() == str(z["sha256"])
+
+
 @pytest.mark.skipif(not os.path.isdir(reference_path("examples")),
                     reason="the reference's example sources are not present")
 def test_fixtures_match_the_programs_run_now():

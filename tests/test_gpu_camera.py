@@ -201,6 +201,34 @@ def test_device_camera_equals_validation_program(gpu_backend):
     assert hashlib.sha256(out.cpu().numpy().tobytes()).hexdigest() == str(z["sha256"])
 
 
+def test_bunny_mesh_equals_bunny_program(gpu_backend):
+    """The examples' own bunny (tests/golden/bunny.obj) read through the OBJ reader and
+    traced by the fused camera traversal at 4096 x 4096: the bunny program's valid mask
+    (the program run unmodified on that file) bit for bit."""
+    import os
+
+    import torch
+
+    from conftest import GOLDEN
+    from portablert_gb300 import obj
+
+    z = np.load(os.path.join(GOLDEN, "bunny_mesh.npz"))
+    tris = obj.load_obj(os.path.join(GOLDEN, "bunny.obj"))
+    assert tris.shape == (4968, 9)
+    gpu_backend.set_tris(tris)
+    d = dict(width=4096, height=4096, form=0, pos=(0.0, -0.02, -0.3), sensor_size=0.05,
+             sensor_dist=0.05, sensor_z=float(F32(-0.3) + F32(0.05)))
+    tags = ("valid",)
+    lay = hitreg.layout(tags)
+    rec = torch.zeros(4096 * 4096 * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    gpu_backend.nearest_hits_camera(_ccam(d), rec.data_ptr(), tags)
+    gpu_backend.sync()
+    valid = rec.cpu().numpy().view(lay.numpy_dtype())["valid"]
+    assert int((valid != 0).sum()) == 2_914_808
+    assert np.array_equal(np.packbits(valid != 0), z["mask_bits"])
+
+
 def test_bunny_setup_equals_bunny_program(gpu_backend):
     """The bunny program's 4096 x 4096 valid mask on the fixture mesh, from the fused
     camera traversal."""

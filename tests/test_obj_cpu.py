@@ -10,7 +10,8 @@ from oracle.refdir import reference_path
 from portablert_gb300 import obj
 from portablert_gb300._lib import PrtError
 
-BUNNY = reference_path("examples", "common", "bunny.obj")
+BUNNY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "bunny.obj")
+REF_BUNNY = reference_path("examples", "common", "bunny.obj")
 
 
 def _py_parse(text):
@@ -87,13 +88,19 @@ def test_empty_file(tmp_path):
     assert obj.load_obj(str(p)).shape == (0, 9)
 
 
-@pytest.mark.skipif(not os.path.exists(BUNNY), reason="reference examples not present")
 def test_examples_bunny():
+    """The examples' own mesh (tests/golden/bunny.obj, a copy of examples/common/bunny.obj)."""
     got = obj.load_obj(BUNNY)
     with open(BUNNY) as f:
         want = _py_parse(f.read())
     assert got.shape == (4968, 9)
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.skipif(not os.path.exists(REF_BUNNY), reason="reference examples not present")
+def test_bunny_fixture_is_the_examples_mesh():
+    with open(BUNNY, "rb") as a, open(REF_BUNNY, "rb") as b:
+        assert a.read() == b.read()
 
 
 def test_number_forms_round_like_python(tmp_path):
