@@ -22,6 +22,7 @@
 // Binning uses box centres; a task deeper than 48 levels, or one whose centres all fall
 // into one bin on every axis, is split into halves instead.  All positions, node ids and
 // list slots are checked before they are written; a failed check sets kErrSah.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -281,15 +282,16 @@ __device__ __forceinline__ uint32_t new_node(const SahArgs &A, uint32_t k) {
 }
 
 // Files a child range as a task of the right tier (called by one lane).  `frame` gives
-// the binning frame of a large child.
-__device__ void add_child(const SahArgs &A, int out_par, uint32_t begin, uint32_t count,
-                          uint32_t node, uint32_t parent, uint32_t buf, uint32_t depth,
-                          const Box6 *frame, const float *pflo, const float *pfsc) {
+// the binning frame of a large child.  Returns the list slot of a large child, whose
+// bins the calling warp then clears (init_new_bins), else kNone.
+__device__ uint32_t add_child(const SahArgs &A, int out_par, uint32_t begin, uint32_t count,
+                              uint32_t node, uint32_t parent, uint32_t buf, uint32_t depth,
+                              const Box6 *frame, const float *pflo, const float *pfsc) {
 	if (count > kLarge) {
 		const uint32_t i = atomicAdd(&A.ctr[kCtrLarge + out_par], 1u);
 		if (i >= A.max_large) {
 			flag(A.err);
-			return;
+			return kNone;
 		}
 		SahTask t;
 		t.begin = begin;
@@ -315,16 +317,12 @@ __device__ void add_child(const SahArgs &A, int out_par, uint32_t begin, uint32_
 		}
 		t.cur_l = t.cur_r = 0;
 		A.large[out_par][i] = t;
-		uint32_t *b = A.bins[out_par] + (size_t)i * kBinWords;
-		for (int k = 0; k < kBinWords; ++k) {
-			const int w = k % 7;
-			b[k] = w < 3 ? kOrdPosInf : (w < 6 ? kOrdNegInf : 0u);
-		}
+		return i;
 	} else if (count > kSmall) {
 		const uint32_t i = atomicAdd(&A.ctr[kCtrMid + out_par], 1u);
 		if (i >= A.max_mid) {
 			flag(A.err);
-			return;
+			return kNone;
 		}
 		SahTask t;
 		memset(&t, 0, sizeof(t));
@@ -338,18 +336,34 @@ __device__ void add_child(const SahArgs &A, int out_par, uint32_t begin, uint32_
 		const uint32_t i = atomicAdd(&A.ctr[kCtrSmall], 1u);
 		if (i >= A.max_small) {
 			flag(A.err);
-			return;
+			return kNone;
 		}
 		A.small[i] = SmallTask{begin, count | (buf << 8) | (depth << 16), node, parent};
 	}
+	return kNone;
+}
+
+// Clears the bins of the large tasks that lane `from_lane`'s add_child calls filed
+// (their slots); the whole warp calls this, 21 words per lane and task.  A single lane
+// clearing the 672 words of two children took most of k_sah_split's time.
+__device__ __forceinline__ void init_new_bins(const SahArgs &A, int out_par, uint32_t slot_a,
+                                              uint32_t slot_b, int from_lane, int lane) {
+	slot_a = __shfl_sync(0xFFFFFFFFu, slot_a, from_lane);
+	slot_b = __shfl_sync(0xFFFFFFFFu, slot_b, from_lane);
+	if (slot_a != kNone)
+		bins_init(A.bins[out_par] + (size_t)slot_a * kBinWords, lane);
+	if (slot_b != kNone)
+		bins_init(A.bins[out_par] + (size_t)slot_b * kBinWords, lane);
 }
 
 // Writes node `t.node` (box, children, range) for split `s` and files both children
-// (lane 0 only).  Children whose range holds one triangle are leaves.
+// (lane 0 only).  Children whose range holds one triangle are leaves.  slots[] receive
+// the list slots of children filed as large tasks (kNone otherwise).
 __device__ void emit_split(const SahArgs &A, const SahTask &t, const Split &s, int out_par,
-                           const float *flo, const float *fsc) {
+                           const float *flo, const float *fsc, uint32_t slots[2]) {
 	const uint32_t buf = (t.meta & 1u) ^ 1u, depth = ((t.meta >> 8) & 0xFFu) + 1u;
 	const uint32_t nl = s.n_left, nr = t.count - s.n_left;
+	slots[0] = slots[1] = kNone;
 	if (nl == 0 || nl >= t.count || t.node == kNone || t.node >= A.node_cap) {
 		flag(A.err);
 		return;
@@ -386,10 +400,10 @@ __device__ void emit_split(const SahArgs &A, const SahTask &t, const Split &s, i
 	write_node_box(A, t.node, s.node, (binned && nl > 1) ? box_area(s.left) : -1.0f,
 	               (binned && nr > 1) ? box_area(s.right) : -1.0f);
 	const uint32_t pl = binned ? kNone : (t.node << 1), pr = binned ? kNone : ((t.node << 1) | 1u);
-	add_child(A, out_par, t.begin, nl, ids[0], pl, buf, depth, binned ? &s.left : nullptr, flo,
-	          fsc);
-	add_child(A, out_par, t.begin + nl, nr, ids[1], pr, buf, depth, binned ? &s.right : nullptr,
-	          flo, fsc);
+	slots[0] = add_child(A, out_par, t.begin, nl, ids[0], pl, buf, depth,
+	                     binned ? &s.left : nullptr, flo, fsc);
+	slots[1] = add_child(A, out_par, t.begin + nl, nr, ids[1], pr, buf, depth,
+	                     binned ? &s.right : nullptr, flo, fsc);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -428,6 +442,36 @@ __global__ void k_sah_records(const float *__restrict__ tris, uint32_t n,
 		mn[k] = live ? c : INFINITY;
 		mx[k] = live ? c : -INFINITY;
 	}
+	if (!scene_of) {
+		// One scene: warps reduce, then the block, and one thread updates the six words
+		// (one set of same-address atomics per block instead of per warp: with 32k warps
+		// on a 1M-triangle scene those atomics were most of this kernel's time).
+		__shared__ float red[32][6];
+#pragma unroll
+		for (int k = 0; k < 3; ++k)
+			for (int o = 16; o > 0; o >>= 1) {
+				mn[k] = fminf(mn[k], __shfl_xor_sync(0xFFFFFFFFu, mn[k], o));
+				mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xFFFFFFFFu, mx[k], o));
+			}
+		const int w = threadIdx.x >> 5;
+		if (lane == 0)
+			for (int k = 0; k < 3; ++k) {
+				red[w][k] = mn[k];
+				red[w][3 + k] = mx[k];
+			}
+		__syncthreads();
+		if (threadIdx.x < 6) {
+			const int k = threadIdx.x;
+			float v = red[0][k];
+			for (int j = 1; j < (int)(blockDim.x >> 5); ++j)
+				v = k < 3 ? fminf(v, red[j][k]) : fmaxf(v, red[j][k]);
+			if (k < 3 && v != INFINITY)
+				atomicMin(&gb[k], f2ord(v));
+			else if (k >= 3 && v != -INFINITY)
+				atomicMax(&gb[k], f2ord(v));
+		}
+		return;
+	}
 	const uint32_t s0 = __shfl_sync(0xFFFFFFFFu, s, 0);
 	if (__all_sync(0xFFFFFFFFu, !live || s == s0)) {
 #pragma unroll
@@ -451,21 +495,27 @@ __global__ void k_sah_records(const float *__restrict__ tris, uint32_t n,
 
 __global__ void k_sah_first_id(uint32_t *ctr, uint32_t S) { ctr[kCtrNodes] = S; }
 
+// One warp per scene: lane 0 files the root task, the warp clears a large root's bins.
 __global__ void k_sah_roots(SahArgs A, const uint32_t *__restrict__ tri_off, uint32_t n_scenes,
                             const uint32_t *__restrict__ gb, uint32_t *roots) {
-	const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+	const uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+	const int lane = threadIdx.x & 31;
 	if (s >= n_scenes)
 		return;
-	roots[s] = s;
 	const uint32_t b = tri_off[s], n = tri_off[s + 1] - b;
-	if (n == 0)
-		return;
-	float flo[3], fsc[3];
-	for (int k = 0; k < 3; ++k) {
-		flo[k] = ord2f(gb[6 * s + k]);
-		fsc[k] = frame_scale(flo[k], ord2f(gb[6 * s + 3 + k]));
+	uint32_t slot = kNone;
+	if (lane == 0) {
+		roots[s] = s;
+		if (n) {
+			float flo[3], fsc[3];
+			for (int k = 0; k < 3; ++k) {
+				flo[k] = ord2f(gb[6 * s + k]);
+				fsc[k] = frame_scale(flo[k], ord2f(gb[6 * s + 3 + k]));
+			}
+			slot = add_child(A, 0, b, n, n > 1 ? s : kNone, kNone, 0u, 0u, nullptr, flo, fsc);
+		}
 	}
-	add_child(A, 0, b, n, n > 1 ? s : kNone, kNone, 0u, 0u, nullptr, flo, fsc);
+	init_new_bins(A, 0, slot, kNone, 0, lane);
 }
 
 // ---------------------------------------------------------------------------------------
@@ -606,6 +656,7 @@ __global__ void __launch_bounds__(128) k_sah_split(SahArgs A, int par) {
 			fsc[k] = t.scale[k];
 		}
 		Split s = choose_split(b, fsc, t.count, lane);
+		uint32_t slots[2] = {kNone, kNone};
 		uint32_t total = b[lane * 7 + 6]; // the axis-0 bins hold every triangle once
 		for (int o = 16; o > 0; o >>= 1)
 			total += __shfl_xor_sync(0xFFFFFFFFu, total, o);
@@ -626,9 +677,9 @@ __global__ void __launch_bounds__(128) k_sah_split(SahArgs A, int par) {
 			tr.n_left = s.n_left;
 			tr.cur_l = t.begin;
 			tr.cur_r = t.begin + s.n_left;
-			emit_split(A, t, s, par ^ 1, flo, fsc);
+			emit_split(A, t, s, par ^ 1, flo, fsc, slots);
 		}
-		__syncwarp();
+		init_new_bins(A, par ^ 1, slots[0], slots[1], 0, lane);
 	}
 }
 
@@ -774,11 +825,12 @@ __global__ void __launch_bounds__(128) k_sah_mid(SahArgs A, int par) {
 			nl_seen += __popc(bl);
 			nr_seen += __popc(br);
 		}
+		uint32_t slots[2] = {kNone, kNone}; // children of mid tasks are never large
 		if (lane == 0) {
 			if (nl_seen != s.n_left)
 				flag(A.err);
 			write_parent_area(A, t.parent, box_area(s.node));
-			emit_split(A, t, s, par ^ 1, flo, fsc);
+			emit_split(A, t, s, par ^ 1, flo, fsc, slots);
 		}
 		__syncwarp();
 	}
@@ -1085,24 +1137,34 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 	if (n)
 		k_sah_records<<<blocks_for(n, 256), 256, 0, st>>>(d_tris, n, scene_of, A.rec[0], gb);
 	k_sah_first_id<<<1, 1, 0, st>>>(A.ctr, S);
-	k_sah_roots<<<blocks_for(S, 128), 128, 0, st>>>(A, d_toff, S, gb, ws.roots.as<uint32_t>());
+	k_sah_roots<<<blocks_for(32ull * S, 128), 128, 0, st>>>(A, d_toff, S, gb,
+	                                                        ws.roots.as<uint32_t>());
 	int level = 0;
 	bool large_left = true; // children are smaller than their parent: once no large task
 	                        // is left, none comes back, and its four kernels are skipped
 	for (;;) {
 		for (int k = 0; k < kLevelsPerCheck && level < kMaxLevels; ++k, ++level) {
 			const int par = level & 1;
+			// Grids no larger than the work the level can hold: each task has at most two
+			// children, so level L has at most S * 2^L tasks of a tier (a small scene's
+			// levels are then a few blocks each instead of 1216 idle ones).
+			const uint64_t tasks = (uint64_t)S << std::min(level, 40);
+			const unsigned g_chunk =
+			    (unsigned)std::min<uint64_t>(1216, n / kChunk + std::min<uint64_t>(tasks, L.max_large));
+			const unsigned g_split = (unsigned)std::min<uint64_t>(152, (tasks + 3) / 4);
+			const unsigned g_mid =
+			    (unsigned)std::min<uint64_t>(1216, (std::min<uint64_t>(tasks, L.max_mid) + 3) / 4);
 			if (large_left) {
 				k_sah_chunks<<<1, 1024, 0, st>>>(A, par);
-				k_sah_bin<<<1216, 256, 0, st>>>(A, par);
-				k_sah_split<<<152, 128, 0, st>>>(A, par);
-				k_sah_part<<<1216, 256, 0, st>>>(A, par);
+				k_sah_bin<<<g_chunk, 256, 0, st>>>(A, par);
+				k_sah_split<<<g_split, 128, 0, st>>>(A, par);
+				k_sah_part<<<g_chunk, 256, 0, st>>>(A, par);
 			} else {
 				// What k_sah_chunks does besides: clear the lists this level fills.
 				cudaMemsetAsync(A.ctr + kCtrLarge + (par ^ 1), 0, 4, st);
 				cudaMemsetAsync(A.ctr + kCtrMid + (par ^ 1), 0, 4, st);
 			}
-			k_sah_mid<<<1216, 128, 0, st>>>(A, par);
+			k_sah_mid<<<g_mid, 128, 0, st>>>(A, par);
 		}
 		uint32_t h[kCtrWordsSah];
 		cudaError_t e = cudaMemcpyAsync(h, A.ctr, sizeof(h), cudaMemcpyDeviceToHost, st);

@@ -34,7 +34,7 @@ def test_heightfield_every_ray(gpu_backend, oracle_lib):
     bvh = oracle_lib.BVH(tris)
     rep = check(hp, bvh.nearest_hits(prim, threads=cores), TAGS, tris, prim, oracle_lib, cores)
     assert rep["n_bad"] == 0, rep
-    assert rep["hits"] > 1_500_000
+    assert rep["hits"] > 400_000
     for delta in (0.01, 0.0):
         sec = W.secondary_rays(tris, prim, hp["valid"] != 0, hp["primitive_id"],
                                np.stack([hp["px"], hp["py"], hp["pz"]], 1), 4_194_304,
