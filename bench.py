@@ -523,6 +523,22 @@ def leg_precision(b, stream, steps, check_rays=0):
     return res
 
 
+SIZE_CLASSES = (("rays<=64Ki", 0, 65_536), ("64Ki<rays<=512Ki", 65_536, 524_288),
+                ("rays>512Ki", 524_288, 1 << 40))
+
+
+def latency_by_size(lat, nrays):
+    """p50 / p99 latency (ms) of the requests in each size class."""
+    out = {}
+    for name, lo, hi in SIZE_CLASSES:
+        m = (nrays > lo) & (nrays <= hi)
+        if m.any():
+            out[name] = {"n": int(m.sum()), "p50_ms": float(np.percentile(lat[m], 50)),
+                         "p99_ms": float(np.percentile(lat[m], 99)),
+                         "max_ms": float(lat[m].max())}
+    return out
+
+
 def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
     """64 resident soup scenes (sizes log-uniform in [16, 1,048,576], seeds 5000+s) and
     a request stream (seed 9000): scene uniform, rays log-uniform in [1,024, 1,048,576],
@@ -626,7 +642,8 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
         cap_rps = n_req / span
         res["capacity"] = {"mrays_s": cap_mrays, "requests_s": cap_rps,
                            "p50_ms": float(np.percentile(lat, 50)),
-                           "p99_ms": float(np.percentile(lat, 99))}
+                           "p99_ms": float(np.percentile(lat, 99)),
+                           "by_size": latency_by_size(lat, nray[idx])}
         res["loads"] = []
         for k, f in enumerate(loads):
             idx = list(range(n_req * (k + 1), n_req * (k + 2)))
@@ -638,6 +655,7 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
                                  "p50_ms": float(np.percentile(lat, 50)),
                                  "p99_ms": float(np.percentile(lat, 99)),
                                  "max_ms": float(lat.max()),
+                                 "by_size": latency_by_size(lat, nray[idx]),
                                  "waves": srv.stat("waves") - w0})
             if log:
                 log(f"serving load {f}: {res['loads'][-1]}")

@@ -441,33 +441,6 @@ int prt_b200_sync(prt_b200_ctx *ctx) {
 	return check_device_errors(ctx);
 }
 
-namespace {
-
-// The address under which the device reaches host buffer p in place, or null: pinned
-// (page-locked, registered) memory through its device alias, pageable memory when the
-// device reads it through the host's page tables (Grace: NVLink-C2C with address
-// translation), managed and device memory as they are.
-void *device_alias(const prt_b200_ctx *ctx, const void *p) {
-	cudaPointerAttributes a;
-	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
-		cudaGetLastError();
-		return nullptr;
-	}
-	switch (a.type) {
-	case cudaMemoryTypeHost:
-		return a.devicePointer;
-	case cudaMemoryTypeDevice:
-	case cudaMemoryTypeManaged:
-		return a.device == ctx->device ? const_cast<void *>(p) : nullptr;
-	case cudaMemoryTypeUnregistered:
-		return ctx->pageable_access ? const_cast<void *>(p) : nullptr;
-	default:
-		return nullptr;
-	}
-}
-
-} // namespace
-
 int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uint32_t field_mask,
                           uint32_t rec_size, const uint8_t offs[8], void *out_host) {
 	if (!ctx)
@@ -494,10 +467,10 @@ int prt_b200_nearest_hits(prt_b200_ctx *ctx, const float *rays6, uint64_t n, uin
 		// so rays that are only 4-byte aligned (a float array at an odd index) are copied
 		// into the aligned staging buffer instead; records may have any alignment.
 		if (ctx->host_direct) {
-			const void *d_in = device_alias(ctx, rays6);
+			const void *d_in = prt::device_alias(ctx, rays6);
 			if (reinterpret_cast<uintptr_t>(d_in) % 8 != 0)
 				d_in = nullptr;
-			void *d_out = d_in ? device_alias(ctx, out_host) : nullptr;
+			void *d_out = d_in ? prt::device_alias(ctx, out_host) : nullptr;
 			ctx->last_in_place = d_in && d_out;
 			if (d_in && d_out) {
 				CAPI_TRY(ctx, prt::launch_nearest_hits(ctx->scene, static_cast<const float *>(d_in),

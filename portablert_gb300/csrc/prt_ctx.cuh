@@ -157,6 +157,29 @@ int guarded(ErrorText *err, const char *what, F &&body, cudaStream_t capture = n
 	return PRT_ERR_OOM;
 }
 
+// The address under which the device reaches host buffer p in place, or null: pinned
+// (page-locked, registered) memory through its device alias, pageable memory when the
+// device reads it through the host's page tables (Grace: NVLink-C2C with address
+// translation), managed and device memory as they are.
+inline void *device_alias(const prt_b200_ctx *ctx, const void *p) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return nullptr;
+	}
+	switch (a.type) {
+	case cudaMemoryTypeHost:
+		return a.devicePointer;
+	case cudaMemoryTypeDevice:
+	case cudaMemoryTypeManaged:
+		return a.device == ctx->device ? const_cast<void *>(p) : nullptr;
+	case cudaMemoryTypeUnregistered:
+		return ctx->pageable_access ? const_cast<void *>(p) : nullptr;
+	default:
+		return nullptr;
+	}
+}
+
 // Validates a HitReg layout descriptor.
 inline bool layout_ok(uint32_t mask, uint32_t rec, const uint8_t *off, std::string &why) {
 	if (mask == 0 || mask > 31u) {

@@ -11,15 +11,21 @@
 //              lane 0 is an express lane (highest stream priority) that takes only
 //              small requests, passing over larger ones queued before them
 //   run     -> per wave, on the lane's stream: rays copied in, ONE launch of the
-//              segment traversal over every request of the wave (each warp takes at
-//              most a few batches, so the blocks of a long wave retire steadily and
-//              a higher-priority wave's blocks are scheduled in between); up to
-//              n_lanes waves are in flight at once, so requests
+//              segment traversal over every request of the wave, smallest requests
+//              first (each warp takes at most a few batches, so the blocks of a long
+//              wave retire steadily and a higher-priority wave's blocks are scheduled
+//              in between); up to n_lanes waves are in flight at once, so requests
 //              that arrive while others run are admitted into the next wave as soon
 //              as memory and a lane are free, and their work overlaps on the device
-//   retire  -> each lane's completer thread waits for its wave's traversal, copies the
-//              records out, stamps the finish time, returns the memory and wakes the
-//              waiters
+//   finish  -> per request: where the device reaches the request's output buffer
+//              (pinned memory; pageable memory on a Grace host) the traversal writes
+//              the records there and raises the request's completion flag when its
+//              last batch is stored; the lane's completer thread polls the flags and
+//              finishes each such request at once (finish time, memory returned,
+//              waiters woken), while the rest of the wave still runs
+//   retire  -> when the wave's launch ends the completer copies out the records of
+//              requests whose buffers the device cannot reach, finishes them and frees
+//              the lane
 //
 // A request's records are exactly nearest_hits<Tags...> on its scene alone: the wave's
 // launch gives each request its own segment (rays padded to whole warps), and the
@@ -27,6 +33,7 @@
 //
 // No counterpart in the reference (portableRT answers one synchronous call at a time,
 // include/portableRT/nearest_hits_impl.hpp:28-36).
+#include <algorithm>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -63,6 +70,7 @@ struct Request {
 	const float *rays = nullptr;
 	uint64_t n = 0;
 	void *out = nullptr;
+	void *dev_out = nullptr; // the device's address of `out` (records written in place), or null
 	uint64_t off = 0, ray_bytes = 0, bytes = 0; // range in the budget region
 	Clock::time_point t_submit, t_launch, t_done;
 	int status = PRT_OK;
@@ -74,9 +82,16 @@ struct Lane {
 	cudaEvent_t ev = nullptr;
 	prt::DevBuf segs;                // SegDesc table of the wave
 	prt::DevBuf work;                // [0] ray counter, [1] error word, [4..7] visits
+	prt::DevBuf seg_ctr;             // per request of the wave: rays stored (device)
+	uint32_t *h_done = nullptr;      // per request: completion flag (pinned, mapped)
+	uint32_t *d_done = nullptr;      // the device's address of h_done
 	prt::SegDesc *h_segs = nullptr;  // pinned staging of the table
 	uint32_t *h_err = nullptr;       // pinned copy of the error word
 	std::vector<Request *> wave;     // requests in flight on this lane
+	// Per request of the wave: written in place (1) or copied out; finished early (1).  A
+	// request finished early may be deleted by its waiter at once, so after that only
+	// these flags are read, never the request.
+	std::vector<uint8_t> in_place, fin;
 	bool launched = false;           // the wave's work (and event) has been queued
 	std::thread completer;
 	std::condition_variable cv;
@@ -106,6 +121,9 @@ struct prt_b200_server {
 	// wave's work runs out): blocks of a long wave retire as they finish, so the block
 	// scheduler can start an express wave's blocks meanwhile.
 	uint32_t batches_per_warp = 2;
+	// Records go straight to a request's host buffer when the device reaches it (the
+	// context's "host_direct" option when the server was created); else they are staged.
+	bool host_direct = true;
 	uint64_t completed = 0, rays_done = 0;
 };
 
@@ -171,18 +189,33 @@ Lane *admit(prt_b200_server *s) {
 	return nullptr;
 }
 
-// Queues the wave's copies, launch and event on the lane's stream (no lock held).
+// Queues the wave's copies, launch and event on the lane's stream (no lock held).  The
+// wave's requests are ordered by size, smallest first: warps take batches in segment
+// order, so a small request's batches are not queued behind a large one's.
 cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 	prt_b200_batch *b = s->batch;
 	uint8_t *base = s->region.as<uint8_t>();
 	unsigned long long nv = 0;
+	std::stable_sort(L.wave.begin(), L.wave.end(),
+	                 [](const Request *x, const Request *y) { return x->n < y->n; });
 	const uint32_t k = (uint32_t)L.wave.size();
+	L.fin.assign(k, 0); // capacity reserved at creation: no allocation
+	L.in_place.assign(k, 0);
+	for (uint32_t i = 0; i < k; ++i)
+		L.in_place[i] = L.wave[i]->dev_out ? 1 : 0;
+	// No launch of this lane is in flight (its last wave retired): the flags can be
+	// cleared from the host.
+	std::memset(L.h_done, 0, 4 * (size_t)k);
+	cudaError_t e0 = cudaMemsetAsync(L.seg_ctr.p, 0, 4 * (size_t)k, L.st);
+	if (e0 != cudaSuccess)
+		return e0;
 	for (uint32_t i = 0; i < k; ++i) {
 		Request *r = L.wave[i];
 		prt::SegDesc &d = L.h_segs[i];
+		d = prt::SegDesc{};
 		d.vbegin = nv;
 		d.rays = reinterpret_cast<const float *>(base + r->off);
-		d.out = base + r->off + r->ray_bytes;
+		d.out = r->dev_out ? static_cast<uint8_t *>(r->dev_out) : base + r->off + r->ray_bytes;
 		d.n_rays = (uint32_t)r->n;
 		d.scene = r->scene;
 		d.mask = r->mask;
@@ -190,6 +223,8 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 		std::memcpy(d.off, r->offs, 8);
 		d.store_mode = prt::store_mode_for(d.out);
 		d.pad = 0;
+		d.done_ctr = L.seg_ctr.as<uint32_t>() + i;
+		d.done_flag = L.d_done + i;
 		nv += (r->n + 31ull) & ~31ull;
 		cudaError_t e = cudaMemcpyAsync(base + r->off, r->rays, 24 * r->n,
 		                                cudaMemcpyHostToDevice, L.st);
@@ -227,7 +262,10 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 // never holds up the scheduler).
 cudaError_t copy_out(prt_b200_server *s, Lane &L) {
 	uint8_t *base = s->region.as<uint8_t>();
-	for (Request *r : L.wave) {
+	for (size_t i = 0; i < L.wave.size(); ++i) {
+		if (L.in_place[i])
+			continue; // written in place by the traversal
+		Request *r = L.wave[i];
 		const cudaError_t e = cudaMemcpyAsync(r->out, base + r->off + r->ray_bytes,
 		                                      (uint64_t)r->rec * r->n, cudaMemcpyDeviceToHost,
 		                                      L.st);
@@ -237,16 +275,22 @@ cudaError_t copy_out(prt_b200_server *s, Lane &L) {
 	return cudaStreamSynchronize(L.st);
 }
 
-// Finishes the requests of a lane's wave (caller holds the lock).
+// Finishes one request (caller holds the lock): its memory returns to the budget.
+void finish(prt_b200_server *s, Request *r, int status, Clock::time_point t) {
+	r->t_done = t;
+	r->status = status;
+	r->done = true;
+	s->alloc.release(r->off, r->bytes);
+	++s->completed;
+	s->rays_done += r->n;
+}
+
+// Finishes the requests of a lane's wave that are not finished yet and frees the lane
+// (caller holds the lock).
 void retire(prt_b200_server *s, Lane &L, int status, Clock::time_point t) {
-	for (Request *r : L.wave) {
-		r->t_done = t;
-		r->status = status;
-		r->done = true;
-		s->alloc.release(r->off, r->bytes);
-		++s->completed;
-		s->rays_done += r->n;
-	}
+	for (size_t i = 0; i < L.wave.size(); ++i)
+		if (i >= L.fin.size() || !L.fin[i])
+			finish(s, L.wave[i], status, t);
 	L.wave.clear();
 	L.launched = false;
 	--s->in_flight;
@@ -301,9 +345,45 @@ void completer(prt_b200_server *s, Lane *L) {
 		if (!L->launched)
 			return;
 		lk.unlock();
-		// The wave's kernels end by themselves (bounded traversal steps), so this wait
+		// Requests whose records the traversal writes in place finish as soon as their
+		// completion flag is up; the rest of the wave finishes when its launch has ended.
+		// The wave's kernels end by themselves (bounded traversal steps), so this loop
 		// ends too.
-		cudaError_t e = cudaEventSynchronize(L->ev);
+		const size_t k = L->wave.size();
+		size_t open = 0;
+		for (size_t i = 0; i < k; ++i)
+			open += L->in_place[i];
+		cudaError_t e = cudaSuccess;
+		for (;;) {
+			const cudaError_t q = cudaEventQuery(L->ev);
+			const bool ended = q != cudaErrorNotReady;
+			if (open) {
+				const Clock::time_point t = Clock::now();
+				bool any = false;
+				for (size_t i = 0; i < k; ++i) {
+					if (L->in_place[i] && !L->fin[i] &&
+					    reinterpret_cast<volatile const uint32_t *>(L->h_done)[i]) {
+						if (!any)
+							lk.lock();
+						any = true;
+						finish(s, L->wave[i], PRT_OK, t);
+						L->fin[i] = 1;
+						--open;
+					}
+				}
+				if (any) {
+					s->cv_done.notify_all();
+					s->cv_sched.notify_one();
+					lk.unlock();
+				}
+			}
+			if (ended) {
+				if (q != cudaSuccess)
+					e = q;
+				break;
+			}
+			std::this_thread::sleep_for(std::chrono::microseconds(20));
+		}
 		if (e == cudaSuccess && !*L->h_err)
 			e = copy_out(s, *L);
 		const Clock::time_point t = Clock::now();
@@ -326,6 +406,11 @@ void release_lane(Lane &L) {
 		cudaStreamSynchronize(L.st);
 	L.segs.release();
 	L.work.release();
+	L.seg_ctr.release();
+	if (L.h_done)
+		cudaFreeHost(L.h_done);
+	L.h_done = nullptr;
+	L.d_done = nullptr;
 	if (L.h_segs)
 		cudaFreeHost(L.h_segs);
 	if (L.h_err)
@@ -388,6 +473,7 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		std::lock_guard<std::mutex> lk(ctx->mu);
 		s->format = ctx->node_format;
 		s->batches_per_warp = (uint32_t)ctx->serve_batches_per_warp;
+		s->host_direct = ctx->host_direct;
 	}
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e == cudaSuccess)
@@ -417,10 +503,18 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 			e = cudaMallocHost(&L->h_segs, sizeof(prt::SegDesc) * kMaxWaveRequests);
 		if (e == cudaSuccess)
 			e = cudaMallocHost(&L->h_err, 16);
+		if (e == cudaSuccess)
+			e = L->seg_ctr.reserve(4 * kMaxWaveRequests);
+		if (e == cudaSuccess)
+			e = cudaHostAlloc(&L->h_done, 4 * kMaxWaveRequests, cudaHostAllocMapped);
+		if (e == cudaSuccess)
+			e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&L->d_done), L->h_done, 0);
 		// A wave holds at most kMaxWaveRequests requests: with the room reserved here the
 		// scheduler thread never allocates to fill one.
 		try {
 			L->wave.reserve(kMaxWaveRequests);
+			L->in_place.reserve(kMaxWaveRequests);
+			L->fin.reserve(kMaxWaveRequests);
 			s->lanes.push_back(std::move(L));
 		} catch (const std::bad_alloc &) {
 			if (L) // not yet owned by the server: free what it holds
@@ -490,7 +584,11 @@ int prt_b200_server_submit(prt_b200_server *s, uint32_t scene, const float *rays
 	r->n = n;
 	r->out = out_host;
 	r->ray_bytes = round256(24 * n);
-	r->bytes = r->ray_bytes + (uint64_t)rec_size * n;
+	// Records go straight to out_host when the device reaches it; otherwise they are
+	// staged in the budget region and copied out when the wave's launch has ended.
+	if (n && s->host_direct)
+		r->dev_out = prt::device_alias(s->ctx, out_host);
+	r->bytes = r->ray_bytes + (r->dev_out ? 0 : (uint64_t)rec_size * n);
 	std::lock_guard<std::mutex> lk(s->mu);
 	if (s->stop)
 		return sfail(s, PRT_ERR_ARG, "server submit: server is stopping");

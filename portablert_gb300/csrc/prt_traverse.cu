@@ -243,7 +243,7 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
                                             uint32_t *pool, const SceneDesc &sd, uint32_t nb,
                                             int lane, int g, int s, uint32_t lt,
                                             uint32_t step_limit, uint32_t &n_visits,
-                                            uint32_t &n_tests) {
+                                            uint32_t &n_tests, bool &fault) {
 	const float4 *__restrict__ tri4 = sd.tri4;
 	const void *__restrict__ nodes = sd.nodes;
 	uint32_t top = 0;  // items in the pool (warp-uniform)
@@ -265,6 +265,7 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		if (++steps > step_limit) {
 			if (lane == 0)
 				atomicOr(a.err, kErrStack);
+			fault = true;
 			break;
 		}
 		const uint32_t take = min(top, (uint32_t)kItems);
@@ -305,6 +306,7 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		if (top + n_push > a.pool_cap) {
 			if (lane == 0)
 				atomicOr(a.err, kErrStack);
+			fault = true;
 		} else {
 			uint32_t pos = top + before;
 #pragma unroll
@@ -458,6 +460,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		S.key[lane] = kNoHit;
 		__syncwarp();
 
+		bool fault = false; // the batch's traversal reported an error (warp-uniform)
 		if (sd.n_tris) {
 			// Nearly every batch has only rays with finite reciprocals.
 			const bool regular =
@@ -470,7 +473,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			if (PASS == 2 && regular)
 				continue; // done by the regular pass
 			trace_batch<FMT, COUNT, LEAF1, PASS == 1>(a, S, queue, pool, sd, nb, lane, g, s, lt,
-			                                          step_limit, n_visits, n_tests);
+			                                          step_limit, n_visits, n_tests, fault);
 		} else if (PASS == 2) {
 			continue; // the regular pass wrote this empty scene's misses
 		}
@@ -539,6 +542,20 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			const uint8_t *sb = reinterpret_cast<const uint8_t *>(stage);
 			for (uint32_t k = lane; k < bytes; k += 32u)
 				dst[k] = sb[k];
+		}
+		if (S.seg.done_ctr) {
+			// The run's completion count (SegDesc): every lane's record stores are made
+			// visible system-wide before lane 0 counts the batch; the batch that finishes
+			// the run raises the host flag after another system fence.
+			__threadfence_system();
+			__syncwarp();
+			if (lane == 0 && !fault) {
+				const uint32_t before = atomicAdd(S.seg.done_ctr, nb);
+				if (before + nb == run_rays) {
+					__threadfence_system();
+					*reinterpret_cast<volatile uint32_t *>(S.seg.done_flag) = 1u;
+				}
+			}
 		}
 		__syncwarp();
 	}

@@ -49,6 +49,14 @@ struct SegDesc {
 	uint8_t off[8];
 	uint32_t store_mode; // 0: 16-B stores, 1: 4-B stores, 2: byte stores
 	uint32_t pad;
+	// Completion of the run (request servers; null: not tracked).  Each batch of the run
+	// adds its rays to *done_ctr (device memory) once its records are stored and fenced
+	// system-wide; the batch that completes the count then sets *done_flag (host memory
+	// the device reaches) to 1, so a host thread sees the run's records finished without
+	// waiting for the rest of the launch.  A batch whose traversal reported an error does
+	// not count, so its run never completes early.
+	uint32_t *done_ctr = nullptr;
+	uint32_t *done_flag = nullptr;
 };
 
 // Levels of the 8-wide tree the traversal can walk.

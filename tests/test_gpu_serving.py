@@ -82,7 +82,10 @@ def test_mix_equals_alone(gpu_backend):
         assert bad is None, (i, s, len(rays), tags, bad)
 
 
-def test_budget_admission_and_limits(gpu_backend):
+@pytest.mark.parametrize("host_direct", [1, 0])
+def test_budget_admission_and_limits(gpu_backend, host_direct):
+    """host_direct 1: records go straight to the host buffers and only rays take budget;
+    0: records are staged in the budget region too and copied out."""
     import torch
 
     from portablert_gb300.serve import Server
@@ -90,10 +93,14 @@ def test_budget_admission_and_limits(gpu_backend):
     tris, off, d_tris = _scenes(torch, [2000, 3000], 5100)
     tags = ("t", "primitive_id", "valid")
     lay = hitreg.layout(tags)
-    n = 20_000  # 480,000 B of rays + 320,000 B of records per request
-    per = ((24 * n + 255) // 256) * 256 + lay.size * n
+    n = 20_000  # 480,000 B of rays (+ 320,000 B of records when staged) per request
+    per = ((24 * n + 255) // 256) * 256 + (0 if host_direct else lay.size * n)
     budget = 2 * per + 1000  # two requests fit at once, not three
-    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=budget, lanes=4)
+    gpu_backend.set_option("host_direct", host_direct)
+    try:
+        srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=budget, lanes=4)
+    finally:
+        gpu_backend.set_option("host_direct", 1)
     try:
         subs = [srv.submit(i % 2, workloads.soup_rays(5200 + i, n), tags) for i in range(9)]
         for t, _ in subs:
@@ -152,6 +159,42 @@ def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
         gpu_backend.set_option("leaf_size", 1)
         gpu_backend.set_option("node_format", 0)
         gpu_backend.set_option("serve_batches_per_warp", 2)
+
+
+def test_requests_finish_alone_not_with_their_wave(gpu_backend):
+    """One lane, so requests queued behind a running wave share the next one: the wave
+    runs its small requests first and each finishes when its own rays are stored, not
+    when the 1.5M-ray request on the dense scene is done."""
+    import torch
+
+    from portablert_gb300.serve import Server
+
+    tris, off, d_tris = _scenes(torch, [300_000, 2_000], 6100)
+    # Records go to the host buffers in place, so a request takes only its rays' bytes
+    # of the budget: 19.2 MB for the first, 36 MB for the large one, under 1 MB for the
+    # small ones.  With 40 MB the first runs alone (the large one does not fit beside it
+    # and the small ones queue behind the large one), and the next wave takes the rest.
+    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=40 << 20, lanes=1)
+    tags = ("t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    try:
+        big_rays = workloads.soup_rays(6201, 1_500_000)
+        small = [(i % 2, workloads.soup_rays(6300 + i, 2_000 + 131 * i)) for i in range(8)]
+        blocker = srv.submit(0, workloads.soup_rays(6200, 800_000), tags)
+        big = srv.submit(0, big_rays, tags)
+        subs = [srv.submit(s, r, tags) for s, r in small]
+        srv.wait(blocker[0])
+        lat = [srv.wait(t) for t, _ in subs]
+        big_lat = srv.wait(big[0])
+        assert srv.stat("max_wave_requests") >= 1 + len(small)
+        assert max(lat) < big_lat, (lat, big_lat)
+        for (s, r), (_, out) in zip(small, subs):
+            gpu_backend.set_tris(tris[s])
+            assert _fields_equal(out, gpu_backend.nearest_hits(r, tags), lay) is None
+        gpu_backend.set_tris(tris[0])
+        assert _fields_equal(big[1], gpu_backend.nearest_hits(big_rays, tags), lay) is None
+    finally:
+        srv.close()
 
 
 def test_close_with_requests_queued(gpu_backend):
