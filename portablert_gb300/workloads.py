@@ -264,3 +264,54 @@ def generate_dev(backend, kind: int, seed: int, n: int, out_ptr: int, param: flo
     backend._check(backend._L.prt_b200_generate(backend.ctx, int(kind), int(seed), int(n),
                                                 float(param), ctypes.c_void_p(out_ptr),
                                                 ctypes.c_void_p(stream) if stream else None))
+
+
+# ---------------------------------------------------------------- command line
+
+def run_clustered(n_rays: int = 1_048_576, repeats: int = 2) -> dict:
+    """The clustered soup (8,388,608 triangles, seed 2) with `n_rays` random rays (seed 2),
+    generated on the device: one set_tris, then `repeats` nearest_hits_dev passes with
+    FP32 nodes and `repeats` with compressed nodes (tags uv, t, primitive_id, valid) --
+    the launches a profiler capture of either node format selects from."""
+    import torch
+
+    from . import backend, hitreg
+
+    b = backend.B200Backend(0)
+    b.init()
+    n_t = 8_388_608
+    tags = ("uv", "t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    d_t = torch.empty(n_t * 9, dtype=torch.float32, device="cuda")
+    d_r = torch.empty(n_rays * 6, dtype=torch.float32, device="cuda")
+    out = torch.zeros(n_rays * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    generate_dev(b, GEN_CLUSTER_TRIS, 2, n_t, d_t.data_ptr(), 256)
+    generate_dev(b, GEN_RANDOM_RAYS, 2, n_rays, d_r.data_ptr(), 12.0)
+    b.sync()
+    b.set_tris_dev(d_t.data_ptr(), n_t)
+    for fmt in (0, 1):
+        b.set_option("node_format", fmt)
+        for _ in range(repeats):
+            b.nearest_hits_dev(d_r.data_ptr(), n_rays, out.data_ptr(), tags)
+        b.sync()
+    b.set_option("node_format", 0)
+    b.set_option("count_visits", 1)
+    b.nearest_hits_dev(d_r.data_ptr(), n_rays, out.data_ptr(), tags)
+    b.sync()
+    res = {"nodes": b.stat("n_nodes"), "depth": b.stat("depth"),
+           "node_visits_per_ray": b.stat("visits_nodes") / n_rays,
+           "tri_tests_per_ray": b.stat("visits_tris") / n_rays}
+    b.shutdown()
+    return res
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="run a workload on cuda:0")
+    ap.add_argument("workload", choices=["clustered"])
+    ap.add_argument("--rays", type=int, default=1_048_576)
+    ap.add_argument("--repeats", type=int, default=2)
+    args = ap.parse_args()
+    print(run_clustered(args.rays, args.repeats))
