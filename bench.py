@@ -965,7 +965,11 @@ def run_gpu(args, world, rank):
     out = {"metric": METRIC, "value": mrays, "unit": "Mrays/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-           "data": "synthetic", "config": workload_config(len(tris), len(prim), n),
+           "data": "synthetic",
+           "config": dict(workload_config(len(tris), len(prim), n),
+                          knobs={"leaf_size": int(b.stat("leaf_size")), "block_threads": 128,
+                                 "width": 8, "node_format": "fp32",
+                                 "build": "binned SAH, 8-wide collapse by least cost"}),
            "e2e": {"value": e2e, "unit": "Mrays/s", "h2d_bytes_per_step": 24 * n,
                    "d2h_bytes_per_step": lay.size * n, "host_memory": "pinned",
                    "path": ("in place: the traversal reads each ray from and writes each "
