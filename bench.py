@@ -539,12 +539,12 @@ def latency_by_size(lat, nrays):
     return out
 
 
-def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
+def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None, lanes=4):
     """64 resident soup scenes (sizes log-uniform in [16, 1,048,576], seeds 5000+s) and
     a request stream (seed 9000): scene uniform, rays log-uniform in [1,024, 1,048,576],
     tags uniform over the 31 combinations; Poisson arrivals at fractions of the measured
     capacity.  Latency = submit to records in (pinned) host memory, from the server's
-    own clock; the memory budget for request buffers is 2 GiB, 4 lanes."""
+    own clock; the memory budget for request buffers is 2 GiB, `lanes` lanes (4)."""
     import threading
 
     import torch
@@ -615,13 +615,13 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
     res = {"workload": f"{n_sc} resident soup scenes ({T:,} tris); requests of 1,024 to "
                        "1,048,576 rays (log-uniform), uniform scene and tag set; Poisson "
                        "arrivals", "n_scenes": n_sc, "n_tris": T, "budget_bytes": 2 << 30,
-           "lanes": 4}
+           "lanes": lanes}
     # Leaf size of the resident scenes, chosen by capacity on the first requests (the
     # largest, densest scenes take most of the GPU time and favour larger leaves).
     trial = {}
     for leaf in (1, 4, 8):
         b.set_option("leaf_size", leaf)
-        srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
+        srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=lanes)
         try:
             run(list(range(40)), 0)
             _, span = run(list(range(200)), 0)
@@ -631,7 +631,7 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None):
     best_leaf = max(trial, key=trial.get)
     res["leaf_size"] = {"chosen": best_leaf, "trial_mrays_s": trial}
     b.set_option("leaf_size", best_leaf)
-    srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=4)
+    srv = Server(b, d_tris.data_ptr(), toff, budget_bytes=2 << 30, lanes=lanes)
     b.set_option("leaf_size", 1)
     try:
         idx = list(range(n_req))

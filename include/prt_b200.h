@@ -209,7 +209,7 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)
  *   "serve_batches_per_warp" request servers created afterwards launch waves whose
  *                  warps take at most this many batches of 32 rays (0 = until the
- *                  work runs out; default 2): lower lets an express wave start sooner
+ *                  work runs out; default 1): lower lets an express wave start sooner
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree

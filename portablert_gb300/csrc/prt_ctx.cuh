@@ -74,7 +74,7 @@ struct prt_b200_ctx {
 	int node_format = PRT_NODES_FP32;
 	int block = 128;
 	int pool_depth = 0; // tree depth a batch graph's traversal pool is sized for (0 = 32)
-	int serve_batches_per_warp = 2; // request servers created later ("serve_batches_per_warp")
+	int serve_batches_per_warp = 1; // request servers created later ("serve_batches_per_warp")
 	bool count = false;
 	bool build_compressed = true;
 	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)

@@ -120,7 +120,7 @@ struct prt_b200_server {
 	// Batches of 32 rays a warp of a wave's launch takes before it exits (0 = until the
 	// wave's work runs out): blocks of a long wave retire as they finish, so the block
 	// scheduler can start an express wave's blocks meanwhile.
-	uint32_t batches_per_warp = 2;
+	uint32_t batches_per_warp = 1;
 	// Records go straight to a request's host buffer when the device reaches it (the
 	// context's "host_direct" option when the server was created); else they are staged.
 	bool host_direct = true;

@@ -306,12 +306,36 @@ def run_clustered(n_rays: int = 1_048_576, repeats: int = 2) -> dict:
     return res
 
 
+def run_heightfield_build(repeats: int = 2) -> dict:
+    """set_tris_dev of the 1,048,576-triangle heightfield (seed 1) `repeats` times with the
+    default SAH build: the launches a profiler capture of the build selects from."""
+    import torch
+
+    from . import backend
+
+    b = backend.B200Backend(0)
+    b.init()
+    tris = heightfield_tris(seed=1)
+    d = torch.from_numpy(tris).cuda()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(repeats):
+        b.set_tris_dev(d.data_ptr(), len(tris))
+        ms.append(b.stat("build_ms"))
+    res = {"build_ms": ms, "nodes": b.stat("n_nodes"), "depth": b.stat("depth")}
+    b.shutdown()
+    return res
+
+
 if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser(description="run a workload on cuda:0")
-    ap.add_argument("workload", choices=["clustered"])
+    ap.add_argument("workload", choices=["clustered", "heightfield-build"])
     ap.add_argument("--rays", type=int, default=1_048_576)
     ap.add_argument("--repeats", type=int, default=2)
     args = ap.parse_args()
-    print(run_clustered(args.rays, args.repeats))
+    if args.workload == "clustered":
+        print(run_clustered(args.rays, args.repeats))
+    else:
+        print(run_heightfield_build(args.repeats))

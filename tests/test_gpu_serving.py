@@ -158,7 +158,7 @@ def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
     finally:
         gpu_backend.set_option("leaf_size", 1)
         gpu_backend.set_option("node_format", 0)
-        gpu_backend.set_option("serve_batches_per_warp", 2)
+        gpu_backend.set_option("serve_batches_per_warp", 1)
 
 
 def test_requests_finish_alone_not_with_their_wave(gpu_backend):
