@@ -539,12 +539,13 @@ def latency_by_size(lat, nrays):
     return out
 
 
-def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None, lanes=4):
+def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None, lanes=4, persistent=1):
     """64 resident soup scenes (sizes log-uniform in [16, 1,048,576], seeds 5000+s) and
     a request stream (seed 9000): scene uniform, rays log-uniform in [1,024, 1,048,576],
     tags uniform over the 31 combinations; Poisson arrivals at fractions of the measured
     capacity.  Latency = submit to records in (pinned) host memory, from the server's
-    own clock; the memory budget for request buffers is 2 GiB, `lanes` lanes (4)."""
+    own clock; the memory budget for request buffers is 2 GiB.  persistent=1 (the
+    default): requests are folded into one running launch; 0: waves on `lanes` lanes."""
     import threading
 
     import torch
@@ -615,7 +616,10 @@ def leg_serving(b, stream, loads=(0.3, 0.6, 0.9), n_req=600, log=None, lanes=4):
     res = {"workload": f"{n_sc} resident soup scenes ({T:,} tris); requests of 1,024 to "
                        "1,048,576 rays (log-uniform), uniform scene and tag set; Poisson "
                        "arrivals", "n_scenes": n_sc, "n_tris": T, "budget_bytes": 2 << 30,
+           "mode": ("persistent: requests folded into one running launch, three queues by "
+                    "size" if persistent else f"waves on {lanes} lanes"),
            "lanes": lanes}
+    b.set_option("serve_persistent", persistent)
     # Leaf size of the resident scenes, chosen by capacity on the first requests (the
     # largest, densest scenes take most of the GPU time and favour larger leaves).
     trial = {}

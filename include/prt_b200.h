@@ -210,6 +210,12 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "serve_batches_per_warp" request servers created afterwards launch waves whose
  *                  warps take at most this many batches of 32 rays (0 = until the
  *                  work runs out; default 1): lower lets an express wave start sooner
+ *   "serve_persistent" request servers created afterwards: 1 = admitted requests are
+ *                  folded into one running launch whose warps take their batches from
+ *                  three device queues by request size (up to 64 Ki rays, up to 512 Ki,
+ *                  larger; smaller first) while the host appends to them; the launch stops after 5 ms without work and starts again
+ *                  with the next request (default 1); 0 = each group of admitted
+ *                  requests is a wave, one launch on one of the server's lanes
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree

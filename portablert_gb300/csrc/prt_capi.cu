@@ -89,7 +89,7 @@ const char *const kOptionKeys[] = {"leaf_size",        "node_format",   "block",
                                    "pipe_chunks",      "pipe_ramp",     "pipe_min_rays",
                                    "serve_batches_per_warp", "pool_depth", "count_visits",
                                    "build_compressed", "build_sah",     "collapse_cost",
-                                   "host_direct"};
+                                   "host_direct",      "serve_persistent"};
 
 // The overrides set in the environment, as (key, value); false with a message when a
 // value is not a decimal integer.
@@ -601,6 +601,8 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 			ctx->collapse_cost = v != 0;
 		} else if (k == "host_direct") {
 			ctx->host_direct = v != 0;
+		} else if (k == "serve_persistent") {
+			ctx->serve_persistent = v != 0;
 		} else if (k == "fail_alloc_after") {
 			if (v < 0)
 				return fail(ctx, PRT_ERR_ARG, "fail_alloc_after must be >= 0");

@@ -75,6 +75,8 @@ struct prt_b200_ctx {
 	int block = 128;
 	int pool_depth = 0; // tree depth a batch graph's traversal pool is sized for (0 = 32)
 	int serve_batches_per_warp = 1; // request servers created later ("serve_batches_per_warp")
+	bool serve_persistent = true;   // request servers created later fold requests into one
+	                                // running launch ("serve_persistent"; 0 = waves)
 	bool count = false;
 	bool build_compressed = true;
 	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)

@@ -97,6 +97,47 @@ struct Lane {
 	std::condition_variable cv;
 };
 
+// A persistent serving launch: the host appends each admitted request to one of three
+// queues by size (at most kExpressRays rays; at most kMediumRays; larger) while the
+// launch runs, and its warps claim the queues' batches in that order (ServeQueues), so a
+// request never waits behind a larger one's batches.
+constexpr uint64_t kMediumRays = 524288;
+constexpr uint32_t kQueueSegs = 4096;        // requests per queue between resets
+constexpr uint64_t kQueueBatches = 1ull << 26; // 2^31 rays in batches of 32
+constexpr auto kIdleStop = std::chrono::milliseconds(5); // stop the launch after this idle time
+constexpr uint32_t kIdlePolls = 1u << 18;    // an idle warp's polls before it leaves (~1 s)
+
+struct PQueue {
+	prt::DevBuf segs;                       // SegDesc[kQueueSegs] (device)
+	prt::DevBuf done_ctr;                   // rays stored per request (device)
+	prt::SegDesc *h_segs = nullptr;         // pinned staging of the descriptors
+	uint32_t *h_words = nullptr;            // pinned staging of (n_segs, published) per request
+	uint32_t *h_done = nullptr;             // completion flags (pinned, mapped)
+	uint32_t *d_done = nullptr;             // the device's address of h_done
+	std::vector<Request *> reqs;            // per request slot
+	std::vector<uint8_t> fin;               // finished
+	uint32_t n_segs = 0, first_open = 0;
+	uint64_t n_batches = 0;
+};
+
+struct Persist {
+	cudaStream_t st = nullptr;  // the serving launch
+	cudaStream_t ctl = nullptr; // resets, ray copies, descriptors, publication, stop flag
+	cudaStream_t out = nullptr; // copy-out of staged records
+	cudaEvent_t ev = nullptr;   // recorded after the serving launch
+	cudaEvent_t ev_ctl = nullptr;
+	prt::DevBuf state;          // ServeQueueState[kServeQueues]
+	prt::DevBuf stop;           // stop flag of the launch
+	prt::DevBuf work;           // the launch's error word
+	uint32_t *h_const = nullptr;             // pinned {0, 1}
+	uint32_t *h_err = nullptr, *d_err = nullptr; // fault flag (pinned, mapped)
+	PQueue q[prt::kServeQueues];
+	bool running = false, stopping = false, faulted = false, full = false;
+	uint64_t outstanding = 0;   // published, not finished
+	Clock::time_point last_activity;
+	std::thread completer;
+};
+
 } // namespace
 
 struct prt_b200_server {
@@ -125,6 +166,10 @@ struct prt_b200_server {
 	// context's "host_direct" option when the server was created); else they are staged.
 	bool host_direct = true;
 	uint64_t completed = 0, rays_done = 0;
+	// Persistent mode (the context's "serve_persistent" option when created): requests
+	// are folded into one running launch instead of launched as waves.
+	bool persistent = true;
+	std::unique_ptr<Persist> P;
 };
 
 namespace {
@@ -425,6 +470,375 @@ void release_lane(Lane &L) {
 	L.st = nullptr;
 }
 
+// ---------------------------------------------------------------------------------------
+// Persistent mode.
+
+// The serving launch's queue arguments (device addresses).
+prt::ServeQueues p_queues(prt_b200_server *s) {
+	Persist &P = *s->P;
+	prt::ServeQueues q;
+	for (int k = 0; k < prt::kServeQueues; ++k) {
+		q.state[k] = P.state.as<prt::ServeQueueState>() + k;
+		q.segs[k] = P.q[k].segs.as<prt::SegDesc>();
+	}
+	q.stop = P.stop.as<uint32_t>();
+	q.err_flag = P.d_err;
+	q.idle_limit = kIdlePolls;
+	q.pad = 0;
+	return q;
+}
+
+// Empties both queues for the next launch (caller holds the lock; no launch runs and
+// no request is outstanding).  Queued on ctl, before any later publication.
+cudaError_t p_reset(prt_b200_server *s) {
+	Persist &P = *s->P;
+	cudaError_t e = cudaMemsetAsync(P.state.p, 0, prt::kServeQueues * sizeof(prt::ServeQueueState),
+	                                P.ctl);
+	for (int k = 0; k < prt::kServeQueues && e == cudaSuccess; ++k) {
+		PQueue &Q = P.q[k];
+		e = cudaMemsetAsync(Q.done_ctr.p, 0, 4 * (size_t)kQueueSegs, P.ctl);
+		std::memset(Q.h_done, 0, 4 * (size_t)kQueueSegs);
+		Q.n_segs = Q.first_open = 0;
+		Q.n_batches = 0;
+	}
+	*reinterpret_cast<volatile uint32_t *>(P.h_err) = 0;
+	P.faulted = P.full = false;
+	return e;
+}
+
+// Starts the serving launch on st after everything queued on ctl so far (the reset and
+// the publications up to now); the stop flag is cleared first.  Caller holds the lock.
+cudaError_t p_launch(prt_b200_server *s) {
+	Persist &P = *s->P;
+	prt_b200_batch *b = s->batch;
+	cudaError_t e = cudaMemcpyAsync(P.stop.p, P.h_const, 4, cudaMemcpyHostToDevice, P.ctl);
+	if (e == cudaSuccess)
+		e = cudaEventRecord(P.ev_ctl, P.ctl);
+	if (e == cudaSuccess)
+		e = cudaStreamWaitEvent(P.st, P.ev_ctl, 0);
+	if (e != cudaSuccess)
+		return e;
+	const prt::SceneDesc *tab = s->format == PRT_NODES_COMPRESSED
+	                                ? b->scenes_comp.as<prt::SceneDesc>()
+	                                : b->scenes_fp32.as<prt::SceneDesc>();
+	e = prt::launch_serving(tab, p_queues(s), b->arena.depth, b->arena.leaf_size,
+	                        b->arena.n_nodes, s->format, P.work.as<uint32_t>(), P.st,
+	                        s->ctx->sms);
+	if (e == cudaSuccess)
+		e = cudaEventRecord(P.ev, P.st);
+	if (e == cudaSuccess) {
+		P.running = true;
+		P.stopping = false;
+		++s->waves;
+	}
+	return e;
+}
+
+// Tells the running launch to end once no batch is left to claim (caller holds the lock).
+void p_stop(prt_b200_server *s) {
+	Persist &P = *s->P;
+	if (cudaMemcpyAsync(P.stop.p, P.h_const + 1, 4, cudaMemcpyHostToDevice, P.ctl) == cudaSuccess)
+		P.stopping = true;
+}
+
+// Appends request r to queue qi and publishes its batches: its rays copied into its
+// budget range, its descriptor into the table, the table size and then the batch count
+// into the queue state, all in order on ctl, so a warp that sees the batches sees the
+// rest.  Caller holds the lock.
+cudaError_t p_publish(prt_b200_server *s, int qi, Request *r) {
+	Persist &P = *s->P;
+	PQueue &Q = P.q[qi];
+	uint8_t *base = s->region.as<uint8_t>();
+	const uint32_t i = Q.n_segs;
+	prt::SegDesc d{};
+	d.vbegin = 32ull * Q.n_batches;
+	d.rays = reinterpret_cast<const float *>(base + r->off);
+	d.out = r->dev_out ? static_cast<uint8_t *>(r->dev_out) : base + r->off + r->ray_bytes;
+	d.n_rays = (uint32_t)r->n;
+	d.scene = r->scene;
+	d.mask = r->mask;
+	d.rec_size = r->rec;
+	std::memcpy(d.off, r->offs, 8);
+	d.store_mode = prt::store_mode_for(d.out);
+	d.pad = 0;
+	d.done_ctr = Q.done_ctr.as<uint32_t>() + i;
+	d.done_flag = Q.d_done + i;
+	Q.h_segs[i] = d;
+	Q.reqs[i] = r;
+	Q.fin[i] = 0;
+	cudaError_t e = cudaMemcpyAsync(base + r->off, r->rays, 24 * r->n, cudaMemcpyHostToDevice, P.ctl);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(Q.segs.as<prt::SegDesc>() + i, Q.h_segs + i, sizeof(prt::SegDesc),
+		                    cudaMemcpyHostToDevice, P.ctl);
+	Q.n_segs = i + 1;
+	Q.n_batches += (r->n + 31) / 32;
+	Q.h_words[2 * i] = Q.n_segs;
+	Q.h_words[2 * i + 1] = (uint32_t)Q.n_batches;
+	prt::ServeQueueState *st = P.state.as<prt::ServeQueueState>() + qi;
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(&st->n_segs, Q.h_words + 2 * i, 4, cudaMemcpyHostToDevice, P.ctl);
+	if (e == cudaSuccess)
+		e = cudaMemcpyAsync(&st->published, Q.h_words + 2 * i + 1, 4, cudaMemcpyHostToDevice, P.ctl);
+	++P.outstanding;
+	s->max_in_flight = std::max<uint64_t>(s->max_in_flight, P.outstanding);
+	if (qi == 0)
+		++s->express_waves;
+	return e;
+}
+
+void scheduler_p(prt_b200_server *s) {
+	cudaSetDevice(s->ctx->device);
+	Persist &P = *s->P;
+	std::unique_lock<std::mutex> lk(s->mu);
+	while (!s->stop) {
+		bool admitted = false, large_blocked = false;
+		if (!P.stopping && !P.faulted && !P.full) {
+			// Arrival order; a small request may pass larger ones that wait for memory.
+			for (auto it = s->waiting.begin(); it != s->waiting.end();) {
+				Request *r = *it;
+				const int qi = r->n <= kExpressRays ? 0 : (r->n <= kMediumRays ? 1 : 2);
+				if (qi > 0 && large_blocked) {
+					++it;
+					continue;
+				}
+				PQueue &Q = P.q[qi];
+				if (Q.n_segs == kQueueSegs || Q.n_batches + (r->n + 31) / 32 > kQueueBatches) {
+					P.full = true; // admitted again after the next reset
+					break;
+				}
+				const uint64_t off = s->alloc.alloc(r->bytes);
+				if (off == prt::RangeAllocator::kFail) {
+					if (qi == 0)
+						break;
+					large_blocked = true;
+					++it;
+					continue;
+				}
+				r->off = off;
+				r->t_launch = Clock::now();
+				it = s->waiting.erase(it);
+				const cudaError_t e = p_publish(s, qi, r);
+				if (e != cudaSuccess) {
+					s->err = std::string("server publish: ") + cudaGetErrorString(e);
+					P.faulted = true; // what reached the queue is finished as failed
+					break;
+				}
+				admitted = true;
+			}
+		}
+		if (admitted) {
+			P.last_activity = Clock::now();
+			if (!P.running) {
+				const cudaError_t e = p_launch(s);
+				if (e != cudaSuccess) {
+					s->err = std::string("server launch: ") + cudaGetErrorString(e);
+					P.faulted = true;
+				}
+			}
+		}
+		s->cv_sched.wait_for(lk, std::chrono::milliseconds(1));
+	}
+	for (Request *r : s->waiting) {
+		r->status = PRT_ERR_ARG;
+		r->t_done = Clock::now();
+		r->done = true;
+	}
+	s->waiting.clear();
+	s->cv_done.notify_all();
+}
+
+// Finishes queue slot i of Q (caller holds the lock): records copied out first where they
+// were staged.
+void p_finish_slot(prt_b200_server *s, PQueue &Q, uint32_t i, int status,
+                   std::unique_lock<std::mutex> &lk) {
+	Persist &P = *s->P;
+	Request *r = Q.reqs[i];
+	if (status == PRT_OK && !r->dev_out) {
+		uint8_t *src = s->region.as<uint8_t>() + r->off + r->ray_bytes;
+		void *dst = r->out;
+		const uint64_t bytes = (uint64_t)r->rec * r->n;
+		lk.unlock();
+		cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, P.out);
+		if (e == cudaSuccess)
+			e = cudaStreamSynchronize(P.out);
+		lk.lock();
+		if (e != cudaSuccess) {
+			status = PRT_ERR_CUDA;
+			s->err = std::string("server copy-out: ") + cudaGetErrorString(e);
+		}
+	}
+	finish(s, r, status, Clock::now());
+	Q.fin[i] = 1;
+	--P.outstanding;
+}
+
+void completer_p(prt_b200_server *s) {
+	cudaSetDevice(s->ctx->device);
+	Persist &P = *s->P;
+	std::unique_lock<std::mutex> lk(s->mu);
+	for (;;) {
+		if (s->stop && s->waiting.empty() && P.outstanding == 0 && !P.running)
+			break;
+		lk.unlock();
+		std::this_thread::sleep_for(std::chrono::microseconds(20));
+		lk.lock();
+		// Requests whose last batch is stored.  (A request's slot is read only while it is
+		// unfinished: a finished request may be deleted by its waiter.)
+		bool any = false;
+		for (int k = 0; k < prt::kServeQueues; ++k) {
+			PQueue &Q = P.q[k];
+			for (uint32_t i = Q.first_open; i < Q.n_segs; ++i)
+				if (!Q.fin[i] && reinterpret_cast<volatile const uint32_t *>(Q.h_done)[i]) {
+					p_finish_slot(s, Q, i, PRT_OK, lk);
+					any = true;
+				}
+			while (Q.first_open < Q.n_segs && Q.fin[Q.first_open])
+				++Q.first_open;
+		}
+		if (any) {
+			P.last_activity = Clock::now();
+			s->cv_done.notify_all();
+			s->cv_sched.notify_one();
+		}
+		// A batch that faulted: its request never completes.  Stop the launch; what is
+		// unfinished fails once the launch has ended (until then it may still write).
+		if (!P.faulted && *reinterpret_cast<volatile const uint32_t *>(P.h_err)) {
+			P.faulted = true;
+			s->err = "server: the traversal reported an error";
+		}
+		if (P.running && !P.stopping &&
+		    (P.faulted || (P.outstanding == 0 &&
+		                   (s->stop || P.full ||
+		                    (s->waiting.empty() && Clock::now() - P.last_activity > kIdleStop)))))
+			p_stop(s);
+		// The launch has ended (stopped, or every warp left idle), or nothing runs after a
+		// failure: fail what a fault left unfinished, then reset or go on.
+		const cudaError_t q = P.running ? cudaEventQuery(P.ev) : cudaSuccess;
+		if ((P.running && q != cudaErrorNotReady) || (!P.running && P.faulted && P.outstanding)) {
+			if (P.running && q != cudaSuccess && !P.faulted) {
+				P.faulted = true;
+				s->err = std::string("server: the serving launch failed: ") + cudaGetErrorString(q);
+			}
+			P.running = false;
+			P.stopping = false;
+			if (P.faulted) {
+				for (int k = 0; k < prt::kServeQueues; ++k) {
+					PQueue &Q = P.q[k];
+					for (uint32_t i = Q.first_open; i < Q.n_segs; ++i)
+						if (!Q.fin[i])
+							p_finish_slot(s, Q, i, PRT_ERR_DEVICE, lk);
+					Q.first_open = Q.n_segs;
+				}
+				s->cv_done.notify_all();
+			}
+			if (P.outstanding == 0) {
+				const cudaError_t e = p_reset(s);
+				if (e != cudaSuccess) {
+					s->err = std::string("server reset: ") + cudaGetErrorString(e);
+					P.faulted = true;
+				}
+			} else {
+				// Every warp left while work was still published (idle limit): go on.
+				const cudaError_t e = p_launch(s);
+				if (e != cudaSuccess) {
+					s->err = std::string("server launch: ") + cudaGetErrorString(e);
+					P.faulted = true;
+				}
+			}
+			s->cv_sched.notify_one();
+		}
+	}
+}
+
+void p_release(Persist &P) {
+	for (cudaStream_t st : {P.st, P.ctl, P.out})
+		if (st)
+			cudaStreamSynchronize(st);
+	for (int k = 0; k < prt::kServeQueues; ++k) {
+		PQueue &Q = P.q[k];
+		Q.segs.release();
+		Q.done_ctr.release();
+		for (void *h : {(void *)Q.h_segs, (void *)Q.h_words, (void *)Q.h_done})
+			if (h)
+				cudaFreeHost(h);
+		Q.h_segs = nullptr;
+		Q.h_words = Q.h_done = Q.d_done = nullptr;
+	}
+	P.state.release();
+	P.stop.release();
+	P.work.release();
+	for (void *h : {(void *)P.h_const, (void *)P.h_err})
+		if (h)
+			cudaFreeHost(h);
+	P.h_const = P.h_err = P.d_err = nullptr;
+	for (cudaEvent_t ev : {P.ev, P.ev_ctl})
+		if (ev)
+			cudaEventDestroy(ev);
+	for (cudaStream_t st : {P.st, P.ctl, P.out})
+		if (st)
+			cudaStreamDestroy(st);
+	P.ev = P.ev_ctl = nullptr;
+	P.st = P.ctl = P.out = nullptr;
+}
+
+// Streams, buffers and the empty queues of persistent mode.
+cudaError_t p_create(prt_b200_server *s) {
+	Persist &P = *s->P;
+	cudaError_t e = cudaSuccess;
+	for (cudaStream_t *st : {&P.st, &P.ctl, &P.out})
+		if (e == cudaSuccess)
+			e = cudaStreamCreateWithFlags(st, cudaStreamNonBlocking);
+	if (e == cudaSuccess)
+		e = cudaEventCreateWithFlags(&P.ev, cudaEventDisableTiming);
+	if (e == cudaSuccess)
+		e = cudaEventCreateWithFlags(&P.ev_ctl, cudaEventDisableTiming);
+	if (e == cudaSuccess)
+		e = P.state.reserve(prt::kServeQueues * sizeof(prt::ServeQueueState));
+	if (e == cudaSuccess)
+		e = P.stop.reserve(16);
+	if (e == cudaSuccess)
+		e = P.work.reserve(16);
+	if (e == cudaSuccess)
+		e = cudaMemset(P.work.p, 0, 16);
+	if (e == cudaSuccess)
+		e = cudaMallocHost(&P.h_const, 8);
+	if (e == cudaSuccess) {
+		P.h_const[0] = 0;
+		P.h_const[1] = 1;
+		e = cudaHostAlloc(&P.h_err, 16, cudaHostAllocMapped);
+	}
+	if (e == cudaSuccess)
+		e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&P.d_err), P.h_err, 0);
+	for (int k = 0; k < prt::kServeQueues && e == cudaSuccess; ++k) {
+		PQueue &Q = P.q[k];
+		e = Q.segs.reserve(sizeof(prt::SegDesc) * kQueueSegs);
+		if (e == cudaSuccess)
+			e = Q.done_ctr.reserve(4 * (size_t)kQueueSegs);
+		if (e == cudaSuccess)
+			e = cudaMallocHost(&Q.h_segs, sizeof(prt::SegDesc) * kQueueSegs);
+		if (e == cudaSuccess)
+			e = cudaMallocHost(&Q.h_words, 8 * (size_t)kQueueSegs);
+		if (e == cudaSuccess)
+			e = cudaHostAlloc(&Q.h_done, 4 * (size_t)kQueueSegs, cudaHostAllocMapped);
+		if (e == cudaSuccess)
+			e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&Q.d_done), Q.h_done, 0);
+		if (e == cudaSuccess) {
+			try {
+				Q.reqs.assign(kQueueSegs, nullptr);
+				Q.fin.assign(kQueueSegs, 1);
+			} catch (const std::bad_alloc &) {
+				e = cudaErrorMemoryAllocation;
+			}
+		}
+	}
+	if (e == cudaSuccess)
+		e = p_reset(s);
+	if (e == cudaSuccess)
+		e = cudaStreamSynchronize(P.ctl);
+	P.last_activity = Clock::now();
+	return e;
+}
+
 void shutdown(prt_b200_server *s) {
 	{
 		std::lock_guard<std::mutex> lk(s->mu);
@@ -433,6 +847,8 @@ void shutdown(prt_b200_server *s) {
 	s->cv_sched.notify_all();
 	if (s->sched.joinable())
 		s->sched.join();
+	if (s->P && s->P->completer.joinable())
+		s->P->completer.join(); // it finishes what is outstanding and stops the launch
 	for (auto &l : s->lanes) {
 		{
 			std::lock_guard<std::mutex> lk(s->mu);
@@ -474,15 +890,20 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		s->format = ctx->node_format;
 		s->batches_per_warp = (uint32_t)ctx->serve_batches_per_warp;
 		s->host_direct = ctx->host_direct;
+		s->persistent = ctx->serve_persistent;
 	}
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e == cudaSuccess)
 		e = s->region.reserve(budget_bytes);
 	s->alloc.reset(budget_bytes, 256);
+	if (e == cudaSuccess && s->persistent) {
+		s->P.reset(new (std::nothrow) Persist());
+		e = s->P ? p_create(s.get()) : cudaErrorMemoryAllocation;
+	}
 	int least = 0, greatest = 0;
 	if (e == cudaSuccess)
 		e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
-	for (uint32_t i = 0; i < n_lanes && e == cudaSuccess; ++i) {
+	for (uint32_t i = 0; i < n_lanes && e == cudaSuccess && !s->persistent; ++i) {
 		std::unique_ptr<Lane> L(new (std::nothrow) Lane());
 		if (!L) {
 			e = cudaErrorMemoryAllocation;
@@ -531,9 +952,14 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 	}
 	prt_b200_server *sp = s.get();
 	try {
-		for (auto &l : sp->lanes)
-			l->completer = std::thread(completer, sp, l.get());
-		sp->sched = std::thread(scheduler, sp);
+		if (sp->persistent) {
+			sp->P->completer = std::thread(completer_p, sp);
+			sp->sched = std::thread(scheduler_p, sp);
+		} else {
+			for (auto &l : sp->lanes)
+				l->completer = std::thread(completer, sp, l.get());
+			sp->sched = std::thread(scheduler, sp);
+		}
 	} catch (const std::exception &ex) {
 		// A thread that could not start: stop those that did and free everything.
 		ctx->err = std::string("server create: ") + ex.what();
@@ -551,6 +977,8 @@ void prt_b200_server_destroy(prt_b200_server *s) {
 	cudaSetDevice(s->ctx->device);
 	for (auto &l : s->lanes)
 		release_lane(*l);
+	if (s->P)
+		p_release(*s->P);
 	for (auto &kv : s->reqs)
 		delete kv.second;
 	s->region.release();

@@ -80,6 +80,7 @@ struct TravArgs {
 	unsigned long long *visits;
 	uint32_t use_cam;        // 1: rays of the single run come from `cam`, not seg0.rays
 	prt_b200_camera cam;
+	ServeQueues serve;       // PASS 3 only
 };
 
 // Per-warp shared memory: fixed part, then the queue and the pool (sizes per launch).
@@ -369,13 +370,80 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 	}
 }
 
+// A copy of a run descriptor that bypasses L1 (a serving launch reads descriptors that the
+// host's copies write while it runs).
+__device__ __forceinline__ SegDesc load_seg_cg(const SegDesc *p) {
+	static_assert(sizeof(SegDesc) % 8 == 0, "descriptor copied as 8-byte words");
+	SegDesc d;
+	const unsigned long long *src = reinterpret_cast<const unsigned long long *>(p);
+	unsigned long long *dst = reinterpret_cast<unsigned long long *>(&d);
+#pragma unroll
+	for (int k = 0; k < (int)(sizeof(SegDesc) / 8); ++k)
+		dst[k] = __ldcg(src + k);
+	return d;
+}
+
+// Serving launches (PASS 3): lane 0 takes the next batch, queues in priority order.  Batches
+// are tickets drawn with atomicAdd on the queue's `next` (a compare-and-swap retried by
+// thousands of warps on one word serialises them); a warp draws only when it saw a
+// published batch, and a ticket that lands past the published end (another warp took
+// the last one meanwhile) is kept in `held` until the host publishes that batch, while
+// the warp serves the other queues.  The host stops a launch only when every published
+// batch is finished, so tickets still held then are past all work.  Returns false when
+// the warp should leave: stop set, or idle for idle_limit polls (an idle warp sleeps 0.25
+// to 4 us between polls).  A warp that still holds a ticket after 16 x idle_limit polls
+// without stop sets the error flag and leaves: every wait is bounded.
+__device__ __forceinline__ bool claim_batch(const ServeQueues &q, uint32_t held[kServeQueues],
+                                            uint32_t &qsel, uint32_t &batch) {
+	uint32_t sleep_ns = 250;
+	for (uint32_t idle = 0;; ++idle) {
+		bool holding = false;
+#pragma unroll
+		for (uint32_t k = 0; k < (uint32_t)kServeQueues; ++k) {
+			ServeQueueState *st = q.state[k];
+			const uint32_t pub = *reinterpret_cast<volatile const uint32_t *>(&st->published);
+			if (held[k] != kNone) {
+				if (held[k] < pub) {
+					qsel = k;
+					batch = held[k];
+					held[k] = kNone;
+					return true;
+				}
+				holding = true;
+				continue;
+			}
+			if (*reinterpret_cast<volatile const uint32_t *>(&st->next) < pub) {
+				const uint32_t t = atomicAdd(&st->next, 1u);
+				if (t < pub) {
+					qsel = k;
+					batch = t;
+					return true;
+				}
+				held[k] = t; // past the end: served once published
+				holding = true;
+			}
+		}
+		if (*reinterpret_cast<volatile const uint32_t *>(q.stop))
+			return false;
+		if (idle >= (holding ? 16u * q.idle_limit : q.idle_limit)) {
+			if (holding)
+				*reinterpret_cast<volatile uint32_t *>(q.err_flag) = 1u;
+			return false;
+		}
+		__nanosleep(sleep_ns);
+		sleep_ns = min(sleep_ns * 2u, 4000u);
+	}
+}
+
 // LEAF1: every leaf holds one triangle (leaf size 1), so a hit leaf queues exactly one.
 // BOUNDED: a warp takes at most a.max_batches batches (a separate instantiation, so the
 // unbounded kernels keep their register allocation).
 // PASS: 0 = every batch with the general box test (the counting runs); 1 = batches whose
 // rays all have finite reciprocals, with the plain slab test only (no conservative code
 // in the kernel at all: 8 % faster), the others counted in a.deferred and skipped; 2 =
-// the skipped batches with the general test (returns at once when there are none).
+// the skipped batches with the general test (returns at once when there are none); 3 =
+// a serving launch: batches claimed from the serving queues (claim_batch), the plain or
+// the general test chosen per batch, descriptors and rays read around L1.
 template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
                                                            ? PRT_TRAVERSE_MIN_BLOCKS_FP32
@@ -397,6 +465,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 
 	if (BOUNDED && lane == 0)
 		S.batches = 0;
+	// Serving launches: lane 0's tickets past the published end, and the queue whose run
+	// S.seg holds (none yet).
+	uint32_t held[kServeQueues], cached_q = kNone;
+#pragma unroll
+	for (int k = 0; k < kServeQueues; ++k)
+		held[k] = kNone;
 	__syncwarp();
 	for (;;) {
 		if (BOUNDED) {
@@ -407,38 +481,69 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 				++S.batches;
 		}
 		// Batches are taken in order from a counter (the deferred pass has its own, so
-		// the few batches it works on spread over all warps).
+		// the few batches it works on spread over all warps); a serving launch claims
+		// them from its queues.
 		uint32_t base = 0;
-		if (lane == 0)
-			base = atomicAdd(PASS == 2 ? a.deferred + 1 : a.counter, 32u);
-		base = __shfl_sync(0xFFFFFFFFu, base, 0);
-		if (base >= a.n_virtual)
-			break;
-		// The run these 32 rays belong to (runs are padded to whole warps).
-		uint32_t si = 0;
-		if (a.n_segs) {
-			if (lane == 0) {
-				uint32_t lo_s = 0, hi_s = a.n_segs;
+		const SegDesc *segs = a.segs;
+		if (PASS == 3) {
+			uint32_t qsel = 0, batch = 0;
+			const bool got = lane == 0 ? claim_batch(a.serve, held, qsel, batch) : false;
+			if (!__shfl_sync(0xFFFFFFFFu, got, 0))
+				break;
+			qsel = __shfl_sync(0xFFFFFFFFu, qsel, 0);
+			base = 32u * __shfl_sync(0xFFFFFFFFu, batch, 0);
+			segs = a.serve.segs[qsel];
+			// The run of this batch: the warp's last one when it still covers it (a large
+			// request's batches mostly go to the same warps in turn), else a binary search
+			// of the table (around L1: the host writes it while the launch runs).
+			if (lane == 0 && !(cached_q == qsel && base >= (uint32_t)S.seg.vbegin &&
+			                   base - (uint32_t)S.seg.vbegin < S.seg.n_rays)) {
+				// Published after the table: covers every claimed batch.
+				const uint32_t n_segs = *reinterpret_cast<volatile const uint32_t *>(
+				    &a.serve.state[qsel]->n_segs);
+				uint32_t lo_s = 0, hi_s = n_segs;
 				while (hi_s - lo_s > 1) {
 					const uint32_t mid = (lo_s + hi_s) >> 1;
-					if (a.segs[mid].vbegin <= base)
+					if (__ldcg(&segs[mid].vbegin) <= base)
 						lo_s = mid;
 					else
 						hi_s = mid;
 				}
-				si = lo_s;
+				S.seg = load_seg_cg(segs + lo_s);
+				cached_q = qsel;
 			}
-			si = __shfl_sync(0xFFFFFFFFu, si, 0);
+		} else {
+			if (lane == 0)
+				base = atomicAdd(PASS == 2 ? a.deferred + 1 : a.counter, 32u);
+			base = __shfl_sync(0xFFFFFFFFu, base, 0);
+			if (base >= a.n_virtual)
+				break;
+			// The run these 32 rays belong to (runs are padded to whole warps).
+			uint32_t si = 0;
+			if (a.n_segs) {
+				if (lane == 0) {
+					uint32_t lo_s = 0, hi_s = a.n_segs;
+					while (hi_s - lo_s > 1) {
+						const uint32_t mid = (lo_s + hi_s) >> 1;
+						if (a.segs[mid].vbegin <= base)
+							lo_s = mid;
+						else
+							hi_s = mid;
+					}
+					si = lo_s;
+				}
+				si = __shfl_sync(0xFFFFFFFFu, si, 0);
+			}
+			if (lane == 0)
+				S.seg = a.n_segs ? a.segs[si] : a.seg0;
 		}
-		if (lane == 0)
-			S.seg = a.n_segs ? a.segs[si] : a.seg0;
 		__syncwarp();
 		const uint32_t local = base - (uint32_t)S.seg.vbegin;
 		const uint32_t run_rays = S.seg.n_rays;
 		if (local >= run_rays)
 			continue; // padding of the run
 		const uint32_t nb = min(32u, run_rays - local);
-		const SceneDesc sd = a.n_segs ? a.scenes[S.seg.scene] : a.scene0;
+		const SceneDesc sd = (PASS == 3 || a.n_segs) ? a.scenes[S.seg.scene] : a.scene0;
 		const float4 *__restrict__ tri4 = sd.tri4;
 
 		if ((uint32_t)lane < nb) {
@@ -450,7 +555,16 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			} else {
 				const float2 *rp =
 				    reinterpret_cast<const float2 *>(S.seg.rays + 6 * (size_t)(local + lane));
-				const float2 p0 = __ldcs(rp), p1 = __ldcs(rp + 1), p2 = __ldcs(rp + 2);
+				float2 p0, p1, p2;
+				if (PASS == 3) {
+					p0 = __ldcg(rp);
+					p1 = __ldcg(rp + 1);
+					p2 = __ldcg(rp + 2);
+				} else {
+					p0 = __ldcs(rp);
+					p1 = __ldcs(rp + 1);
+					p2 = __ldcs(rp + 2);
+				}
 				r = make_ray(p0.x, p0.y, p1.x, p1.y, p2.x, p2.y);
 			}
 			S.ro[lane] = make_float4(r.ox, r.oy, r.oz, __int_as_float(r.kind));
@@ -472,8 +586,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			}
 			if (PASS == 2 && regular)
 				continue; // done by the regular pass
-			trace_batch<FMT, COUNT, LEAF1, PASS == 1>(a, S, queue, pool, sd, nb, lane, g, s, lt,
-			                                          step_limit, n_visits, n_tests, fault);
+			if (PASS == 3 && regular)
+				trace_batch<FMT, COUNT, LEAF1, true>(a, S, queue, pool, sd, nb, lane, g, s, lt,
+				                                     step_limit, n_visits, n_tests, fault);
+			else
+				trace_batch<FMT, COUNT, LEAF1, PASS == 1>(a, S, queue, pool, sd, nb, lane, g, s,
+				                                          lt, step_limit, n_visits, n_tests, fault);
 		} else if (PASS == 2) {
 			continue; // the regular pass wrote this empty scene's misses
 		}
@@ -556,6 +674,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 					*reinterpret_cast<volatile uint32_t *>(S.seg.done_flag) = 1u;
 				}
 			}
+		}
+		if (PASS == 3 && fault && lane == 0) {
+			// The host learns of the fault at once (the run will never complete).
+			__threadfence_system();
+			*reinterpret_cast<volatile uint32_t *>(a.serve.err_flag) = 1u;
 		}
 		__syncwarp();
 	}
@@ -748,6 +871,44 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
 	a.err = d_err;
 	a.visits = d_visits;
 	return dispatch(a, cfg, sm_count, st);
+}
+
+namespace {
+
+template <int FMT, bool LEAF1>
+void launch_serving_t(const TravArgs &a, int sm_count, cudaStream_t st) {
+	const int bps = blocks_per_sm<FMT, false, LEAF1, false, 3>(kWarpsPerBlock, a.warp_bytes);
+	k_trace8<FMT, false, LEAF1, false, 3>
+	    <<<(unsigned)(sm_count * bps), 32 * kWarpsPerBlock, (size_t)a.warp_bytes * kWarpsPerBlock,
+	       st>>>(a);
+}
+
+} // namespace
+
+cudaError_t launch_serving(const SceneDesc *d_scenes, const ServeQueues &q, uint32_t depth,
+                           int leaf_size, uint32_t n_nodes, int format, uint32_t *d_err,
+                           cudaStream_t st, int sm_count) {
+	TravArgs a;
+	memset(&a, 0, sizeof a);
+	a.scenes = d_scenes;
+	a.serve = q;
+	a.n_nodes = n_nodes;
+	size_smem(a, depth, leaf_size);
+	a.err = d_err;
+	// Every resident slot: the warps poll for work, none waits for another, so the
+	// launch needs no co-residency (blocks that do not fit start as others leave).
+	if (format == PRT_NODES_COMPRESSED) {
+		if (a.max_leaf <= 1u)
+			launch_serving_t<PRT_NODES_COMPRESSED, true>(a, sm_count, st);
+		else
+			launch_serving_t<PRT_NODES_COMPRESSED, false>(a, sm_count, st);
+	} else {
+		if (a.max_leaf <= 1u)
+			launch_serving_t<PRT_NODES_FP32, true>(a, sm_count, st);
+		else
+			launch_serving_t<PRT_NODES_FP32, false>(a, sm_count, st);
+	}
+	return cudaGetLastError();
 }
 
 } // namespace prt

@@ -59,6 +59,30 @@ struct SegDesc {
 	uint32_t *done_flag = nullptr;
 };
 
+// The state of one serving queue (device memory): the host appends runs to its segment
+// table and then publishes their batches; warps of a running serving launch claim
+// batches one at a time with a compare-and-swap on `next`.
+struct ServeQueueState {
+	uint32_t published; // batches of 32 rays published (the host's copies)
+	uint32_t n_segs;    // runs in the table (copied by the host before `published`)
+	uint32_t next;      // batches claimed
+	uint32_t pad;
+};
+
+// A serving launch: kServeQueues queues in priority order (small requests' first).  The
+// launch's warps claim batches while any is published; an idle warp polls with a
+// growing sleep and leaves when *stop is set or after idle_limit polls, so the launch
+// ends by itself.
+constexpr int kServeQueues = 3;
+struct ServeQueues {
+	ServeQueueState *state[kServeQueues];
+	const SegDesc *segs[kServeQueues];
+	const uint32_t *stop;  // device memory, set by the host
+	uint32_t *err_flag;    // host memory the device reaches: set to 1 when a batch faults
+	uint32_t idle_limit;   // polls of an idle warp before it leaves
+	uint32_t pad;
+};
+
 // Levels of the 8-wide tree the traversal can walk.
 int traversal_stack_depth();
 
@@ -85,6 +109,12 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
                                          const TravConfig &cfg, uint32_t *d_work,
                                          unsigned long long *d_visits, uint32_t *d_err,
                                          cudaStream_t st, int sm_count);
+
+// Queues one serving launch over the queues `q` on `st` (resident warps only; it runs
+// until it is stopped or idle).  Scenes as for launch_nearest_hits_segments.
+cudaError_t launch_serving(const SceneDesc *d_scenes, const ServeQueues &q, uint32_t depth,
+                           int leaf_size, uint32_t n_nodes, int format, uint32_t *d_err,
+                           cudaStream_t st, int sm_count);
 
 // Store mode for an output pointer (16-byte, 4-byte or byte stores).
 inline uint32_t store_mode_for(const void *p) {

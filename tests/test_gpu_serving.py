@@ -25,6 +25,18 @@ def _fields_equal(a, b, lay):
     return None
 
 
+def _server(backend, d_tris, off, persistent=1, **kw):
+    """A server in persistent mode (requests folded into one running launch) or wave mode
+    (each group of admitted requests one launch on a lane)."""
+    from portablert_gb300.serve import Server
+
+    backend.set_option("serve_persistent", persistent)
+    try:
+        return Server(backend, d_tris.data_ptr(), off, **kw)
+    finally:
+        backend.set_option("serve_persistent", 1)
+
+
 def _scenes(torch, sizes, seed):
     tris = [workloads.soup_tris(seed + s, n) for s, n in enumerate(sizes)]
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.uint64)
@@ -33,10 +45,9 @@ def _scenes(torch, sizes, seed):
     return tris, off, d
 
 
-def test_mix_equals_alone(gpu_backend):
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_mix_equals_alone(gpu_backend, persistent):
     import torch
-
-    from portablert_gb300.serve import Server
 
     sizes = [16, 300, 5000, 40_000, 1, 2, 120_000, 777]
     tris, off, d_tris = _scenes(torch, sizes, 5000)
@@ -47,7 +58,7 @@ def test_mix_equals_alone(gpu_backend):
         n = int(np.exp(rng.uniform(np.log(1), np.log(300_000))))
         tags = COMBOS[int(rng.integers(len(COMBOS)))]
         reqs.append((s, workloads.soup_rays(9100 + i, n), tags))
-    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=64 << 20, lanes=4)
+    srv = _server(gpu_backend, d_tris, off, persistent, budget_bytes=64 << 20, lanes=4)
     results = [None] * len(reqs)
     try:
         def client(k):
@@ -68,7 +79,7 @@ def test_mix_equals_alone(gpu_backend):
         lat = [srv.wait(r[0]) for r in results]
         assert all(x >= 0 for x in lat)
         assert srv.stat("completed") == len(reqs)
-        assert srv.stat("waves") >= 2
+        assert srv.stat("waves") >= (1 if persistent else 2)
         assert srv.stat("peak_bytes") <= srv.stat("budget_bytes")
         assert srv.stat("bytes_in_use") == 0
     finally:
@@ -82,13 +93,13 @@ def test_mix_equals_alone(gpu_backend):
         assert bad is None, (i, s, len(rays), tags, bad)
 
 
+@pytest.mark.parametrize("persistent", [1, 0])
 @pytest.mark.parametrize("host_direct", [1, 0])
-def test_budget_admission_and_limits(gpu_backend, host_direct):
+def test_budget_admission_and_limits(gpu_backend, host_direct, persistent):
     """host_direct 1: records go straight to the host buffers and only rays take budget;
-    0: records are staged in the budget region too and copied out."""
+    0: records are staged in the budget region too and copied out.  At most two requests
+    are admitted at once, in waves or in the running launch."""
     import torch
-
-    from portablert_gb300.serve import Server
 
     tris, off, d_tris = _scenes(torch, [2000, 3000], 5100)
     tags = ("t", "primitive_id", "valid")
@@ -98,7 +109,7 @@ def test_budget_admission_and_limits(gpu_backend, host_direct):
     budget = 2 * per + 1000  # two requests fit at once, not three
     gpu_backend.set_option("host_direct", host_direct)
     try:
-        srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=budget, lanes=4)
+        srv = _server(gpu_backend, d_tris, off, persistent, budget_bytes=budget, lanes=4)
     finally:
         gpu_backend.set_option("host_direct", 1)
     try:
@@ -106,8 +117,11 @@ def test_budget_admission_and_limits(gpu_backend, host_direct):
         for t, _ in subs:
             srv.wait(t)
         assert srv.stat("peak_bytes") <= budget
-        assert srv.stat("waves") >= 5  # at most two requests per wave
-        assert srv.stat("max_wave_requests") <= 2
+        if persistent:
+            assert srv.stat("max_in_flight_waves") <= 2  # requests admitted at once
+        else:
+            assert srv.stat("waves") >= 5  # at most two requests per wave
+            assert srv.stat("max_wave_requests") <= 2
         for i, (_, out) in enumerate(subs):
             gpu_backend.set_tris(tris[i % 2])
             want = gpu_backend.nearest_hits(workloads.soup_rays(5200 + i, n), tags)
@@ -124,15 +138,15 @@ def test_budget_admission_and_limits(gpu_backend, host_direct):
         srv.close()
 
 
-@pytest.mark.parametrize("leaf,fmt,per_warp", [(1, 0, 1), (8, 0, 2), (4, 1, 2), (8, 1, 0),
-                                               (1, 1, 3)])
-def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
-    """Every traversal variant a wave can run -- leaf sizes, node formats, warps bounded
-    to 1-3 batches of 32 rays or persistent (0) -- gives each request the records of
-    nearest_hits on its scene alone."""
+@pytest.mark.parametrize("leaf,fmt,per_warp,persistent",
+                         [(1, 0, 1, 0), (8, 0, 2, 0), (4, 1, 2, 0), (8, 1, 0, 0), (1, 1, 3, 0),
+                          (1, 0, 1, 1), (8, 0, 1, 1), (4, 1, 1, 1), (1, 1, 1, 1)])
+def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp, persistent):
+    """Every traversal variant a server can run -- leaf sizes, node formats, wave warps
+    bounded to 1-3 batches of 32 rays or unbounded (0), and the running launch of
+    persistent mode -- gives each request the records of nearest_hits on its scene
+    alone."""
     import torch
-
-    from portablert_gb300.serve import Server
 
     sizes = [3000, 50_000, 7, 200_000]
     tris, off, d_tris = _scenes(torch, sizes, 5800 + leaf)
@@ -142,7 +156,7 @@ def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
         gpu_backend.set_option("leaf_size", leaf)
         gpu_backend.set_option("node_format", fmt)
         gpu_backend.set_option("serve_batches_per_warp", per_warp)
-        srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=128 << 20, lanes=3)
+        srv = _server(gpu_backend, d_tris, off, persistent, budget_bytes=128 << 20, lanes=3)
         try:
             reqs = [(i % len(sizes), workloads.soup_rays(5900 + i, [33, 70_000, 1, 9_999][i % 4]))
                     for i in range(12)]
@@ -162,19 +176,17 @@ def test_wave_kernels_equal_alone(gpu_backend, leaf, fmt, per_warp):
 
 
 def test_requests_finish_alone_not_with_their_wave(gpu_backend):
-    """One lane, so requests queued behind a running wave share the next one: the wave
-    runs its small requests first and each finishes when its own rays are stored, not
-    when the 1.5M-ray request on the dense scene is done."""
+    """Wave mode, one lane, so requests queued behind a running wave share the next one:
+    the wave runs its small requests first and each finishes when its own rays are
+    stored, not when the 1.5M-ray request on the dense scene is done."""
     import torch
-
-    from portablert_gb300.serve import Server
 
     tris, off, d_tris = _scenes(torch, [300_000, 2_000], 6100)
     # Records go to the host buffers in place, so a request takes only its rays' bytes
     # of the budget: 19.2 MB for the first, 36 MB for the large one, under 1 MB for the
     # small ones.  With 40 MB the first runs alone (the large one does not fit beside it
     # and the small ones queue behind the large one), and the next wave takes the rest.
-    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=40 << 20, lanes=1)
+    srv = _server(gpu_backend, d_tris, off, 0, budget_bytes=40 << 20, lanes=1)
     tags = ("t", "primitive_id", "valid")
     lay = hitreg.layout(tags)
     try:
@@ -197,27 +209,27 @@ def test_requests_finish_alone_not_with_their_wave(gpu_backend):
         srv.close()
 
 
-def test_close_with_requests_queued(gpu_backend):
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_close_with_requests_queued(gpu_backend, persistent):
     import torch
 
-    from portablert_gb300.serve import Server
-
     _, off, d_tris = _scenes(torch, [50_000], 5300)
-    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=32 << 20, lanes=2)
+    srv = _server(gpu_backend, d_tris, off, persistent, budget_bytes=32 << 20, lanes=2)
     keep = [srv.submit(0, workloads.soup_rays(5400 + i, 100_000), ("valid",)) for i in range(6)]
     srv.close()  # answers or fails every queued request, joins its threads
     assert keep
 
 
-def test_small_requests_take_the_express_lane(gpu_backend):
+@pytest.mark.parametrize("persistent", [1, 0])
+def test_small_requests_take_the_express_lane(gpu_backend, persistent):
     """Small requests queued behind a large one on a dense scene go to the express lane
-    (lane 0, highest priority) and still equal their answers alone."""
+    (wave mode: lane 0, highest priority) or the express queue (persistent mode: warps
+    take its batches first), finish before the large one and still equal their answers
+    alone."""
     import torch
 
-    from portablert_gb300.serve import Server
-
     tris, off, d_tris = _scenes(torch, [300_000, 2_000], 5500)
-    srv = Server(gpu_backend, d_tris.data_ptr(), off, budget_bytes=256 << 20, lanes=3)
+    srv = _server(gpu_backend, d_tris, off, persistent, budget_bytes=256 << 20, lanes=3)
     tags = ("t", "primitive_id", "valid")
     lay = hitreg.layout(tags)
     try:
@@ -231,5 +243,30 @@ def test_small_requests_take_the_express_lane(gpu_backend):
         for (s, r), (_, out) in zip(small, subs):
             gpu_backend.set_tris(tris[s])
             assert _fields_equal(out, gpu_backend.nearest_hits(r, tags), lay) is None
+    finally:
+        srv.close()
+
+
+def test_running_launch_stops_when_idle_and_starts_again(gpu_backend):
+    """Persistent mode: the running launch ends after 5 ms without work and the next
+    request starts another; answers stay equal to nearest_hits alone."""
+    import torch
+
+    tris, off, d_tris = _scenes(torch, [20_000], 6500)
+    srv = _server(gpu_backend, d_tris, off, 1, budget_bytes=64 << 20, lanes=1)
+    tags = hitreg.TAGS
+    lay = hitreg.layout(tags)
+    try:
+        outs = []
+        for k in range(3):
+            rays = workloads.soup_rays(6600 + k, 50_000)
+            t, out = srv.submit(0, rays, tags)
+            srv.wait(t)
+            outs.append((rays, out))
+            time.sleep(0.05)  # long enough for the launch to stop
+        assert srv.stat("waves") >= 3  # one launch per burst
+        gpu_backend.set_tris(tris[0])
+        for rays, out in outs:
+            assert _fields_equal(out, gpu_backend.nearest_hits(rays, tags), lay) is None
     finally:
         srv.close()
