@@ -8,9 +8,11 @@ Inputs are synthetic (seeded generators in portablert_gb300/workloads.py).
 
 Prints one JSON line (driver contract): value = Mrays/s over the timed steps (CUDA
 events on the launching stream, L2 flushed between steps), e2e = the same through the
-host-buffer C ABI call (rays copied in and records copied out every step), roofline of
-the traversal kernel against the measured HBM bandwidth, the CPU baseline (the oracle
-port of the reference CPU backend on this host's cores, bounded sample), and the SM
+host-buffer C ABI call (rays read from and records written to host memory within every
+timed call), rooflines of the traversal kernel (instruction issue, L2, HBM) with the one
+that binds, the build's roofline, parity of every timed ray against the oracle port of
+the reference CPU backend (run in the CPU-baseline leg, which also times that port on
+this host's cores on a bounded sample), the other configurations' legs, and the SM
 clocks sampled during the timed region.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
@@ -163,6 +165,69 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, ctypes; reads
+    only) every millisecond while the timed region runs -- nvidia-smi's 50 ms period
+    sees one or two samples of a 32 ms region.  Falls back to ClockSampler when NVML
+    cannot be loaded."""
+
+    # nvmlClocksEventReason bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device: int = 0, period_s: float = 0.001):
+        self.device, self.period = device, period_s
+        self.samples, self.reasons, self.max_mhz = [], 0, None
+        self.fallback = None
+        self.stop_evt = threading.Event()
+        try:
+            import ctypes
+
+            L = ctypes.CDLL("libnvidia-ml.so.1")
+            if L.nvmlInit_v2() != 0:
+                raise OSError("nvmlInit failed")
+            h = ctypes.c_void_p()
+            if L.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(device), ctypes.byref(h)) != 0:
+                raise OSError("no NVML handle")
+            fn = getattr(L, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                L.nvmlDeviceGetCurrentClocksThrottleReasons
+            self.L, self.h, self.reason_fn, self.ct = L, h, fn, ctypes
+            mx = ctypes.c_uint()
+            if L.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:  # 1 = NVML_CLOCK_SM
+                self.max_mhz = float(mx.value)
+        except (OSError, AttributeError):
+            self.L = None
+            self.fallback = ClockSampler(device)
+
+    def _run(self):
+        ct = self.ct
+        mhz, r = ct.c_uint(), ct.c_ulonglong()
+        while not self.stop_evt.is_set():
+            if self.L.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(mhz)) == 0:
+                self.samples.append(float(mhz.value))
+            if self.reason_fn(self.h, ct.byref(r)) == 0:
+                self.reasons |= int(r.value)
+            time.sleep(self.period)
+
+    def start(self):
+        if self.fallback:
+            return self.fallback.start()
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        if self.fallback:
+            return self.fallback.stop()
+        self.stop_evt.set()
+        self.t.join()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(self.samples)), "sm_max_mhz": self.max_mhz,
+                "sm_min_mhz": float(min(self.samples)),
+                "reasons": sorted(n for bit, n in self.REASONS.items() if self.reasons & bit),
+                "samples": len(self.samples), "source": "NVML, 1 ms period"}
 
 
 def make_workload(prim_hits_fn):
@@ -827,7 +892,7 @@ def run_gpu(args, world, rank):
     b.sync()
     sync_ranks(world)
     torch.cuda.synchronize()
-    clocks = ClockSampler(dev)
+    clocks = NvmlSampler(dev)
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
