@@ -1142,8 +1142,20 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 	int level = 0;
 	bool large_left = true; // children are smaller than their parent: once no large task
 	                        // is left, none comes back, and its four kernels are skipped
+	// Before the first look at the level counters (a host wait each): as many levels as
+	// halving splits need to bring the largest scene under the large-task size, since a
+	// split leaves at least one triangle on each side and most leave about half.
+	int ahead = 1;
+	{
+		uint32_t biggest = 0;
+		for (uint32_t sc = 0; sc < S; ++sc)
+			biggest = std::max(biggest, plan.toff[sc + 1] - plan.toff[sc]);
+		for (uint64_t c = biggest; c > kLarge; c = (c + 1) / 2)
+			++ahead;
+		ahead = std::max(ahead, kLevelsPerCheck);
+	}
 	for (;;) {
-		for (int k = 0; k < kLevelsPerCheck && level < kMaxLevels; ++k, ++level) {
+		for (int k = 0; k < ahead && level < kMaxLevels; ++k, ++level) {
 			const int par = level & 1;
 			// Grids no larger than the work the level can hold: each task has at most two
 			// children, so level L has at most S * 2^L tasks of a tier (a small scene's
@@ -1183,6 +1195,7 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 			msg = "sah build: more than " + std::to_string(kMaxLevels) + " levels";
 			return PRT_ERR_LIMIT;
 		}
+		ahead = kLevelsPerCheck;
 	}
 	k_sah_small<<<2432, 128, 0, st>>>(A);
 	// Every node id handed out must have been written before the collapse follows the
