@@ -93,7 +93,11 @@ struct alignas(16) WarpFixed {
 	float4 rd[32];              // direction per slot
 	SegDesc seg;                // the run the current 32 rays belong to
 	uint32_t batches;           // batches this warp has taken (kept here, not in a register)
-	uint32_t pad_[3];
+	// Serving launches: tickets past the published end per queue, and the queue whose
+	// run `seg` holds (kept here, not in registers).
+	uint32_t held[kServeQueues];
+	uint32_t cached_q;
+	uint32_t pad_[(16 - (4 + 4 * kServeQueues + 4) % 16) % 16 / 4];
 };
 static_assert(sizeof(WarpFixed) % 16 == 0, "queue and pool must start 16-byte aligned");
 
@@ -465,12 +469,11 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 
 	if (BOUNDED && lane == 0)
 		S.batches = 0;
-	// Serving launches: lane 0's tickets past the published end, and the queue whose run
-	// S.seg holds (none yet).
-	uint32_t held[kServeQueues], cached_q = kNone;
-#pragma unroll
-	for (int k = 0; k < kServeQueues; ++k)
-		held[k] = kNone;
+	if (PASS == 3 && lane == 0) {
+		for (int k = 0; k < kServeQueues; ++k)
+			S.held[k] = kNone;
+		S.cached_q = kNone;
+	}
 	__syncwarp();
 	for (;;) {
 		if (BOUNDED) {
@@ -487,7 +490,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		const SegDesc *segs = a.segs;
 		if (PASS == 3) {
 			uint32_t qsel = 0, batch = 0;
-			const bool got = lane == 0 ? claim_batch(a.serve, held, qsel, batch) : false;
+			const bool got = lane == 0 ? claim_batch(a.serve, S.held, qsel, batch) : false;
 			if (!__shfl_sync(0xFFFFFFFFu, got, 0))
 				break;
 			qsel = __shfl_sync(0xFFFFFFFFu, qsel, 0);
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			// The run of this batch: the warp's last one when it still covers it (a large
 			// request's batches mostly go to the same warps in turn), else a binary search
 			// of the table (around L1: the host writes it while the launch runs).
-			if (lane == 0 && !(cached_q == qsel && base >= (uint32_t)S.seg.vbegin &&
+			if (lane == 0 && !(S.cached_q == qsel && base >= (uint32_t)S.seg.vbegin &&
 			                   base - (uint32_t)S.seg.vbegin < S.seg.n_rays)) {
 				// Published after the table: covers every claimed batch.
 				const uint32_t n_segs = *reinterpret_cast<volatile const uint32_t *>(
@@ -510,7 +513,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 						hi_s = mid;
 				}
 				S.seg = load_seg_cg(segs + lo_s);
-				cached_q = qsel;
+				S.cached_q = qsel;
 			}
 		} else {
 			if (lane == 0)
