@@ -204,6 +204,12 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *                  memory, once; the call that meets it returns PRT_ERR_OOM and the
  *                  context stays usable.  0 disarms (default 0).  Only this call sets
  *                  it; it has no environment override
+ *   "fail_serve_after" test hook: n > 0 makes persistent request servers created
+ *                  afterwards treat their n-th publication as if one of its batches had
+ *                  faulted: the request never completes and the fault flag rises from the
+ *                  host.  The server stops its launch once the rest of the published work
+ *                  is done, fails that request with PRT_ERR_DEVICE, resets its queues and
+ *                  serves again.  0 = off (default 0).  Only this call sets it
  *   "pipe_chunks"  1..16: chunks a host-buffer nearest_hits splits its rays into, so
  *                  copies and traversals overlap (default 8)
  *   "pipe_min_rays" fewest rays per chunk, a multiple of 32 (default 2^15)

@@ -82,9 +82,9 @@ int check_device_errors(prt_b200_ctx *ctx) {
 // Every tuning option prt_b200_set_option accepts.  PRT_B200_<KEY> in the environment
 // (the name in upper case, e.g. PRT_B200_LEAF_SIZE=4) sets option <key> of each new
 // context, so programs that use the backend through portableRT's API can be tuned
-// unchanged.  The test hook "fail_alloc_after" is deliberately not among them: it arms
-// a process-wide allocation-failure injector, which no environment variable of a
-// production program should be able to reach.
+// unchanged.  The test hooks "fail_alloc_after" and "fail_serve_after" are deliberately
+// not among them: they inject failures, which no environment variable of a production
+// program should be able to reach.
 const char *const kOptionKeys[] = {"leaf_size",        "node_format",   "block",
                                    "pipe_chunks",      "pipe_ramp",     "pipe_min_rays",
                                    "serve_batches_per_warp", "pool_depth", "count_visits",
@@ -603,6 +603,10 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 			ctx->host_direct = v != 0;
 		} else if (k == "serve_persistent") {
 			ctx->serve_persistent = v != 0;
+		} else if (k == "fail_serve_after") {
+			if (v < 0)
+				return fail(ctx, PRT_ERR_ARG, "fail_serve_after must be >= 0");
+			ctx->fail_serve_after = v;
 		} else if (k == "fail_alloc_after") {
 			if (v < 0)
 				return fail(ctx, PRT_ERR_ARG, "fail_alloc_after must be >= 0");

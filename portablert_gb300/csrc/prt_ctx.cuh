@@ -75,6 +75,8 @@ struct prt_b200_ctx {
 	int block = 128;
 	int pool_depth = 0; // tree depth a batch graph's traversal pool is sized for (0 = 32)
 	int serve_batches_per_warp = 1; // request servers created later ("serve_batches_per_warp")
+	int64_t fail_serve_after = 0;   // test hook: a new persistent server's n-th publication
+	                                // raises its fault flag ("fail_serve_after"; 0 = off)
 	bool serve_persistent = true;   // request servers created later fold requests into one
 	                                // running launch ("serve_persistent"; 0 = waves)
 	bool count = false;

@@ -134,6 +134,8 @@ struct Persist {
 	PQueue q[prt::kServeQueues];
 	bool running = false, stopping = false, faulted = false, full = false;
 	uint64_t outstanding = 0;   // published, not finished
+	uint64_t fail_after = 0;    // test hook: raise the fault flag after this publication
+	uint64_t published = 0;     // publications so far
 	Clock::time_point last_activity;
 	std::thread completer;
 };
@@ -563,6 +565,11 @@ cudaError_t p_publish(prt_b200_server *s, int qi, Request *r) {
 	d.pad = 0;
 	d.done_ctr = Q.done_ctr.as<uint32_t>() + i;
 	d.done_flag = Q.d_done + i;
+	// Test hook: this publication behaves as if one of its batches faulted -- its run is
+	// not counted, so the request never completes -- and the fault flag rises.
+	const bool inject = P.fail_after && ++P.published == P.fail_after;
+	if (inject)
+		d.done_ctr = d.done_flag = nullptr;
 	Q.h_segs[i] = d;
 	Q.reqs[i] = r;
 	Q.fin[i] = 0;
@@ -581,6 +588,8 @@ cudaError_t p_publish(prt_b200_server *s, int qi, Request *r) {
 		e = cudaMemcpyAsync(&st->published, Q.h_words + 2 * i + 1, 4, cudaMemcpyHostToDevice, P.ctl);
 	++P.outstanding;
 	s->max_in_flight = std::max<uint64_t>(s->max_in_flight, P.outstanding);
+	if (inject)
+		*reinterpret_cast<volatile uint32_t *>(P.h_err) = 1u; // as the faulted batch would
 	if (qi == 0)
 		++s->express_waves;
 	return e;
@@ -885,12 +894,14 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 		prt_b200_batch_destroy(s->batch);
 		return rc;
 	}
+	uint64_t fail_serve_after = 0;
 	{
 		std::lock_guard<std::mutex> lk(ctx->mu);
 		s->format = ctx->node_format;
 		s->batches_per_warp = (uint32_t)ctx->serve_batches_per_warp;
 		s->host_direct = ctx->host_direct;
 		s->persistent = ctx->serve_persistent;
+		fail_serve_after = (uint64_t)ctx->fail_serve_after;
 	}
 	cudaError_t e = cudaSetDevice(ctx->device);
 	if (e == cudaSuccess)
@@ -899,6 +910,8 @@ int prt_b200_server_create(prt_b200_ctx *ctx, const float *d_tris, const uint64_
 	if (e == cudaSuccess && s->persistent) {
 		s->P.reset(new (std::nothrow) Persist());
 		e = s->P ? p_create(s.get()) : cudaErrorMemoryAllocation;
+		if (s->P)
+			s->P->fail_after = fail_serve_after;
 	}
 	int least = 0, greatest = 0;
 	if (e == cudaSuccess)

@@ -155,7 +155,7 @@ def _option_lists():
     return accepted, env_keys, documented
 
 
-TEST_HOOKS = {"fail_alloc_after"}  # set_option only: no environment override
+TEST_HOOKS = {"fail_alloc_after", "fail_serve_after"}  # set_option only: no environment override
 
 
 def test_every_option_is_documented_and_settable_from_the_environment():

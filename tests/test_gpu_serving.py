@@ -270,3 +270,43 @@ def test_running_launch_stops_when_idle_and_starts_again(gpu_backend):
             assert _fields_equal(out, gpu_backend.nearest_hits(rays, tags), lay) is None
     finally:
         srv.close()
+
+
+def test_fault_fails_unfinished_requests_then_serves(gpu_backend):
+    """Persistent mode, failure injected on the host (option fail_serve_after): the third
+    request is published as if one of its batches had faulted (it never completes) and
+    the fault flag rises.  The server stops its launch once the other published work is
+    done (their answers stay right), fails the third request with PRT_ERR_DEVICE, resets
+    its queues and then serves again."""
+    import torch
+
+    tris, off, d_tris = _scenes(torch, [300_000, 3_000], 6700)
+    gpu_backend.set_option("fail_serve_after", 3)
+    try:
+        srv = _server(gpu_backend, d_tris, off, 1, budget_bytes=256 << 20, lanes=1)
+    finally:
+        gpu_backend.set_option("fail_serve_after", 0)
+    tags = ("t", "primitive_id", "valid")
+    lay = hitreg.layout(tags)
+    try:
+        reqs = [(0, workloads.soup_rays(6800 + i, 400_000)) for i in range(6)]
+        subs = [srv.submit(s, r, tags) for s, r in reqs]
+        codes = []
+        for t, _ in subs:
+            try:
+                srv.wait(t)
+                codes.append(0)
+            except PrtError as e:
+                codes.append(e.code)
+        assert codes == [0, 0, 5, 0, 0, 0], codes  # PRT_ERR_DEVICE for the third
+        gpu_backend.set_tris(tris[0])
+        for (s, r), (_, out), c in zip(reqs, subs, codes):
+            if c == 0:
+                assert _fields_equal(out, gpu_backend.nearest_hits(r, tags), lay) is None
+        rays = workloads.soup_rays(6900, 20_000)
+        t, out = srv.submit(1, rays, tags)
+        srv.wait(t)
+        gpu_backend.set_tris(tris[1])
+        assert _fields_equal(out, gpu_backend.nearest_hits(rays, tags), lay) is None
+    finally:
+        srv.close()
