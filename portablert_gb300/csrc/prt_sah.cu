@@ -238,16 +238,16 @@ __device__ Split choose_split(const uint32_t *b, const float *fsc, uint32_t coun
 			s.node = shfl_box(p, 31);
 		const Box6 r = shfl_box(q, min(lane + 1, 31));
 		const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, qc, 1);
-		uint64_t key = ~0ull;
-		if (fsc[a] > 0.0f && lane < 31 && pc > 0 && rc > 0) {
-			const float cost = box_area(p) * (float)pc + box_area(r) * (float)rc;
-			key = ((uint64_t)f2ord(cost) << 32) | ((uint32_t)a << 8) | (uint32_t)lane;
-		}
-#pragma unroll
-		for (int o = 16; o > 0; o >>= 1) {
-			const uint64_t y = __shfl_xor_sync(0xFFFFFFFFu, key, o);
-			key = y < key ? y : key;
-		}
+		// The least cost on this axis, then the lowest plane with it (two redux.sync
+		// minima).
+		uint32_t c32 = 0xFFFFFFFFu;
+		if (fsc[a] > 0.0f && lane < 31 && pc > 0 && rc > 0)
+			c32 = f2ord(box_area(p) * (float)pc + box_area(r) * (float)rc);
+		const uint32_t cmin = __reduce_min_sync(0xFFFFFFFFu, c32);
+		const uint32_t plane = __reduce_min_sync(
+		    0xFFFFFFFFu, (c32 == cmin && c32 != 0xFFFFFFFFu) ? (uint32_t)lane : 0xFFu);
+		const uint64_t key =
+		    cmin == 0xFFFFFFFFu ? ~0ull : (((uint64_t)cmin << 32) | ((uint32_t)a << 8) | plane);
 		if (key < best) {
 			best = key;
 			const int src = (int)(key & 0xFF);
@@ -948,17 +948,20 @@ __global__ void __launch_bounds__(128) k_sah_small(SahArgs A) {
 								q = box_union(q, qd);
 						}
 						const Box6 r = shfl_box(q, min(lane + 1, 31));
-						uint64_t ck = ~0ull;
+						// The least cost on this axis and, among its lanes, the lowest
+						// position: two 32-bit warp minima (redux.sync) instead of five
+						// shuffle rounds of a 64-bit key.
+						uint32_t c32 = 0xFFFFFFFFu;
 						if (in && lane < f + cnt - 1) {
 							const int nl = lane - f + 1, nr = cnt - nl;
-							const float cost = box_area(p) * (float)nl + box_area(r) * (float)nr;
-							ck = ((uint64_t)f2ord(cost) << 32) | ((uint32_t)a << 8) | (uint32_t)(lane - f);
+							c32 = f2ord(box_area(p) * (float)nl + box_area(r) * (float)nr);
 						}
-#pragma unroll
-						for (int o = 16; o > 0; o >>= 1) {
-							const uint64_t y = __shfl_xor_sync(0xFFFFFFFFu, ck, o);
-							ck = y < ck ? y : ck;
-						}
+						const uint32_t cmin = __reduce_min_sync(0xFFFFFFFFu, c32);
+						const uint32_t pos = __reduce_min_sync(
+						    0xFFFFFFFFu, (c32 == cmin && c32 != 0xFFFFFFFFu) ? (uint32_t)(lane - f) : 0xFFu);
+						const uint64_t ck = cmin == 0xFFFFFFFFu
+						                        ? ~0ull
+						                        : (((uint64_t)cmin << 32) | ((uint32_t)a << 8) | pos);
 						if (ck < best) {
 							best = ck;
 							axis_best = a;
