@@ -27,9 +27,16 @@
 //              requests whose buffers the device cannot reach, finishes them and frees
 //              the lane
 //
-// A request's records are exactly nearest_hits<Tags...> on its scene alone: the wave's
-// launch gives each request its own segment (rays padded to whole warps), and the
-// traversal of a ray depends only on the ray, its scene and the record layout.
+// That is wave mode (option serve_persistent 0).  In persistent mode (the default) there
+// are no waves: the scheduler appends each admitted request to one of three device
+// queues by size while one serving launch runs, the launch's warps take the queues'
+// batches smallest-request-first, and the completer finishes requests from their
+// completion flags, stops the launch when the server is idle and starts it again when
+// work is outstanding (see the persistent-mode section below).
+//
+// A request's records are exactly nearest_hits<Tags...> on its scene alone: the launch
+// gives each request its own segment (rays padded to whole warps), and the traversal of
+// a ray depends only on the ray, its scene and the record layout.
 //
 // No counterpart in the reference (portableRT answers one synchronous call at a time,
 // include/portableRT/nearest_hits_impl.hpp:28-36).

@@ -26,7 +26,9 @@
 //    rays all have finite reciprocals (the plain slab test only), which counts and skips
 //    the others, and a deferred pass over those with the conservative test for zero
 //    direction components (it returns at once when there are none).  Camera queries and
-//    counting runs are one general launch.
+//    counting runs are one general launch.  A request server's serving launch (pass 3)
+//    takes its batches from device queues that the host extends while it runs
+//    (claim_batch) and picks the plain or the general test per batch.
 //  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
 //    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
 //  * When the pool and the queue are empty the warp recomputes each slot's winning
