@@ -132,7 +132,7 @@ def tree_dependent_rays(tris, rays, oracle, threads=0):
 
 
 def check(got, want, tags, tris, rays, oracle, threads=0):
-    """The full parity verdict of `got` against the reference's records `want`:
+    """The full parity outcome of `got` against the reference's records `want`:
     compare() for every ray, except that a tree-dependent ray must instead equal the
     leaf-only answer bit for bit.  Returns {n, hits, n_bad, bad (first 20), ties,
     tree_dependent}."""

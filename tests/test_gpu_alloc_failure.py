@@ -88,8 +88,8 @@ def test_host_call_staging_fails_then_recovers():
     try:
         b.set_tris(tris)
         # The copy pipeline from the first query on.  A call grows the rays' staging
-        # buffer, then the records', when its batch is larger than any before: round 1
-        # fails the first growth, round 2 (twice the rays) the second.
+        # buffer, then the records', when its batch is larger than any before: the first
+        # call fails the first growth, the second (twice the rays) the second growth.
         b.set_option("host_direct", 0)
         for k, m in ((1, 50_001), (2, 100_003)):
             with Armed(b, k):
