@@ -1148,12 +1148,15 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 	// Before the first look at the level counters (a host wait each): as many levels as
 	// halving splits need to bring the largest scene under the large-task size, since a
 	// split leaves at least one triangle on each side and most leave about half.
+	// For scenes of at most 64 Ki triangles the mid levels too (down to the small-task
+	// size): their empty large-tier launches cost less than the wait they save.
 	int ahead = 1;
 	{
 		uint32_t biggest = 0;
 		for (uint32_t sc = 0; sc < S; ++sc)
 			biggest = std::max(biggest, plan.toff[sc + 1] - plan.toff[sc]);
-		for (uint64_t c = biggest; c > kLarge; c = (c + 1) / 2)
+		const uint32_t floor = biggest <= 65536u ? kSmall : kLarge;
+		for (uint64_t c = biggest; c > floor; c = (c + 1) / 2)
 			++ahead;
 		ahead = std::max(ahead, kLevelsPerCheck);
 	}

@@ -327,15 +327,35 @@ def run_heightfield_build(repeats: int = 2) -> dict:
     return res
 
 
+def run_soup_build(n_tris: int = 4096, repeats: int = 2) -> dict:
+    """set_tris of the small configuration's soup (seed 0, n_tris triangles) `repeats`
+    times with the default SAH build."""
+    from . import backend
+
+    b = backend.B200Backend(0)
+    b.init()
+    tris = soup_tris(0, n_tris)
+    ms = []
+    for _ in range(repeats):
+        b.set_tris(tris)
+        ms.append(b.stat("build_ms"))
+    res = {"build_ms": ms, "nodes": b.stat("n_nodes"), "depth": b.stat("depth")}
+    b.shutdown()
+    return res
+
+
 if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser(description="run a workload on cuda:0")
-    ap.add_argument("workload", choices=["clustered", "heightfield-build"])
+    ap.add_argument("workload", choices=["clustered", "heightfield-build", "soup-build"])
+    ap.add_argument("--tris", type=int, default=4096)
     ap.add_argument("--rays", type=int, default=1_048_576)
     ap.add_argument("--repeats", type=int, default=2)
     args = ap.parse_args()
     if args.workload == "clustered":
         print(run_clustered(args.rays, args.repeats))
+    elif args.workload == "soup-build":
+        print(run_soup_build(args.tris, args.repeats))
     else:
         print(run_heightfield_build(args.repeats))
