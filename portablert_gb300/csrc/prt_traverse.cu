@@ -19,8 +19,11 @@
 //    group reads one 128-byte line of the node (children 2s and 2s + 1 would spread each
 //    load over two lines and double the L1 wavefronts: 15 % slower).  Hit inner children
 //    are pushed back as items and hit leaf triangles are appended to a triangle queue,
-//    at positions from ballots and popc.  Roots of new rays are admitted whenever fewer
-//    than 8 items are left.  Unused child slots hold NaN boxes, which no plain slab test
+//    at positions from ballots and popc, child-major (all lanes' first children, then
+//    all second children: no position depends on the lane's previous child; the step
+//    issues 16 % fewer ALU-pipe instructions than in lane order, and the half-rate ALU
+//    pipe is what bounds it).  Roots of new rays are admitted whenever fewer than 8
+//    items are left.  Unused child slots hold NaN boxes, which no plain slab test
 //    passes.
 //  * A query of ray buffers is two launches: a regular pass over the batches whose 32
 //    rays all have finite reciprocals (the plain slab test only), which counts and skips
@@ -36,8 +39,8 @@
 //    caller's HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
 //  * The pool holds at most 7 K (D - 1) + K items for K = 8 items per step and a tree of
 //    depth D (each step's pushes leave at most 7 K items behind per level); it is sized
-//    per launch as 7 K (D - 1) + 2 K, and a push that would not fit is reported as an
-//    error instead of written.
+//    per launch as 7 K (D - 1) + 2 K; a push that would not fit, or a batch that takes
+//    more steps than a tree can need, is reported as an error and ends the batch.
 //
 // Algorithmic bytes per ray: 24 (ray) + R (record) + node bytes visited + 48 per
 // triangle tested; the counting variant (COUNT) measures the visits.
@@ -258,22 +261,19 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 	uint32_t next = 0; // next slot whose root is not yet in the pool
 	uint32_t steps = 0;
 	for (;;) {
-		// Admit new rays while fewer than K items are pending.
-		if (top < (uint32_t)kItems && next < nb) {
-			const uint32_t add = min((uint32_t)kItems - top, nb - next);
-			if ((uint32_t)lane < add)
-				pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
-			top += add;
-			next += add;
-			__syncwarp();
-		}
-		if (top == 0u)
-			break;
-		if (++steps > step_limit) {
-			if (lane == 0)
-				atomicOr(a.err, kErrStack);
-			fault = true;
-			break;
+		// Admit new rays while fewer than K items are pending (a branch the common step
+		// skips with one test).
+		if (top < (uint32_t)kItems) {
+			if (next < nb) {
+				const uint32_t add = min((uint32_t)kItems - top, nb - next);
+				if ((uint32_t)lane < add)
+					pool[top + lane] = ((next + lane) << kIndexBits) | sd.root;
+				top += add;
+				next += add;
+				__syncwarp();
+			}
+			if (top == 0u)
+				break;
 		}
 		const uint32_t take = min(top, (uint32_t)kItems);
 		top -= take;
@@ -291,62 +291,68 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		uint32_t child[kChildPerLane], leaf_n[kChildPerLane];
 #pragma unroll
 		for (int j = 0; j < kChildPerLane; ++j) {
-			hit[j] = false;
-			inner[j] = false;
-			child[j] = 0;
-			leaf_n[j] = 0;
 			test_child<FMT, REGULAR>(nodes, r, node, s + kLanesPerNode * j, hit[j], inner[j],
 			                         child[j], leaf_n[j]);
 			hit[j] = hit[j] && work;
 		}
+		// Every hit leaf of the step holds one triangle: always with single-triangle leaves
+		// (predicates only on that path: the half-rate ALU pipe bounds the step).
+		bool one_each = true;
+		if (!LEAF1) {
+			bool single = true;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j)
+				single = single && (!hit[j] || inner[j] || leaf_n[j] <= 1u);
+			one_each = __all_sync(0xFFFFFFFFu, single);
+		}
 
-		// Push the hit inner children as new items (lane order, then child order).
-		uint32_t n_push = 0, before = 0;
-		bool push[kChildPerLane];
+		// Positions, child-major: every lane's child j before any lane's child j + 1, so
+		// no position waits on the lane's previous child.  Pushed inner children go to
+		// the pool; with at most one triangle per hit leaf the queue positions come from
+		// the same ballots.
+		uint32_t pp[kChildPerLane], pq[kChildPerLane];
+		uint32_t ptop = top, qtop = q;
 #pragma unroll
 		for (int j = 0; j < kChildPerLane; ++j) {
-			push[j] = hit[j] && inner[j];
-			const uint32_t b = __ballot_sync(0xFFFFFFFFu, push[j]);
-			n_push += __popc(b);
-			before += __popc(b & lt);
+			const uint32_t bp = __ballot_sync(0xFFFFFFFFu, hit[j] && inner[j]);
+			pp[j] = ptop + __popc(bp & lt);
+			ptop += __popc(bp);
+			if (one_each) {
+				const uint32_t bl = __ballot_sync(0xFFFFFFFFu, hit[j] && !inner[j]);
+				pq[j] = qtop + __popc(bl & lt);
+				qtop += __popc(bl);
+			}
 		}
-		if (top + n_push > a.pool_cap) {
+		// The pool holds every push of a well-formed tree and a well-formed tree ends
+		// within step_limit steps; anything else is reported and ends the batch.
+		++steps;
+		if (ptop > a.pool_cap || steps > step_limit) {
 			if (lane == 0)
 				atomicOr(a.err, kErrStack);
 			fault = true;
-		} else {
-			uint32_t pos = top + before;
-#pragma unroll
-			for (int j = 0; j < kChildPerLane; ++j)
-				if (push[j])
-					pool[pos++] = (slot << kIndexBits) | child[j];
-			top += n_push;
+			break;
 		}
-
-		// Queue the triangles of the hit leaf children.
-		uint32_t cnt[kChildPerLane], all_cnt = 0;
-		bool single = true;
-#pragma unroll
-		for (int j = 0; j < kChildPerLane; ++j) {
-			cnt[j] = (hit[j] && !inner[j]) ? (LEAF1 ? 1u : leaf_n[j]) : 0u;
-			all_cnt += cnt[j];
-			single = single && cnt[j] <= 1u;
-		}
-		if (LEAF1 || __all_sync(0xFFFFFFFFu, single)) {
-			uint32_t n_add = 0, pre = 0;
+		const uint32_t hi = slot << kIndexBits;
+		if (one_each) {
 #pragma unroll
 			for (int j = 0; j < kChildPerLane; ++j) {
-				const uint32_t b = __ballot_sync(0xFFFFFFFFu, cnt[j] != 0u);
-				n_add += __popc(b);
-				pre += __popc(b & lt);
+				if (hit[j] && inner[j])
+					pool[pp[j]] = hi | child[j];
+				if (hit[j] && !inner[j])
+					queue[pq[j]] = hi | child[j];
 			}
-			uint32_t pos = q + pre;
+		} else {
 #pragma unroll
 			for (int j = 0; j < kChildPerLane; ++j)
-				if (cnt[j])
-					queue[pos++] = (slot << kIndexBits) | child[j];
-			q += n_add;
-		} else {
+				if (hit[j] && inner[j])
+					pool[pp[j]] = hi | child[j];
+			// Leaves of several triangles: positions from a scan of the per-lane counts.
+			uint32_t cnt[kChildPerLane], all_cnt = 0;
+#pragma unroll
+			for (int j = 0; j < kChildPerLane; ++j) {
+				cnt[j] = (hit[j] && !inner[j]) ? leaf_n[j] : 0u;
+				all_cnt += cnt[j];
+			}
 			uint32_t incl = all_cnt;
 #pragma unroll
 			for (int o = 1; o < 32; o <<= 1) {
@@ -358,9 +364,11 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 #pragma unroll
 			for (int j = 0; j < kChildPerLane; ++j)
 				for (uint32_t k = 0; k < cnt[j]; ++k)
-					queue[pos++] = (slot << kIndexBits) | (child[j] + k);
-			q += __shfl_sync(0xFFFFFFFFu, incl, 31);
+					queue[pos++] = hi | (child[j] + k);
+			qtop = q + __shfl_sync(0xFFFFFFFFu, incl, 31);
 		}
+		top = ptop;
+		q = qtop;
 		__syncwarp();
 		while (q >= 32u) {
 			q -= 32u;
