@@ -35,8 +35,8 @@ sys.path.insert(0, ROOT)
 from portablert_gb300 import hitreg, workloads  # noqa: E402
 
 METRIC = "nearest-hit Mrays/s (plain vs compressed BVH, same hits); build Mtris/s; p99 ms"
-N_SECONDARY = 4_194_304
-DELTA = 0.01
+N_SECONDARY = workloads.HF_SECONDARY
+DELTA = workloads.HF_DELTA
 TAGS = hitreg.TAGS
 
 
@@ -231,14 +231,7 @@ class NvmlSampler:
 
 
 def make_workload(prim_hits_fn):
-    tris = workloads.heightfield_tris(seed=1)
-    prim = workloads.camera_rays()
-    h = prim_hits_fn(tris, prim)
-    sec = workloads.secondary_rays(tris, prim, h["valid"] != 0, h["primitive_id"],
-                                   np.stack([h["px"], h["py"], h["pz"]], 1), N_SECONDARY,
-                                   delta=DELTA, seed=1)
-    rays = np.ascontiguousarray(np.concatenate([prim, sec]), dtype=np.float32)
-    return tris, prim, rays
+    return workloads.heightfield_workload(prim_hits_fn)
 
 
 def workload_config(n_tris, n_prim, n_rays):

@@ -615,8 +615,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		uint32_t *stage = pool;
 		const uint32_t rec = S.seg.rec_size, fmask = S.seg.mask;
 		const uint32_t rw = rec >> 2;
-		for (uint32_t w = 0; w < rw; ++w)
-			stage[lane * rw + w] = 0u;
+		// 32 records of rw words: rw * 8 16-byte words (record sizes are multiples of 4).
+		for (uint32_t k = lane; k < rw * 8u; k += 32u)
+			reinterpret_cast<uint4 *>(stage)[k] = make_uint4(0u, 0u, 0u, 0u);
 		__syncwarp();
 		if ((uint32_t)lane < nb) {
 			const RayC r = slot_ray(S, lane);

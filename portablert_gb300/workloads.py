@@ -111,6 +111,7 @@ def soup(seed: int = 0, n_tris: int = 4096, n_rays: int = 65536):
 # ---------------------------------------------------------------- heightfield
 
 HF_NX, HF_NZ = 1024, 512
+HF_SECONDARY, HF_DELTA = 4_194_304, 0.01 # secondary rays of the heightfield workload
 CAM_EYE = (0.0, 3.0, -6.0)
 CAM_W, CAM_H = 1920, 1080
 
@@ -306,6 +307,59 @@ def run_clustered(n_rays: int = 1_048_576, repeats: int = 2) -> dict:
     return res
 
 
+def heightfield_workload(primary_hits):
+    """The heightfield workload: 1,048,576 triangles (seed 1), 1920x1080 pinhole primary
+    rays and HF_SECONDARY cosine secondary rays (seed 1) leaving the primary hits offset
+    by HF_DELTA.  primary_hits(tris, prim) returns the primary rays' records as a dict of
+    fields (valid, primitive_id, px, py, pz)."""
+    tris = heightfield_tris(seed=1)
+    prim = camera_rays()
+    h = primary_hits(tris, prim)
+    sec = secondary_rays(tris, prim, h["valid"] != 0, h["primitive_id"],
+                         np.stack([h["px"], h["py"], h["pz"]], 1), HF_SECONDARY,
+                         delta=HF_DELTA, seed=1)
+    rays = np.ascontiguousarray(np.concatenate([prim, sec]), dtype=np.float32)
+    return tris, prim, rays
+
+
+def run_heightfield(repeats: int = 2) -> dict:
+    """The heightfield workload (all five tags): one set_tris, then `repeats`
+    nearest_hits_dev passes with FP32 nodes and `repeats` with compressed nodes over all
+    6,267,904 rays -- the launches a profiler capture of the regular pass selects from
+    (the primary-ray pass that makes the secondary rays comes first)."""
+    import torch
+
+    from . import backend, hitreg
+
+    b = backend.B200Backend(0)
+    b.init()
+
+    def primary_hits(tris, prim):
+        b.set_tris(tris)
+        return b.nearest_hits(prim, hitreg.TAGS)
+
+    tris, prim, rays = heightfield_workload(primary_hits)
+    n = len(rays)
+    lay = hitreg.layout(hitreg.TAGS)
+    d_r = torch.from_numpy(rays).cuda()
+    out = torch.zeros(n * lay.size, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    for fmt in (0, 1):
+        b.set_option("node_format", fmt)
+        for _ in range(repeats):
+            b.nearest_hits_dev(d_r.data_ptr(), n, out.data_ptr(), hitreg.TAGS)
+        b.sync()
+    b.set_option("node_format", 0)
+    b.set_option("count_visits", 1)
+    b.nearest_hits_dev(d_r.data_ptr(), n, out.data_ptr(), hitreg.TAGS)
+    b.sync()
+    res = {"rays": n, "nodes": b.stat("n_nodes"), "depth": b.stat("depth"),
+           "node_visits_per_ray": b.stat("visits_nodes") / n,
+           "tri_tests_per_ray": b.stat("visits_tris") / n}
+    b.shutdown()
+    return res
+
+
 def run_heightfield_build(repeats: int = 2) -> dict:
     """set_tris_dev of the 1,048,576-triangle heightfield (seed 1) `repeats` times with the
     default SAH build: the launches a profiler capture of the build selects from."""
@@ -348,13 +402,16 @@ if __name__ == "__main__":
     import argparse
 
     ap = argparse.ArgumentParser(description="run a workload on cuda:0")
-    ap.add_argument("workload", choices=["clustered", "heightfield-build", "soup-build"])
+    ap.add_argument("workload",
+                    choices=["clustered", "heightfield", "heightfield-build", "soup-build"])
     ap.add_argument("--tris", type=int, default=4096)
     ap.add_argument("--rays", type=int, default=1_048_576)
     ap.add_argument("--repeats", type=int, default=2)
     args = ap.parse_args()
     if args.workload == "clustered":
         print(run_clustered(args.rays, args.repeats))
+    elif args.workload == "heightfield":
+        print(run_heightfield(args.repeats))
     elif args.workload == "soup-build":
         print(run_soup_build(args.tris, args.repeats))
     else:
