@@ -193,6 +193,11 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "collapse_cost" 1 = the binary tree is collapsed to 8-wide nodes by the least
  *                  expected cost per ray (a bottom-up pass chooses which subtrees become
  *                  nodes and leaves), 0 = by opening the largest child first (default 1)
+ *   "build_small"  1 = with build_sah, set_tris builds a scene of at most 4,096 triangles
+ *                  in one thread block: Morton order, PLOC clustering (radius 3) into a
+ *                  binary tree whose least-cost records are computed as it merges, the
+ *                  collapse and the triangle re-layout in one launch (default 1; 0 = the
+ *                  binned-SAH build at every size)
  *   "host_direct"  1 = a host-buffer nearest_hits whose buffers the device can reach in
  *                  place (pinned memory; pageable memory where the device reads it
  *                  through the host's page tables, as on Grace) traverses them there:
@@ -225,7 +230,8 @@ int prt_b200_batch_stat(prt_b200_batch *batch, const char *key, double *value);
  *   "pipe_ramp"    1 = chunk sizes ramp up and down (1, 2, 4, 8, ..., 8, 4, 2, 1), so
  *                  the unoverlapped first copy-in and last copy-out are short (default 1)
  * Statistics: "n_tris", "n_nodes", "depth", "build_ms", "build_sah" (1 = the scene's tree
- *   is an SAH tree), "in_place" (1 = the last host-buffer nearest_hits traversed the
+ *   is from the quality build: binned SAH, or the one-block build), "build_small" (1 = the
+ *   one-block build made it), "in_place" (1 = the last host-buffer nearest_hits traversed the
  *   caller's buffers in place), "node_bytes", "tri_bytes",
  *   "visits_nodes", "visits_tris" (totals of the last counted nearest_hits), "sms".
  * Every option but the test hook can also be set for each new context from the

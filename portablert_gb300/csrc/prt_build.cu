@@ -32,6 +32,7 @@
 
 #include "../../include/prt_b200.h"
 #include "prt_build.cuh"
+#include "prt_collapse.cuh"
 #include "prt_sah.cuh"
 
 namespace prt {
@@ -64,13 +65,6 @@ void BuildScratch::release() {
 }
 
 namespace {
-
-constexpr int kMaxLevels = 32;       // 8-wide levels (the traversal's depth limit)
-constexpr int kLevelsPerCheck = 4;   // collapse launches between host checks
-// counters layout: [0, kMaxLevels] frontier size per level, then nodes used, triangles placed
-constexpr int kCtrNodes = kMaxLevels + 1;
-constexpr int kCtrTris = kMaxLevels + 2;
-constexpr int kCtrWords = kMaxLevels + 3;
 
 struct Item {
 	uint32_t ref;  // binary-tree reference (bit 31 = leaf); kNone = empty scene
@@ -331,12 +325,6 @@ __global__ void k_leaf_boxes(const float *__restrict__ tris, const uint32_t *__r
 	lbox[2 * i + 1] = hi;
 }
 
-__device__ __forceinline__ float half_area(float4 lo, float4 hi) {
-	float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-	float a = dx * dy + dx * dz + dy * dz;
-	return isfinite(a) ? a : FLT_MAX;
-}
-
 // atomicAdd(p, 1) with acquire-release ordering at device scope.
 __device__ __forceinline__ uint32_t arrive_acq_rel(uint32_t *p) {
 	uint32_t old;
@@ -395,48 +383,6 @@ __global__ void k_refit(uint32_t n, uint32_t n_int, const uint32_t *__restrict__
 	}
 }
 
-// Cost-optimal collapse.  Without culling by t, a ray tests the children of every 8-wide
-// node whose box it passes and every triangle of every leaf box it passes, so the
-// expected work per ray is proportional to the sum of area x cost over those boxes: 1
-// per 8-wide node, kTriCost per triangle of a leaf.  A bottom-up pass computes for each
-// binary node the least cost of its subtree in a single child slot (c1: as a leaf, or
-// as an 8-wide node whose 8 slots are shared out below it) and in i = 2..8 slots when
-// the node itself is opened (cd), with the split of the slots between its children; the
-// collapse then opens exactly what the optimum opens.  (The dynamic programme of Ylitie,
-// Karras and Laine 2017 for compressed wide BVHs, restated for this traversal's costs.)
-// Costs are stored in units of the node's own surface area (expected work once a ray
-// passes its box), so they stay in float range whatever the scene's scale; a child
-// enters its parent's sums weighted by the ratio of the two areas, both computed from
-// half extents divided by the parent's largest one (values in [0, 1]: no overflow for
-// [-FLT_MAX, FLT_MAX] boxes, no underflow for tiny scenes).
-constexpr float kTriCost = 0.25f; // a triangle test against a node visit (measured)
-
-struct CostNode {
-	float c1;
-	float cd[7];   // slots 2..8
-	uint32_t bits; // 3 bits per slot count i = 2..8: (left share - 1); bit 31: leaf is best
-};
-
-__device__ __forceinline__ float3 half_extent(float4 lo, float4 hi) {
-	return make_float3(fmaxf(hi.x * 0.5f - lo.x * 0.5f, 0.0f),
-	                   fmaxf(hi.y * 0.5f - lo.y * 0.5f, 0.0f),
-	                   fmaxf(hi.z * 0.5f - lo.z * 0.5f, 0.0f));
-}
-
-// Surface area (up to a constant) of a box of half extents e, in units of unit^2.
-__device__ __forceinline__ float scaled_area(float3 e, float unit) {
-	if (!(unit > 0.0f))
-		return 0.0f;
-	const float x = fminf(e.x / unit, 1.0f), y = fminf(e.y / unit, 1.0f),
-	            z = fminf(e.z / unit, 1.0f);
-	return x * y + x * z + y * z;
-}
-
-__device__ __forceinline__ uint32_t split_of(uint32_t bits, uint32_t i) {
-	const uint32_t a = ((bits >> (3u * (i - 2u))) & 7u) + 1u;
-	return min(max(a, 1u), i - 1u);
-}
-
 // Costs of child `y` in j = 1..7 slots (cs[j]), in units of its own area; returns its
 // half extents.
 __device__ __forceinline__ float3 child_costs(uint32_t y, const CostNode *cost,
@@ -444,16 +390,15 @@ __device__ __forceinline__ float3 child_costs(uint32_t y, const CostNode *cost,
                                               float cs[8]) {
 	if (y & kLeafBit) {
 		const uint32_t k = y & ~kLeafBit;
-#pragma unroll
-		for (int j = 1; j < 8; ++j)
-			cs[j] = kTriCost;
+		leaf_costs(cs);
 		return half_extent(__ldcg(&lbox[2 * k]), __ldcg(&lbox[2 * k + 1]));
 	}
-	const float c1 = __ldcg(&cost[y].c1);
-	cs[1] = c1;
+	CostNode c;
+	c.c1 = __ldcg(&cost[y].c1);
 #pragma unroll
-	for (int j = 2; j < 8; ++j)
-		cs[j] = fminf(c1, __ldcg(&cost[y].cd[j - 2]));
+	for (int j = 0; j < 7; ++j)
+		c.cd[j] = __ldcg(&cost[y].cd[j]);
+	node_costs(c, cs);
 	return half_extent(__ldcg(&ibox[2 * y]), __ldcg(&ibox[2 * y + 1]));
 }
 
@@ -481,39 +426,8 @@ __global__ void k_collapse_cost(uint32_t n, uint32_t n_ids, const uint32_t *__re
 		const float3 el = child_costs(left[p], cost, ibox, lbox, cl);
 		const float3 er = child_costs(right[p], cost, ibox, lbox, cr);
 		const float3 ep = half_extent(__ldcg(&ibox[2 * p]), __ldcg(&ibox[2 * p + 1]));
-		const float unit = fmaxf(ep.x, fmaxf(ep.y, ep.z));
-		const float ap = scaled_area(ep, unit);
-		const float rl = ap > 0.0f ? fminf(scaled_area(el, unit) / ap, 1.0f) : 0.0f;
-		const float rr = ap > 0.0f ? fminf(scaled_area(er, unit) / ap, 1.0f) : 0.0f;
-#pragma unroll
-		for (int j = 1; j < 8; ++j) {
-			cl[j] *= rl;
-			cr[j] *= rr;
-		}
-		CostNode c;
-		c.bits = 0;
-#pragma unroll
-		for (uint32_t s = 2; s <= 8; ++s) {
-			float best = INFINITY;
-			uint32_t ba = 1;
-#pragma unroll
-			for (uint32_t a = 1; a < s; ++a) {
-				const float v = cl[a] + cr[s - a];
-				if (v < best) {
-					best = v;
-					ba = a;
-				}
-			}
-			c.cd[s - 2] = best;
-			c.bits |= (ba - 1u) << (3u * (s - 2u));
-		}
-		const uint32_t count = rlast[p] - rfirst[p] + 1u;
-		const float as_node = 1.0f + c.cd[6];
-		const bool may_leaf = count <= leaf_size;
-		const float as_leaf = kTriCost * (float)count;
-		c.c1 = may_leaf ? fminf(as_node, as_leaf) : as_node;
-		if (may_leaf && as_leaf <= as_node)
-			c.bits |= 0x80000000u;
+		const CostNode c =
+		    merge_costs(cl, cr, el, er, ep, rlast[p] - rfirst[p] + 1u, leaf_size);
 		__stcg(&cost[p].c1, c.c1);
 #pragma unroll
 		for (int k = 0; k < 7; ++k)
@@ -973,7 +887,7 @@ inline unsigned blocks_for(uint64_t n, unsigned t) { return (unsigned)((n + t - 
 
 int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg, bool sah, bool collapse_cost) {
+               std::string &msg, bool sah, bool collapse_cost, bool one_block) {
 	if (leaf_size < 1 || leaf_size > kMaxLeaf) {
 		msg = "leaf_size must be in [1, 8]";
 		return PRT_ERR_ARG;
@@ -1000,6 +914,7 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	plan.multi = S > 1;
 	plan.sah = sah;
 	plan.collapse_cost = collapse_cost;
+	plan.small = one_block && sah && S == 1 && n64 >= 1 && n64 <= small_build_max();
 	plan.toff.resize(S + 1);
 	plan.ioff.resize(S + 1);
 	for (uint32_t s = 0; s <= S; ++s)
@@ -1028,6 +943,7 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	sc.n_nodes = 0;
 	sc.depth = 0;
 	sc.has_cnodes = false;
+	sc.built_small = false;
 	sc.h_tri_off.assign(tri_off64, tri_off64 + S + 1);
 
 	const size_t key_bytes = plan.multi ? 8 : 4;
@@ -1059,7 +975,7 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	BUILD_TRY(ws.sort_tiles.reserve(8 * 4));
 	BUILD_TRY(ws.sort_status.reserve(4 * sort_status_words(n)));
 	BUILD_TRY(ws.bounds.reserve(24ull * S));
-	if (sah) {
+	if (sah && !plan.small) {
 		BUILD_TRY(ws.sah.reserve(sah_scratch_bytes(n, S)));
 		BUILD_TRY(ws.roots.reserve(4ull * S));
 	}
@@ -1072,6 +988,8 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * (size_t)plan.node_cap));
 	if (!ws.h_counters)
 		BUILD_TRY(cudaMallocHost(&ws.h_counters, 4 * kCtrWords));
+	if (plan.small)
+		return PRT_OK; // the one-block build reads no offset table
 	BUILD_TRY(cudaMemcpyAsync(sc.tri_off.p, plan.toff.data(), 4ull * (S + 1),
 	                          cudaMemcpyHostToDevice, st));
 	BUILD_TRY(cudaMemcpyAsync(ws.int_off.p, plan.ioff.data(), 4ull * (S + 1),
@@ -1147,6 +1065,22 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 	if (plan.sah && !host_checks) {
 		msg = "the SAH build reads its level counters on the host";
 		return PRT_ERR_ARG;
+	}
+	if (plan.small) {
+		// One block: PLOC, collapse and re-layout in one launch; the compression reads the
+		// node count on the device, so the host waits once, at the end.
+		uint32_t *ctr = ws.counters.as<uint32_t>();
+		BUILD_TRY(cudaMemsetAsync(ctr, 0, 4 * kCtrWords, st));
+		BUILD_TRY(launch_build_small(d_tris, n, (uint32_t)plan.leaf_size, plan.collapse_cost, ws,
+		                             sc, plan.node_cap, ctr, d_err, st));
+		sc.built_small = true;
+		if (plan.compressed) {
+			k_compress<<<blocks_for(8ull * plan.node_cap, 256), 256, 0, st>>>(
+			    sc.nodes.as<Node8>(), plan.node_cap, ctr + kCtrNodes, sc.cnodes.as<CNode8>());
+			sc.has_cnodes = true;
+		}
+		BUILD_TRY(cudaGetLastError());
+		return host_checks ? build_finish(sc, ws, st, msg) : PRT_OK;
 	}
 	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
 	uint32_t *d_ioff = ws.int_off.as<uint32_t>();
@@ -1250,10 +1184,11 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
-                 uint32_t *d_err, std::string &msg, bool sah, bool collapse_cost) {
+                 uint32_t *d_err, std::string &msg, bool sah, bool collapse_cost,
+                 bool one_block) {
 	BuildPlan plan;
 	int rc = build_plan(tri_off, n_scenes, leaf_size, compressed, sc, ws, st, plan, msg, sah,
-	                    collapse_cost);
+	                    collapse_cost, one_block);
 	if (rc != PRT_OK)
 		return rc;
 	return build_enqueue(d_tris, plan, sc, ws, st, d_err, true, msg);
@@ -1261,10 +1196,10 @@ int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes
 
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
                 BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg, bool sah,
-                bool collapse_cost) {
+                bool collapse_cost, bool one_block) {
 	const uint64_t off[2] = {0, n};
 	return build_scenes(d_tris, off, 1, leaf_size, compressed, sc, ws, st, d_err, msg, sah,
-	                    collapse_cost);
+	                    collapse_cost, one_block);
 }
 
 } // namespace prt

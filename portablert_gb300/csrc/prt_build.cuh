@@ -59,6 +59,7 @@ struct SceneGPU {
 	uint32_t depth = 0;  // levels of the deepest tree
 	int leaf_size = 1;
 	bool has_cnodes = false;
+	bool built_small = false; // the last build was the one-block build (prt_build_small.cu)
 	DevBuf tri4;         // float4[3 n]
 	DevBuf inv;          // uint32[n]
 	DevBuf nodes;        // Node8[n_nodes]
@@ -109,6 +110,8 @@ struct BuildPlan {
 	bool compressed = false, multi = false;
 	bool sah = false;                 // binned-SAH binary trees instead of LBVH
 	bool collapse_cost = true;        // cost-optimal 8-wide collapse (else largest area first)
+	bool small = false;               // one scene of 1..small_build_max() triangles, with the
+	                                  // quality build requested: one block builds it (PLOC)
 	std::vector<uint32_t> toff, ioff; // triangle and binary-node offsets per scene
 };
 
@@ -118,9 +121,12 @@ struct BuildPlan {
 // Morton/Karras hierarchy; needs host checks.  collapse_cost: collapse to 8-wide nodes
 // by the least expected cost (a bottom-up pass over the binary tree) instead of opening
 // the largest child first.
+// one_block: a single scene of at most small_build_max() triangles with sah set is built
+// by one thread block (prt_build_small.cu) instead.
 int build_plan(const uint64_t *tri_off, uint32_t n_scenes, int leaf_size, bool compressed,
                SceneGPU &sc, BuildScratch &ws, cudaStream_t st, BuildPlan &plan,
-               std::string &msg, bool sah = false, bool collapse_cost = true);
+               std::string &msg, bool sah = false, bool collapse_cost = true,
+               bool one_block = false);
 
 // Queues the build kernels.  host_checks: read the level counters every few levels and
 // finish with build_finish (synchronises).  Without host checks nothing synchronises:
@@ -140,11 +146,19 @@ int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &m
 int build_scenes(const float *d_tris, const uint64_t *tri_off, uint32_t n_scenes, int leaf_size,
                  bool compressed, SceneGPU &sc, BuildScratch &ws, cudaStream_t st,
                  uint32_t *d_err, std::string &msg, bool sah = false,
-                 bool collapse_cost = true);
+                 bool collapse_cost = true, bool one_block = false);
 
 // One scene: build_scenes with tri_off = {0, n}.
 int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed, SceneGPU &sc,
                 BuildScratch &ws, cudaStream_t st, uint32_t *d_err, std::string &msg,
-                bool sah = false, bool collapse_cost = true);
+                bool sah = false, bool collapse_cost = true, bool one_block = false);
+
+// The one-block build (prt_build_small.cu): the largest scene it takes, and its launch
+// (PLOC binary tree, collapse, triangle re-layout; the level counters at `ctr` end as
+// the multi-launch build leaves them).
+uint32_t small_build_max();
+cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
+                               BuildScratch &ws, SceneGPU &sc, uint32_t node_cap, uint32_t *ctr,
+                               uint32_t *d_err, cudaStream_t st);
 
 } // namespace prt

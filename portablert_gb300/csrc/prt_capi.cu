@@ -89,7 +89,7 @@ const char *const kOptionKeys[] = {"leaf_size",        "node_format",   "block",
                                    "pipe_chunks",      "pipe_ramp",     "pipe_min_rays",
                                    "serve_batches_per_warp", "pool_depth", "count_visits",
                                    "build_compressed", "build_sah",     "collapse_cost",
-                                   "host_direct",      "serve_persistent"};
+                                   "build_small",      "host_direct",   "serve_persistent"};
 
 // The overrides set in the environment, as (key, value); false with a message when a
 // value is not a decimal integer.
@@ -141,7 +141,8 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 	std::string msg;
 	bool sah = ctx->build_sah;
 	int rc = prt::build_scene(d_tris, n, ctx->leaf_size, ctx->build_compressed, ctx->scene,
-	                          ctx->ws, ctx->stream, ctx->d_err(), msg, sah, ctx->collapse_cost);
+	                          ctx->ws, ctx->stream, ctx->d_err(), msg, sah, ctx->collapse_cost,
+	                          ctx->build_small);
 	if (sah && rc == PRT_ERR_LIMIT) {
 		// An SAH tree deeper than the collapse's 32 levels: the LBVH's depth is bounded.
 		sah = false;
@@ -150,6 +151,7 @@ int do_build(prt_b200_ctx *ctx, const float *d_tris, uint64_t n) {
 		                      ctx->ws, ctx->stream, ctx->d_err(), msg, false, ctx->collapse_cost);
 	}
 	ctx->last_build_sah = sah;
+	ctx->last_build_small = ctx->scene.built_small;
 	cudaEventRecord(ev.b, ctx->stream);
 	ctx->build_ms = ev.elapsed_ms();
 	ctx->scene_set = false;
@@ -599,6 +601,8 @@ int prt_b200_set_option(prt_b200_ctx *ctx, const char *key, int64_t v) {
 			ctx->build_sah = v != 0;
 		} else if (k == "collapse_cost") {
 			ctx->collapse_cost = v != 0;
+		} else if (k == "build_small") {
+			ctx->build_small = v != 0;
 		} else if (k == "host_direct") {
 			ctx->host_direct = v != 0;
 		} else if (k == "serve_persistent") {
@@ -635,6 +639,8 @@ int prt_b200_get_stat(prt_b200_ctx *ctx, const char *key, double *value) {
 			*value = ctx->build_ms;
 		else if (k == "build_sah")
 			*value = ctx->last_build_sah ? 1.0 : 0.0;
+		else if (k == "build_small")
+			*value = ctx->last_build_small ? 1.0 : 0.0;
 		else if (k == "in_place")
 			*value = ctx->last_in_place ? 1.0 : 0.0;
 		else if (k == "node_bytes")

@@ -83,9 +83,11 @@ struct prt_b200_ctx {
 	bool build_compressed = true;
 	bool build_sah = true;       // set_tris builds binned-SAH trees ("build_sah"; 0 = LBVH)
 	bool collapse_cost = true;   // cost-optimal 8-wide collapse ("collapse_cost")
+	bool build_small = true;     // one block builds scenes of <= 4,096 tris ("build_small")
 	bool host_direct = true;     // host-buffer calls traverse in place when they can
 	bool last_in_place = false;  // the last host-buffer call did
-	bool last_build_sah = false; // the scene's tree is an SAH tree
+	bool last_build_sah = false; // the scene's tree is from the quality build
+	bool last_build_small = false; // ... made by the one-block build
 	double build_ms = 0.0;
 	unsigned long long visits[2] = {0, 0};
 

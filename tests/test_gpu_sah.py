@@ -27,7 +27,9 @@ def _same(got, want):
 @pytest.fixture
 def sah(gpu_backend):
     gpu_backend.set_option("build_sah", 1)  # the default for set_tris
+    gpu_backend.set_option("build_small", 0)  # the binned-SAH builder at every size
     yield gpu_backend
+    gpu_backend.set_option("build_small", 1)
     gpu_backend.set_option("leaf_size", 1)
     gpu_backend.set_option("node_format", 0)
 
@@ -100,6 +102,7 @@ def test_equals_lbvh_with_fewer_visits(gpu_backend, scene):
     res = {}
     try:
         gpu_backend.set_option("count_visits", 1)
+        gpu_backend.set_option("build_small", 0)
         for sah in (0, 1):
             gpu_backend.set_option("build_sah", sah)
             gpu_backend.set_tris(tris)
@@ -108,6 +111,7 @@ def test_equals_lbvh_with_fewer_visits(gpu_backend, scene):
     finally:
         gpu_backend.set_option("count_visits", 0)
         gpu_backend.set_option("build_sah", 1)
+        gpu_backend.set_option("build_small", 1)
     assert res[0][0].tobytes() == res[1][0].tobytes()
     assert res[1][1] < res[0][1], (res[1][1], res[0][1])
 
