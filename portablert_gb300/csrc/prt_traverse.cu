@@ -124,11 +124,41 @@ __device__ __forceinline__ void ld_nc_256(const void *p, float4 &a, float4 &b) {
 	    : "l"(p));
 }
 
-template <bool REGULAR>
+// Three-input minimum and maximum (sm_100 and later; NaN operands ignored, as fminf and
+// fmaxf ignore them).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+	float r;
+	asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+	return r;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+	float r;
+	asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+	return r;
+}
+
+// regular_box with its two comparisons folded into one: tmax >= 0 and tmin <= tmax hold
+// exactly when max(tmin, 0) <= tmax, and the 0 joins the last axis' minimum.  Same
+// products, same answer (an unused slot's NaN box: max(NaN, 0) = 0, and 0 <= NaN fails);
+// one ALU instruction fewer per child, which the half-rate ALU pipe of FP32-node steps
+// turns into 1 % more rays (compressed nodes measured 1 % slower with it, so they keep
+// regular_box).
+__device__ __forceinline__ bool regular_box_folded(const RayC &r, float lx, float hx, float ly,
+                                                   float hy, float lz, float hz) {
+	const float t1 = (lx - r.ox) * r.fx, t2 = (hx - r.ox) * r.fx;
+	const float t3 = (ly - r.oy) * r.fy, t4 = (hy - r.oy) * r.fy;
+	const float t5 = (lz - r.oz) * r.fz, t6 = (hz - r.oz) * r.fz;
+	const float tmin = max3f(fminf(t1, t2), fminf(t3, t4), fmaxf(fminf(t5, t6), 0.0f));
+	const float tmax = min3f(fmaxf(t1, t2), fmaxf(t3, t4), fmaxf(t5, t6));
+	return tmin <= tmax;
+}
+
+template <bool REGULAR, bool FOLDED = false>
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
 	if (REGULAR)
-		return regular_box(r, lx, hx, ly, hy, lz, hz);
+		return FOLDED ? regular_box_folded(r, lx, hx, ly, hy, lz, hz)
+		              : regular_box(r, lx, hx, ly, hy, lz, hz);
 	return r.kind == 0 ? regular_box(r, lx, hx, ly, hy, lz, hz)
 	                   : conservative_box(r, lx, hx, ly, hy, lz, hz);
 }
@@ -195,7 +225,7 @@ __device__ __forceinline__ void test_child(const void *__restrict__ nodes, const
 		// conservative test would, so only the general pass checks the reference.
 		if (REGULAR || ref != kNone) {
 			inner = !ref_is_leaf(ref);
-			hit = box_test<REGULAR>(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+			hit = box_test<REGULAR, true>(r, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
 			// A node index, or a leaf's first triangle: both below 2^27, under the
 			// leaf flag and count bits.
 			child = ref & kIndexMask;
