@@ -3,8 +3,9 @@
 // Replaces, for small scenes, the chain of about 57 dependent launches of the binned-SAH
 // build (each level's kernels wait on global memory; at this size the build is latency,
 // not work) with one launch whose dependencies go through shared memory:
-//   1. centroid bounds and 30-bit Morton codes (as k_morton), a bitonic sort of
-//      (code, index) in shared memory;
+//   1. one pass over the triangles (boxes into shared memory, centroid bounds), 30-bit
+//      Morton codes (as k_morton makes them), a bitonic sort of (code, index) in shared
+//      memory;
 //   2. PLOC (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding
 //      Volume Hierarchy Construction", 2018): the clusters in Morton order each find
 //      the cluster within kRadius (3) positions whose union with it has the least surface
@@ -16,14 +17,15 @@
 //      instead of one pair at a time.  After kPlocRounds iterations (scenes whose
 //      clusters keep choosing one neighbour, such as exponentially spaced triangles)
 //      positions 2k and 2k + 1 merge regardless, which bounds the iterations and the
-//      depth by kPlocRounds + log2(n).  Each
-//      merge computes the new node's least-expected-cost record from its children's
-//      (merge_costs, the model of prt_collapse.cuh), so no bottom-up pass follows;
+//      depth by kPlocRounds + log2(n).  Each merge computes the new node's
+//      least-expected-cost record from its children's (merge_costs, the model of
+//      prt_collapse.cuh), so no bottom-up pass follows;
 //   3. the 8-wide collapse, level by level from shared-memory copies of the binary
 //      nodes' children, counts and cost records (or areas, for the largest-child-first
-//      collapse), positions from block scans: a node's inner children are consecutive
-//      in slot order and its leaf triangles contiguous, as k_collapse lays them out;
-//      the triangles are re-laid out in leaf order in the same pass (as k_relayout).
+//      collapse), eight lanes per frontier node (lane c writes child c), positions from
+//      block scans: a node's inner children are consecutive in slot order and its leaf
+//      triangles contiguous, as k_collapse lays them out; the triangles are re-laid out
+//      in leaf order in the same pass (as k_relayout).
 // The counters end as the multi-launch build leaves them (build_finish reads them).
 // No thread waits on another except at __syncthreads; every loop is bounded.
 #include <cfloat>
@@ -43,7 +45,8 @@ constexpr int kThreads = 1024;
 #endif
 constexpr int kRadius = PRT_PLOC_RADIUS; // PLOC's search radius in Morton order
 constexpr uint32_t kPlocRounds = 48; // PLOC iterations before neighbours pair regardless
-constexpr uint32_t kLeaf16 = 0x8000u; // 16-bit node references: leaf flag | triangle
+// 16-bit node references: a binary node's index, or the leaf flag | triangle index.
+constexpr uint32_t kLeaf16 = 0x8000u;
 
 // Shared memory (bytes).  PLOC: two cluster buffers, each six box arrays and one word
 // per cluster (16-bit reference | triangle count << 16); the nearest neighbours of an
@@ -447,7 +450,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 	__syncthreads();
 	const uint32_t c8 = tid & 7u;            // this lane's child
 	const uint32_t lane = tid & 31u;
-	const unsigned gmask = 0xFFu << (lane & 24u);
 	uint32_t n_items = 1, n_nodes = 1, n_placed = 0;
 	int level = 0;
 	for (;; ++level) {
@@ -611,7 +613,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 				ch.pad = 0u;
 				nodes[slot].c[c8] = ch;
 			}
-			(void)gmask;
 			n_nodes += total & 0xFFFFu;
 			next_items += total & 0xFFFFu;
 			n_placed += total >> 16;
