@@ -28,6 +28,7 @@
 //      in leaf order in the same pass (as k_relayout).
 // The counters end as the multi-launch build leaves them (build_finish reads them).
 // No thread waits on another except at __syncthreads; every loop is bounded.
+#include <atomic>
 #include <cfloat>
 
 #include "../../include/prt_b200.h"
@@ -638,14 +639,19 @@ uint32_t small_build_max() { return kSmallMax; }
 cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
                                BuildScratch &ws, SceneGPU &sc, uint32_t node_cap, uint32_t *ctr,
                                uint32_t *d_err, cudaStream_t st) {
-	static bool attr_set = false;
-	if (!attr_set) {
-		cudaError_t e = cudaFuncSetAttribute(k_build_small,
-		                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                                     (int)kSmemBytes);
+	// The shared-memory limit is a per-device attribute: set once per device.
+	static std::atomic<uint32_t> attr_set{0};
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess)
+		return e;
+	const uint32_t bit = (dev >= 0 && dev < 32) ? (1u << dev) : 0u;
+	if (!bit || !(attr_set.load() & bit)) {
+		e = cudaFuncSetAttribute(k_build_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                         (int)kSmemBytes);
 		if (e != cudaSuccess)
 			return e;
-		attr_set = true;
+		attr_set.fetch_or(bit);
 	}
 	k_build_small<<<1, kThreads, kSmemBytes, st>>>(
 	    d_tris, n, leaf_size, use_cost ? 1 : 0, ws.ibox.as<float4>(), ws.left.as<uint32_t>(),

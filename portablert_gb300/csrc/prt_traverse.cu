@@ -45,6 +45,7 @@
 // Algorithmic bytes per ray: 24 (ray) + R (record) + node bytes visited + 48 per
 // triangle tested; the counting variant (COUNT) measures the visits.
 #include <algorithm>
+#include <mutex>
 
 #include "../../include/prt_b200.h"
 #include "prt_camera.cuh"
@@ -156,11 +157,10 @@ __device__ __forceinline__ bool regular_box_folded(const RayC &r, float lx, floa
 template <bool REGULAR, bool FOLDED = false>
 __device__ __forceinline__ bool box_test(const RayC &r, float lx, float hx, float ly, float hy,
                                          float lz, float hz) {
-	if (REGULAR)
+	if (REGULAR || r.kind == 0)
 		return FOLDED ? regular_box_folded(r, lx, hx, ly, hy, lz, hz)
 		              : regular_box(r, lx, hx, ly, hy, lz, hz);
-	return r.kind == 0 ? regular_box(r, lx, hx, ly, hy, lz, hz)
-	                   : conservative_box(r, lx, hx, ly, hy, lz, hz);
+	return conservative_box(r, lx, hx, ly, hy, lz, hz);
 }
 
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int k) { return (w >> (8 * k)) & 0xFFu; }
@@ -739,25 +739,40 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 	}
 }
 
-// Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each.
+// Resident blocks per SM for `warps` warps of `warp_bytes` shared memory each, on the
+// current device.  The kernel's dynamic shared-memory limit is a per-device attribute
+// that only grows (under a lock), so a launch that another thread sized earlier still
+// fits when this one needs less.
+constexpr int kCachedDevices = 16;
 template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 int blocks_per_sm(int warps, uint32_t warp_bytes) {
-	static int cached_warps = -1;
-	static uint32_t cached_bytes = 0;
-	static int cached = 0;
-	if (cached_warps != warps || cached_bytes != warp_bytes) {
-		const size_t smem = (size_t)warp_bytes * warps;
-		cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>,
-		                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-		                     (int)smem);
+	struct Cache {
+		int warps = -1;
+		uint32_t bytes = 0;
+		int blocks = 1;
+		size_t limit = 0;
+	};
+	static std::mutex mu;
+	static Cache cache[kCachedDevices];
+	int dev = 0;
+	cudaGetDevice(&dev);
+	const size_t smem = (size_t)warp_bytes * warps;
+	std::lock_guard<std::mutex> lk(mu);
+	Cache uncached;
+	Cache &c = (dev >= 0 && dev < kCachedDevices) ? cache[dev] : uncached;
+	if (smem > c.limit &&
+	    cudaFuncSetAttribute(k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>,
+	                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess)
+		c.limit = smem;
+	if (c.warps != warps || c.bytes != warp_bytes) {
 		int b = 0;
 		cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_trace8<FMT, COUNT, LEAF1, BOUNDED, PASS>,
 		                                              32 * warps, smem);
-		cached = b > 0 ? b : 1;
-		cached_warps = warps;
-		cached_bytes = warp_bytes;
+		c.blocks = b > 0 ? b : 1;
+		c.warps = warps;
+		c.bytes = warp_bytes;
 	}
-	return cached;
+	return c.blocks;
 }
 
 template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
