@@ -79,6 +79,8 @@ struct TravArgs {
 	uint32_t warp_bytes;     // shared memory per warp
 	uint32_t max_leaf;       // most triangles in a leaf of any scene of the launch
 	uint32_t max_batches;    // batches per warp before it exits (0 = no bound)
+	uint32_t batch;          // rays a warp takes at a time: 32, or 16 / 8 for one small
+	                         // run (more warps busy, shorter chains per warp)
 	uint32_t *counter;
 	uint32_t *deferred;      // [0] batches the regular pass left to the general one,
 	                         // [1] the deferred pass's batch counter
@@ -557,11 +559,12 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			}
 		} else {
 			if (lane == 0)
-				base = atomicAdd(PASS == 2 ? a.deferred + 1 : a.counter, 32u);
+				base = atomicAdd(PASS == 2 ? a.deferred + 1 : a.counter, a.batch);
 			base = __shfl_sync(0xFFFFFFFFu, base, 0);
 			if (base >= a.n_virtual)
 				break;
-			// The run these 32 rays belong to (runs are padded to whole warps).
+			// The run these rays belong to (runs are padded to whole warps of 32, and
+			// a batch of fewer rays never straddles one).
 			uint32_t si = 0;
 			if (a.n_segs) {
 				if (lane == 0) {
@@ -585,7 +588,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		const uint32_t run_rays = S.seg.n_rays;
 		if (local >= run_rays)
 			continue; // padding of the run
-		const uint32_t nb = min(32u, run_rays - local);
+		const uint32_t nb = min(PASS == 3 ? 32u : a.batch, run_rays - local);
 		const SceneDesc sd = (PASS == 3 || a.n_segs) ? a.scenes[S.seg.scene] : a.scene0;
 		const float4 *__restrict__ tri4 = sd.tri4;
 
@@ -691,7 +694,7 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		uint8_t *dst = S.seg.out + (size_t)local * rec;
 		const uint32_t bytes = nb * rec;
 		const uint32_t mode = S.seg.store_mode;
-		if (mode == 0 && nb == 32u) {
+		if (mode == 0 && (bytes & 15u) == 0u) { // local is a multiple of 8: 16-byte aligned
 			uint4 *d4 = reinterpret_cast<uint4 *>(dst);
 			const uint4 *s4 = reinterpret_cast<const uint4 *>(stage);
 			for (uint32_t k = lane; k < bytes / 16u; k += 32u)
@@ -778,7 +781,7 @@ int blocks_per_sm(int warps, uint32_t warp_bytes) {
 template <int FMT, bool COUNT, bool LEAF1, bool BOUNDED, int PASS>
 void launch_t(const TravArgs &a, int warps, int sm_count, cudaStream_t st) {
 	const int bps = blocks_per_sm<FMT, COUNT, LEAF1, BOUNDED, PASS>(warps, a.warp_bytes);
-	const uint64_t batches = (a.n_virtual + 31ull) / 32ull;
+	const uint64_t batches = (a.n_virtual + a.batch - 1ull) / a.batch;
 	// Unbounded warps: at most one block per resident slot (persistent).  Bounded: enough
 	// blocks that every batch has a warp even if each warp takes its maximum.
 	const uint64_t per_block = (uint64_t)warps * (BOUNDED ? a.max_batches : 1u);
@@ -822,6 +825,17 @@ void size_smem(TravArgs &a, uint32_t depth, int leaf_size) {
 	a.max_leaf = (uint32_t)std::max(leaf_size, 1);
 	a.max_batches = 0;
 	a.warp_bytes = (warp_smem_bytes(a.pool_cap, a.queue_cap) + 15u) & ~15u;
+}
+
+// Rays per warp batch for one run of m rays: 32 when the launch holds at least two
+// batches for every resident warp (about 36 per SM), else 16, else 8: a small query
+// then spreads over all warps instead of leaving most of them idle while a few walk 32
+// rays each (bounded waves keep 32: their batch count per warp is the caller's).
+uint32_t batch_rays(uint64_t m, int sm_count, uint32_t max_batches) {
+	const uint64_t wave = (uint64_t)std::max(sm_count, 1) * 36u * 32u;
+	if (max_batches > 0 || m >= 2 * wave)
+		return 32;
+	return m >= wave ? 16 : 8;
 }
 
 int warps_for(const TravConfig &cfg) {
@@ -893,6 +907,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.n_nodes = sc.n_nodes;
 		size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : sc.depth, sc.leaf_size);
 		a.max_batches = cfg.max_batches;
+		a.batch = batch_rays(m, sm_count, cfg.max_batches);
 		a.counter = d_work;
 		a.deferred = d_work + 2;
 		a.err = d_err;
@@ -925,6 +940,7 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
 	a.n_nodes = n_nodes;
 	size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : depth, leaf_size);
 	a.max_batches = cfg.max_batches;
+	a.batch = 32; // runs are padded to whole warps of 32
 	a.counter = d_work;
 	a.deferred = d_work + 2;
 	a.err = d_err;
@@ -953,6 +969,7 @@ cudaError_t launch_serving(const SceneDesc *d_scenes, const ServeQueues &q, uint
 	a.serve = q;
 	a.n_nodes = n_nodes;
 	size_smem(a, depth, leaf_size);
+	a.batch = 32; // one ticket = 32 rays
 	a.err = d_err;
 	// Every resident slot: the warps poll for work, none waits for another, so the
 	// launch needs no co-residency (blocks that do not fit start as others leave).
