@@ -144,7 +144,7 @@ int launch_query(prt_b200_batch *b, Slot &s, const std::vector<prt::SegDesc> &se
 	uint32_t *w = s.work.as<uint32_t>();
 	B_TRY(ctx, prt::launch_nearest_hits_segments(
 	               tab, s.segs.as<prt::SegDesc>(), (uint32_t)segs.size(), n_virtual,
-	               b->arena.depth, b->arena.leaf_size, n_nodes, cfg, w,
+	               b->arena.depth, b->arena.leaf_size, n_nodes, b->arena.dead, cfg, w,
 	               reinterpret_cast<unsigned long long *>(w + 4), w + 1, st, ctx->sms));
 	return PRT_OK;
 }

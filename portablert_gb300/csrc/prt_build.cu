@@ -983,9 +983,12 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 		BUILD_TRY(ws.cost.reserve(sizeof(CostNode) * ni));
 	BUILD_TRY(sc.tri4.reserve(48 * nn));
 	BUILD_TRY(sc.inv.reserve(4 * nn));
-	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * (size_t)plan.node_cap));
+	// One node past the capacity: the empty node the traversal pads partial steps with.
+	BUILD_TRY(sc.nodes.reserve(sizeof(Node8) * ((size_t)plan.node_cap + 1)));
 	if (compressed)
-		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * (size_t)plan.node_cap));
+		BUILD_TRY(sc.cnodes.reserve(sizeof(CNode8) * ((size_t)plan.node_cap + 1)));
+	// Work items hold 27-bit node indices; a tree's nodes stay below n - 1 < 2^27 - 1.
+	sc.dead = std::min<uint32_t>(plan.node_cap, kIndexMask);
 	if (!ws.h_counters)
 		BUILD_TRY(cudaMallocHost(&ws.h_counters, 4 * kCtrWords));
 	if (plan.small)
@@ -1059,6 +1062,20 @@ static int lbvh_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch
 	return PRT_OK;
 }
 
+// The empty node at index sc.dead (node_cap, past every built node): eight NaN boxes with no reference (no slab test
+// passes them, and the general test skips a child without reference); compressed, a
+// node with no inner mask and no leaf counts.  Queued on the build's stream, so a batch
+// graph captures it with the build.
+static cudaError_t write_dead_node(const BuildPlan &plan, SceneGPU &sc, cudaStream_t st) {
+	cudaError_t e = cudaMemsetAsync(static_cast<char *>(sc.nodes.p) +
+	                                    sizeof(Node8) * (size_t)sc.dead,
+	                                0xFF, sizeof(Node8), st);
+	if (e == cudaSuccess && plan.compressed)
+		e = cudaMemsetAsync(static_cast<char *>(sc.cnodes.p) + sizeof(CNode8) * (size_t)sc.dead,
+		                    0, sizeof(CNode8), st);
+	return e;
+}
+
 int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, BuildScratch &ws,
                   cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg) {
 	const uint32_t S = plan.S, n = plan.n, n_int = plan.n_int;
@@ -1066,6 +1083,7 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 		msg = "the SAH build reads its level counters on the host";
 		return PRT_ERR_ARG;
 	}
+	BUILD_TRY(write_dead_node(plan, sc, st));
 	if (plan.small) {
 		// One block: PLOC, collapse and re-layout in one launch; the compression reads the
 		// node count on the device, so the host waits once, at the end.

@@ -60,10 +60,12 @@ struct SceneGPU {
 	int leaf_size = 1;
 	bool has_cnodes = false;
 	bool built_small = false; // the last build was the one-block build (prt_build_small.cu)
+	uint32_t dead = 0;   // a node of eight empty children (past every built node): the
+	                     // traversal pads a partial step with it
 	DevBuf tri4;         // float4[3 n]
 	DevBuf inv;          // uint32[n]
-	DevBuf nodes;        // Node8[n_nodes]
-	DevBuf cnodes;       // CNode8[n_nodes]
+	DevBuf nodes;        // Node8[n_nodes], and the empty node at `dead`
+	DevBuf cnodes;       // CNode8[n_nodes], likewise
 	DevBuf tri_off;      // uint32[n_scenes + 1] (device copy)
 	std::vector<uint64_t> h_tri_off;
 	void release() {

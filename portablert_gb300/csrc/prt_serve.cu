@@ -300,7 +300,8 @@ cudaError_t launch_wave(prt_b200_server *s, Lane &L) {
 	                                : b->scenes_fp32.as<prt::SceneDesc>();
 	uint32_t *w = L.work.as<uint32_t>();
 	e = prt::launch_nearest_hits_segments(tab, L.segs.as<prt::SegDesc>(), k, nv, b->arena.depth,
-	                                      b->arena.leaf_size, b->arena.n_nodes, cfg, w,
+	                                      b->arena.leaf_size, b->arena.n_nodes, b->arena.dead,
+	                                      cfg, w,
 	                                      reinterpret_cast<unsigned long long *>(w + 4), w + 1,
 	                                      L.st, s->ctx->sms);
 	if (e != cudaSuccess)
@@ -531,8 +532,8 @@ cudaError_t p_launch(prt_b200_server *s) {
 	                                ? b->scenes_comp.as<prt::SceneDesc>()
 	                                : b->scenes_fp32.as<prt::SceneDesc>();
 	e = prt::launch_serving(tab, p_queues(s), b->arena.depth, b->arena.leaf_size,
-	                        b->arena.n_nodes, s->format, P.work.as<uint32_t>(), P.st,
-	                        s->ctx->sms);
+	                        b->arena.n_nodes, b->arena.dead, s->format, P.work.as<uint32_t>(),
+	                        P.st, s->ctx->sms);
 	if (e == cudaSuccess)
 		e = cudaEventRecord(P.ev, P.st);
 	if (e == cudaSuccess) {

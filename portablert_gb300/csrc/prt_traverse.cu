@@ -74,6 +74,8 @@ struct TravArgs {
 	SceneDesc scene0;
 	SegDesc seg0;
 	uint32_t n_nodes;        // largest node array (bounds the steps of a batch)
+	uint32_t dead;           // index of a node of eight empty children in every scene's
+	                         // node array (pads a step that has fewer than K items)
 	uint32_t pool_cap;       // entries of the pool (>= 256, it also holds the staged records)
 	uint32_t queue_cap;      // entries of the triangle queue
 	uint32_t warp_bytes;     // shared memory per warp
@@ -306,13 +308,22 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 			}
 			if (top == 0u)
 				break;
+			// Fewer than K items left: the empty node (slot 0's ray) fills the step, so
+			// every step takes K items and no group needs a "has an item" test.  A
+			// counting run keeps the test (it counts visits of real items only).
+			if (!COUNT && top < (uint32_t)kItems) {
+				if ((uint32_t)lane >= top && lane < kItems)
+					pool[lane] = a.dead;
+				top = kItems;
+				__syncwarp();
+			}
 		}
-		const uint32_t take = min(top, (uint32_t)kItems);
+		const uint32_t take = COUNT ? min(top, (uint32_t)kItems) : (uint32_t)kItems;
 		top -= take;
-		// Groups without an item this step repeat the first one (same loads, no branch)
-		// and drop what they find.
-		const bool work = (uint32_t)g < take;
-		const uint32_t item = pool[top + (work ? g : 0)];
+		// (Counting runs: groups without an item repeat the first one and drop what they
+		// find.)
+		const bool work = !COUNT || (uint32_t)g < take;
+		const uint32_t item = pool[top + (COUNT ? (work ? g : 0) : g)];
 		__syncwarp(); // the pops above are read before the pushes below overwrite them
 		const uint32_t slot = item >> kIndexBits, node = item & kIndexMask;
 		const RayC r = slot_ray(S, slot);
@@ -905,6 +916,7 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 		a.seg0.store_mode = store_mode_for(a.seg0.out);
 		a.seg0.pad = 0;
 		a.n_nodes = sc.n_nodes;
+		a.dead = sc.dead;
 		size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : sc.depth, sc.leaf_size);
 		a.max_batches = cfg.max_batches;
 		a.batch = batch_rays(m, sm_count, cfg.max_batches);
@@ -922,9 +934,9 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDesc *d_segs,
                                          uint32_t n_segs, unsigned long long n_virtual,
                                          uint32_t depth, int leaf_size, uint32_t n_nodes,
-                                         const TravConfig &cfg, uint32_t *d_work,
-                                         unsigned long long *d_visits, uint32_t *d_err,
-                                         cudaStream_t st, int sm_count) {
+                                         uint32_t dead, const TravConfig &cfg,
+                                         uint32_t *d_work, unsigned long long *d_visits,
+                                         uint32_t *d_err, cudaStream_t st, int sm_count) {
 	if (cfg.count)
 		cudaMemsetAsync(d_visits, 0, 2 * sizeof(unsigned long long), st);
 	if (n_segs == 0 || n_virtual == 0)
@@ -938,6 +950,7 @@ cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDes
 	a.n_segs = n_segs;
 	a.n_virtual = (uint32_t)n_virtual;
 	a.n_nodes = n_nodes;
+	a.dead = dead;
 	size_smem(a, cfg.pool_depth ? (uint32_t)cfg.pool_depth : depth, leaf_size);
 	a.max_batches = cfg.max_batches;
 	a.batch = 32; // runs are padded to whole warps of 32
@@ -961,13 +974,14 @@ void launch_serving_t(const TravArgs &a, int sm_count, cudaStream_t st) {
 } // namespace
 
 cudaError_t launch_serving(const SceneDesc *d_scenes, const ServeQueues &q, uint32_t depth,
-                           int leaf_size, uint32_t n_nodes, int format, uint32_t *d_err,
-                           cudaStream_t st, int sm_count) {
+                           int leaf_size, uint32_t n_nodes, uint32_t dead, int format,
+                           uint32_t *d_err, cudaStream_t st, int sm_count) {
 	TravArgs a;
 	memset(&a, 0, sizeof a);
 	a.scenes = d_scenes;
 	a.serve = q;
 	a.n_nodes = n_nodes;
+	a.dead = dead;
 	size_smem(a, depth, leaf_size);
 	a.batch = 32; // one ticket = 32 rays
 	a.err = d_err;

@@ -102,19 +102,21 @@ cudaError_t launch_nearest_hits(const SceneGPU &sc, const float *d_rays, uint64_
 // its own output layout.  d_scenes / d_segs: device copies of the tables (segments
 // sorted by vbegin); n_virtual: the padded ray count (end of the last run).  depth and
 // leaf_size: the largest over the scenes (they size the shared-memory pool and queue);
-// n_nodes: the largest node array (bounds the steps of a batch).  d_work as above.
+// n_nodes: the largest node array (bounds the steps of a batch); dead: the index of the
+// empty node (SceneGPU::dead) in the node array every scene's `nodes` points into.
+// d_work as above.
 cudaError_t launch_nearest_hits_segments(const SceneDesc *d_scenes, const SegDesc *d_segs,
                                          uint32_t n_segs, unsigned long long n_virtual,
                                          uint32_t depth, int leaf_size, uint32_t n_nodes,
-                                         const TravConfig &cfg, uint32_t *d_work,
-                                         unsigned long long *d_visits, uint32_t *d_err,
-                                         cudaStream_t st, int sm_count);
+                                         uint32_t dead, const TravConfig &cfg,
+                                         uint32_t *d_work, unsigned long long *d_visits,
+                                         uint32_t *d_err, cudaStream_t st, int sm_count);
 
 // Queues one serving launch over the queues `q` on `st` (resident warps only; it runs
 // until it is stopped or idle).  Scenes as for launch_nearest_hits_segments.
 cudaError_t launch_serving(const SceneDesc *d_scenes, const ServeQueues &q, uint32_t depth,
-                           int leaf_size, uint32_t n_nodes, int format, uint32_t *d_err,
-                           cudaStream_t st, int sm_count);
+                           int leaf_size, uint32_t n_nodes, uint32_t dead, int format,
+                           uint32_t *d_err, cudaStream_t st, int sm_count);
 
 // Store mode for an output pointer (16-byte, 4-byte or byte stores).
 inline uint32_t store_mode_for(const void *p) {
