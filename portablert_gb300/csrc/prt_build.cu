@@ -726,7 +726,7 @@ __global__ void k_relayout(const float *__restrict__ tris, const uint32_t *__res
 	inv[g] = i;
 	const float *t = tris + 9 * (size_t)g;
 	tri4[3 * (size_t)i] = make_float4(t[0], t[1], t[2], __uint_as_float(pid));
-	tri4[3 * (size_t)i + 1] = make_float4(t[3], t[4], t[5], 0.0f);
+	tri4[3 * (size_t)i + 1] = make_float4(t[3], t[4], t[5], tri_finite(t) ? 0.0f : 1.0f);
 	tri4[3 * (size_t)i + 2] = make_float4(t[6], t[7], t[8], 0.0f);
 }
 

@@ -580,17 +580,18 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
 								for (int q = 0; q < 9; ++q)
 									t[q] = __ldg(tris + 9 * (size_t)p + q);
-								if (y & kLeaf16) {
-									bool fin = true;
+								bool fin = true;
 #pragma unroll
-									for (int q = 0; q < 9; ++q)
-										fin = fin && isfinite(t[q]);
+								for (int q = 0; q < 9; ++q)
+									fin = fin && isfinite(t[q]);
+								if (y & kLeaf16) {
 									const Box tb9 = tri_box(t, fin);
 									lo = box_lo(tb9);
 									hi = box_hi(tb9);
 								}
+								// As k_relayout: the second word's w flags a non-finite vertex.
 								tri4[3 * (size_t)dst] = make_float4(t[0], t[1], t[2], __uint_as_float(p));
-								tri4[3 * (size_t)dst + 1] = make_float4(t[3], t[4], t[5], 0.0f);
+								tri4[3 * (size_t)dst + 1] = make_float4(t[3], t[4], t[5], fin ? 0.0f : 1.0f);
 								tri4[3 * (size_t)dst + 2] = make_float4(t[6], t[7], t[8], 0.0f);
 								inv[p] = dst;
 								++dst;

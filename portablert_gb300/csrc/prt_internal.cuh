@@ -270,17 +270,44 @@ __device__ __forceinline__ void best_init(Best &b) {
 	b.pid = kNone;
 }
 
+// The box half of tri_test for a ray with finite origin, direction and reciprocals (kind
+// 0) and a triangle whose nine coordinates are finite (its record's flag word is 0):
+// then no value is NaN, the select min/max of the reference agree with fminf / fmaxf
+// (three-input where they nest; a zero's sign can differ, and no comparison sees it),
+// and the answer is ref_slab's with fewer instructions.
+__device__ __forceinline__ bool tri_box_finite(const RayC &r, const float4 a, const float4 b,
+                                               const float4 c) {
+	const float lx = fminf(a.x, fminf(b.x, c.x)), ly = fminf(a.y, fminf(b.y, c.y)),
+	            lz = fminf(a.z, fminf(b.z, c.z));
+	const float hx = fmaxf(a.x, fmaxf(b.x, c.x)), hy = fmaxf(a.y, fmaxf(b.y, c.y)),
+	            hz = fmaxf(a.z, fmaxf(b.z, c.z));
+	return regular_box(r, lx, hx, ly, hy, lz, hz);
+}
+
+// A triangle record's flag word (the second float4's w): 0 when every coordinate is
+// finite, 1 otherwise.
+__device__ __forceinline__ bool tri_record_finite(const float4 &b) { return b.w == 0.0f; }
+
 // Exact per-triangle test: the reference slab test on the triangle's own bounding
 // box (make_aabb, bvh.hpp:28-37, select semantics) and then Moller-Trumbore.  True
 // when the reference would accept the triangle (its t may still be +inf or NaN, which
 // the reference never records).
+// finite: the ray is of kind 0 and the triangle's record flags no non-finite coordinate
+// (tri_box_finite then decides the box test, with the same answer).
 __device__ __forceinline__ bool tri_test(const RayC &r, const float4 a, const float4 b,
-                                         const float4 c, float &t, float &u, float &v) {
-	float lx = rmin(a.x, rmin(b.x, c.x)), ly = rmin(a.y, rmin(b.y, c.y)),
-	      lz = rmin(a.z, rmin(b.z, c.z));
-	float hx = rmax(a.x, rmax(b.x, c.x)), hy = rmax(a.y, rmax(b.y, c.y)),
-	      hz = rmax(a.z, rmax(b.z, c.z));
-	if (!ref_slab(r, lx, ly, lz, hx, hy, hz))
+                                         const float4 c, float &t, float &u, float &v,
+                                         bool finite = false) {
+	bool pass;
+	if (finite) {
+		pass = tri_box_finite(r, a, b, c);
+	} else {
+		float lx = rmin(a.x, rmin(b.x, c.x)), ly = rmin(a.y, rmin(b.y, c.y)),
+		      lz = rmin(a.z, rmin(b.z, c.z));
+		float hx = rmax(a.x, rmax(b.x, c.x)), hy = rmax(a.y, rmax(b.y, c.y)),
+		      hz = rmax(a.z, rmax(b.z, c.z));
+		pass = ref_slab(r, lx, ly, lz, hx, hy, hz);
+	}
+	if (!pass)
 		return false;
 	return ref_mt(r, a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, t, u, v);
 }

@@ -205,7 +205,8 @@ __device__ __forceinline__ void test_queued(const float4 *__restrict__ tri4, War
 		const float4 *p = tri4 + 3 * (size_t)(e & kIndexMask);
 		const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
 		float t, u, v;
-		if (tri_test(r, A, B, C, t, u, v) && t < INFINITY)
+		// Finite ray and triangle (nearly always): the box test with plain min/max.
+		if (tri_test(r, A, B, C, t, u, v, r.kind == 0 && tri_record_finite(B)) && t < INFINITY)
 			atomicMin(&S.key[slot], hit_key(t, __float_as_uint(A.w)));
 		if (COUNT)
 			++n_tests;
@@ -671,8 +672,9 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			if (key != kNoHit) {
 				const uint32_t pid = (uint32_t)key;
 				const float4 *p = tri4 + 3 * (size_t)__ldg(&sd.inv[pid]);
+				const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
 				float t, u, v;
-				if (tri_test(r, __ldg(p), __ldg(p + 1), __ldg(p + 2), t, u, v)) {
+				if (tri_test(r, A, B, C, t, u, v, r.kind == 0 && tri_record_finite(B))) {
 					best.t = t;
 					best.u = u;
 					best.v = v;
