@@ -33,9 +33,10 @@
 //    takes its batches from device queues that the host extends while it runs
 //    (claim_batch) and picks the plain or the general test per batch.
 //  * When 32 triangles are queued, the 32 lanes test one each with the exact reference
-//    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin.
-//  * When the pool and the queue are empty the warp recomputes each slot's winning
-//    triangle (identical arithmetic, identical t, u, v), writes the 32 records in the
+//    test and fold (t, primitive id) into the slot's 64-bit key with a shared atomicMin;
+//    with FP32 nodes the lane whose key the slot kept records its u, v (and a zero t's
+//    sign) beside it, with compressed nodes the winner is tested again at the end.
+//  * When the pool and the queue are empty the warp writes the 32 records in the
 //    caller's HitReg<Tags...> layout to shared memory and stores them as 16-byte words.
 //  * The pool holds at most 7 K (D - 1) + K items for K = 8 items per step and a tree of
 //    depth D (each step's pushes leave at most 7 K items behind per level); it is sized
@@ -101,13 +102,18 @@ struct alignas(16) WarpFixed {
 	float4 ro[32];              // origin and kind (int bits) per slot
 	float4 rf[32];              // reciprocals per slot
 	float4 rd[32];              // direction per slot
+	// rf[s].w and rd[s].w: u and v of slot s's winning hit (its key holds t exactly, up
+	// to the sign of a zero, which bit s of negzero keeps); no array of their own, so
+	// shared memory does not grow (a deep tree's pool already brings nine blocks close
+	// to the SM's limit, and the L1 cache gets what shared memory leaves).
 	SegDesc seg;                // the run the current 32 rays belong to
 	uint32_t batches;           // batches this warp has taken (kept here, not in a register)
 	// Serving launches: tickets past the published end per queue, and the queue whose
 	// run `seg` holds (kept here, not in registers).
 	uint32_t held[kServeQueues];
 	uint32_t cached_q;
-	uint32_t pad_[(16 - (4 + 4 * kServeQueues + 4) % 16) % 16 / 4];
+	uint32_t negzero; // bit s: slot s's winning t is -0 (read only when its key's t is 0)
+	uint32_t pad_[(16 - (4 + 4 * kServeQueues + 4 + 4) % 16) % 16 / 4];
 };
 static_assert(sizeof(WarpFixed) % 16 == 0, "queue and pool must start 16-byte aligned");
 
@@ -193,11 +199,15 @@ __device__ __forceinline__ RayC slot_ray(const WarpFixed &S, uint32_t s) {
 	return r;
 }
 
-// Tests queue entries [lo, lo + n) (n <= 32), one per lane.
-template <bool COUNT>
+// Tests queue entries [lo, lo + n) (n <= 32), one per lane.  KEEP: the lane whose hit a
+// slot keeps also records its u, v (and the sign of a zero t) for the records.
+template <bool COUNT, bool KEEP>
 __device__ __forceinline__ void test_queued(const float4 *__restrict__ tri4, WarpFixed &S,
                                             const uint32_t *queue, uint32_t lo, uint32_t n,
                                             int lane, uint32_t &n_tests) {
+	unsigned long long mykey = kNoHit;
+	uint32_t my_slot = 0;
+	float mt = 0.0f, mu = 0.0f, mv = 0.0f;
 	if ((uint32_t)lane < n) {
 		const uint32_t e = queue[lo + lane];
 		const uint32_t slot = e >> kIndexBits;
@@ -206,10 +216,31 @@ __device__ __forceinline__ void test_queued(const float4 *__restrict__ tri4, War
 		const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
 		float t, u, v;
 		// Finite ray and triangle (nearly always): the box test with plain min/max.
-		if (tri_test(r, A, B, C, t, u, v, r.kind == 0 && tri_record_finite(B)) && t < INFINITY)
-			atomicMin(&S.key[slot], hit_key(t, __float_as_uint(A.w)));
+		if (tri_test(r, A, B, C, t, u, v, r.kind == 0 && tri_record_finite(B)) && t < INFINITY) {
+			mykey = hit_key(t, __float_as_uint(A.w));
+			atomicMin(&S.key[slot], mykey);
+			my_slot = slot;
+			mt = t;
+			mu = u;
+			mv = v;
+		}
 		if (COUNT)
 			++n_tests;
+	}
+	// The lane whose key the slot kept (keys are unique: they hold the primitive id)
+	// records its u and v, so the records need no second test of the winner.
+	if (!KEEP)
+		return;
+	__syncwarp();
+	if (mykey != kNoHit && S.key[my_slot] == mykey) {
+		S.rf[my_slot].w = mu;
+		S.rd[my_slot].w = mv;
+		if (mt == 0.0f) { // the key holds +0 for both zeros
+			if (signbit(mt))
+				atomicOr(&S.negzero, 1u << my_slot);
+			else
+				atomicAnd(&S.negzero, ~(1u << my_slot));
+		}
 	}
 }
 
@@ -416,14 +447,14 @@ __device__ __forceinline__ void trace_batch(const TravArgs &a, WarpFixed &S, uin
 		__syncwarp();
 		while (q >= 32u) {
 			q -= 32u;
-			test_queued<COUNT>(tri4, S, queue, q, 32u, lane, n_tests);
+			test_queued<COUNT, FMT == PRT_NODES_FP32>(tri4, S, queue, q, 32u, lane, n_tests);
 			__syncwarp();
 		}
 	}
 	while (q > 0u) {
 		const uint32_t n = min(q, 32u);
 		q -= n;
-		test_queued<COUNT>(tri4, S, queue, q, n, lane, n_tests);
+		test_queued<COUNT, FMT == PRT_NODES_FP32>(tri4, S, queue, q, n, lane, n_tests);
 		__syncwarp();
 	}
 }
@@ -655,8 +686,8 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 		}
 		__syncwarp();
 
-		// Finalise: recompute the winning triangle of each slot and stage the record in
-		// the run's HitReg<Tags...> layout.
+		// Finalise: stage each slot's record (its winner's t, u, v as its test found them)
+		// in the run's HitReg<Tags...> layout.
 		uint32_t *stage = pool;
 		const uint32_t rec = S.seg.rec_size, fmask = S.seg.mask;
 		const uint32_t rw = rec >> 2;
@@ -669,7 +700,14 @@ __global__ void __launch_bounds__(32 * kWarpsPerBlock, FMT == PRT_NODES_FP32
 			Best best;
 			best_init(best);
 			const unsigned long long key = S.key[lane];
-			if (key != kNoHit) {
+			if (key != kNoHit && FMT == PRT_NODES_FP32) {
+				const float tk = ord2f((uint32_t)(key >> 32));
+				best.t = tk != 0.0f ? tk : (((S.negzero >> lane) & 1u) ? -0.0f : 0.0f);
+				best.u = S.rf[lane].w;
+				best.v = S.rd[lane].w;
+				best.pid = (uint32_t)key;
+			} else if (key != kNoHit) {
+				// Compressed nodes (measured 1 % faster this way): the winner's test again.
 				const uint32_t pid = (uint32_t)key;
 				const float4 *p = tri4 + 3 * (size_t)__ldg(&sd.inv[pid]);
 				const float4 A = __ldg(p), B = __ldg(p + 1), C = __ldg(p + 2);
