@@ -314,8 +314,9 @@ __device__ __forceinline__ bool tri_test(const RayC &r, const float4 a, const fl
 
 // The closest hit as one 64-bit key: order-preserving bits of t above the primitive
 // id, so the minimum key is the smallest t and, among equal t, the smallest id (ties in
-// t go to the smaller id).  -0 and +0 compare equal as floats, so both map to +0's key;
-// the hit itself is recomputed from the winning id.  kNoHit: nothing recorded.
+// t go to the smaller id).  -0 and +0 compare equal as floats, so both map to +0's key
+// (the traversal keeps the winner's own zero sign, u and v beside the key, or tests the
+// winner again).  kNoHit: nothing recorded.
 constexpr unsigned long long kNoHit = ~0ull;
 
 __device__ __forceinline__ unsigned long long hit_key(float t, uint32_t pid) {

@@ -11,7 +11,8 @@
 // visit order changes the answer; ties in t go to the smaller primitive id.
 //
 // Execution: one warp = 8 groups of 4 lanes; all state for 32 rays is in shared memory.
-//  * A warp takes 32 consecutive rays from a global counter ("slots"): origin,
+//  * A warp takes up to 32 consecutive rays from a global counter ("slots": 32 per
+//    batch, or 8 or 16 when one small run would leave most warps idle): origin,
 //    direction, reciprocal and best-hit key per slot live in shared memory.
 //  * Work items (slot, node) sit in a warp-local LIFO pool.  Each step every group
 //    pops one item and each of its 4 lanes loads and slab-tests 2 of the node's 8
