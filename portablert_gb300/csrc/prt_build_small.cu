@@ -3,29 +3,32 @@
 // Replaces, for small scenes, the chain of about 57 dependent launches of the binned-SAH
 // build (each level's kernels wait on global memory; at this size the build is latency,
 // not work) with one launch whose dependencies go through shared memory:
-//   1. one pass over the triangles (boxes into shared memory, centroid bounds), 30-bit
-//      Morton codes (as k_morton makes them), a bitonic sort of (code, index) in shared
-//      memory;
+//   1. one pass over the triangles (boxes into shared memory and to the leaf-box array,
+//      centroid bounds), 30-bit Morton codes (as k_morton makes them), a bitonic sort of
+//      (code, index) in shared memory;
 //   2. PLOC (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding
 //      Volume Hierarchy Construction", 2018): the clusters in Morton order each find
 //      the cluster within kRadius (3) positions whose union with it has the least surface
 //      area; mutual nearest neighbours merge into a binary node; the survivors are
-//      compacted in order; repeated until one cluster is left.  Candidates are ordered
-//      by (area, distance in Morton order, parity of the lower position, lower
-//      position): a total order on pairs, so the least pair of an iteration is mutual
-//      and every iteration merges at least one; equal clusters pair up as (2k, 2k + 1)
-//      instead of one pair at a time.  After kPlocRounds iterations (scenes whose
-//      clusters keep choosing one neighbour, such as exponentially spaced triangles)
-//      positions 2k and 2k + 1 merge regardless, which bounds the iterations and the
-//      depth by kPlocRounds + log2(n).  Each merge computes the new node's
-//      least-expected-cost record from its children's (merge_costs, the model of
-//      prt_collapse.cuh), so no bottom-up pass follows;
+//      compacted in order (staged in free rows); repeated until one cluster is left.
+//      Candidates are ordered by (area, distance in Morton order, parity of the lower
+//      position, lower position): a total order on pairs, so the least pair of an
+//      iteration is mutual and every iteration merges at least one; equal clusters pair
+//      up as (2k, 2k + 1) instead of one pair at a time.  After kPlocRounds iterations
+//      (scenes whose clusters keep choosing one neighbour, such as exponentially spaced
+//      triangles) positions 2k and 2k + 1 merge regardless, which bounds the iterations
+//      and the depth by kPlocRounds + log2(n).  An iteration's merges are numbered in
+//      position order (a block scan) and dealt out one per thread; each computes the new
+//      node's least-expected-cost record from its children's (merge_costs, the model of
+//      prt_collapse.cuh), kept in shared memory, so no bottom-up pass follows;
 //   3. the 8-wide collapse, level by level from shared-memory copies of the binary
 //      nodes' children, counts and cost records (or areas, for the largest-child-first
 //      collapse), eight lanes per frontier node (lane c writes child c), positions from
 //      block scans: a node's inner children are consecutive in slot order and its leaf
-//      triangles contiguous, as k_collapse lays them out; the triangles are re-laid out
-//      in leaf order in the same pass (as k_relayout).
+//      triangles contiguous, as k_collapse lays them out; each leaf's triangles go to a
+//      shared-memory permutation;
+//   4. the triangles re-laid out in leaf order (as k_relayout): copied into shared
+//      memory with coalesced loads, then written out in permutation order.
 // The counters end as the multi-launch build leaves them (build_finish reads them).
 // No thread waits on another except at __syncthreads; every loop is bounded.
 #include <atomic>
@@ -48,24 +51,37 @@ constexpr int kRadius = PRT_PLOC_RADIUS; // PLOC's search radius in Morton order
 constexpr uint32_t kPlocRounds = 48; // PLOC iterations before neighbours pair regardless
 // 16-bit node references: a binary node's index, or the leaf flag | triangle index.
 constexpr uint32_t kLeaf16 = 0x8000u;
+// A cluster's word: its reference, its nearest neighbour's position (12 bits) and its
+// triangle count, saturating at 15 (exact up to the largest leaf, which is all a count
+// above leaf_size is used for).
+constexpr uint32_t kNnShift = 16, kNnMask = 0xFFFu, kCntShift = 28, kCntMax = 15u;
+static_assert(kSmallMax - 1u <= kNnMask, "neighbour positions take 12 bits");
+static_assert((uint32_t)kMaxLeaf < kCntMax, "saturated counts must exceed every leaf size");
 
-// Shared memory (bytes).  PLOC: two cluster buffers, each six box arrays and one word
-// per cluster (16-bit reference | triangle count << 16); the nearest neighbours of an
-// iteration sit in the buffer the iteration writes (read into registers before it is
-// written).  Before PLOC the triangles' boxes, in input order, fill buffer 1 and the
-// sort's keys buffer 0.  Collapse: the binary nodes' cost records (or areas), children
-// and counts, and two frontiers.  The block-scan words last.
-constexpr uint32_t kBoxBytes = 6u * 4u * kSmallMax;
-constexpr uint32_t kOffBox0 = 0, kOffBox1 = kBoxBytes;
-constexpr uint32_t kOffId0 = 2u * kBoxBytes, kOffId1 = kOffId0 + 4u * kSmallMax;
-constexpr uint32_t kOffScan = kOffId1 + 4u * kSmallMax;
-constexpr uint32_t kOffCost = 0;
-constexpr uint32_t kOffLr = kOffCost + (uint32_t)sizeof(CostNode) * kSmallMax;
-constexpr uint32_t kOffCnt = kOffLr + 4u * kSmallMax;
-constexpr uint32_t kOffFr0 = kOffCnt + 2u * kSmallMax;
-constexpr uint32_t kOffFr1 = kOffFr0 + 4u * kSmallMax;
+// Shared memory, in rows of one word per triangle.  PLOC: the clusters' boxes (six rows,
+// structure of arrays), their words, and seven rows of the binary nodes' costs in 1..7
+// child slots (row k - 1 for k slots; row 0 holds the area for the largest-child-first
+// collapse).  Before PLOC the sort's keys take the box rows and the triangles' boxes in
+// input order the cost rows; within an iteration, row 6 of the nodes it is about to make
+// lists its merges, and the rows of the nodes after those stage its survivors.
+// Collapse, over the box and word rows: the leaf permutation, the binary nodes'
+// children, slot splits and counts, and two frontiers (the cost rows stay).  Re-layout:
+// the permutation, then the triangles as loaded.  The block-scan words last.
+constexpr uint32_t kRow = 4u * kSmallMax;
+constexpr uint32_t kOffBox = 0;
+constexpr uint32_t kOffWord = 6u * kRow;
+constexpr uint32_t kOffCost = 7u * kRow;
+constexpr uint32_t kOffScan = 14u * kRow;
 constexpr uint32_t kSmemBytes = kOffScan + 4u * 64u;
-static_assert(kOffFr1 + 4u * kSmallMax <= kOffScan, "collapse tables overlap the scan words");
+constexpr uint32_t kOffPerm = 0;                         // leaf order -> triangle (16 bits)
+constexpr uint32_t kOffLr = kOffPerm + 2u * kSmallMax;    // children (16 + 16 bits)
+constexpr uint32_t kOffBits = kOffLr + kRow;              // slot splits (CostNode::bits)
+constexpr uint32_t kOffCnt = kOffBits + kRow;             // counts (16 bits)
+constexpr uint32_t kOffFr0 = kOffCnt + 2u * kSmallMax;    // frontier: ref | slot << 16
+constexpr uint32_t kOffFr1 = kOffFr0 + kRow;
+constexpr uint32_t kOffStage = kOffPerm + 2u * kSmallMax; // 9 words per triangle
+static_assert(kOffFr1 + kRow <= kOffCost, "collapse tables overlap the cost rows");
+static_assert(kOffStage + 36u * kSmallMax <= kOffScan, "staged triangles overlap the scan words");
 static_assert(kSmemBytes <= 232448u, "more shared memory than a block can have");
 constexpr int kPer = (int)(kSmallMax / kThreads); // positions per thread
 
@@ -111,14 +127,16 @@ __device__ __forceinline__ Box tri_box(const float t[9], bool fin) {
 	           fmaxf(t[1], fmaxf(t[4], t[7])), fmaxf(t[2], fmaxf(t[5], t[8]))};
 }
 
-__device__ __forceinline__ CostNode load_cost(const CostNode *p) {
-	CostNode c;
-	c.c1 = __ldcg(&p->c1);
+// A child's costs in 1..7 slots (cs[1..7], in units of its own area): a triangle's from
+// the model, a binary node's from its cost rows (node_costs' values, stored that way).
+__device__ __forceinline__ void row_costs(uint32_t y, const float *crow, float cs[8]) {
+	if (y & kLeaf16) {
+		leaf_costs(cs);
+		return;
+	}
 #pragma unroll
-	for (int k = 0; k < 7; ++k)
-		c.cd[k] = __ldcg(&p->cd[k]);
-	c.bits = __ldcg(&p->bits);
-	return c;
+	for (int j = 1; j < 8; ++j)
+		cs[j] = crow[(uint32_t)(j - 1) * kSmallMax + y];
 }
 
 __device__ __forceinline__ float tri_centroid(const float t[9], int k) {
@@ -165,25 +183,26 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t *words, uint
 
 // Whether child y (16-bit reference) of an 8-wide node becomes a node of its own.
 __device__ __forceinline__ bool child_inner(uint32_t y, uint32_t count, uint32_t leaf_size,
-                                            int use_cost, const CostNode *cs) {
-	return !(y & kLeaf16) && (count > leaf_size || (use_cost && (cs[y].bits >> 31) == 0u));
+                                            int use_cost, const uint32_t *bits) {
+	return !(y & kLeaf16) && (count > leaf_size || (use_cost && (bits[y] >> 31) == 0u));
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
     k_build_small(const float *__restrict__ tris, uint32_t n, uint32_t leaf_size, int use_cost,
-                  float4 *__restrict__ ibox, uint32_t *__restrict__ lr,
+                  float4 *__restrict__ ibox, float4 *__restrict__ lbox, uint32_t *__restrict__ lr,
                   CostNode *__restrict__ cost, Node8 *__restrict__ nodes, uint32_t node_cap,
                   float4 *__restrict__ tri4, uint32_t *__restrict__ inv, uint32_t *__restrict__ ctr,
                   uint32_t *__restrict__ err) {
 	extern __shared__ __align__(16) unsigned char sm[];
 	uint32_t *scan = reinterpret_cast<uint32_t *>(sm + kOffScan);
 	const uint32_t tid = threadIdx.x;
-	float *box[2] = {reinterpret_cast<float *>(sm + kOffBox0), reinterpret_cast<float *>(sm + kOffBox1)};
-	uint32_t *ids[2] = {reinterpret_cast<uint32_t *>(sm + kOffId0),
-	                    reinterpret_cast<uint32_t *>(sm + kOffId1)};
+	float *box = reinterpret_cast<float *>(sm + kOffBox);
+	uint32_t *word = reinterpret_cast<uint32_t *>(sm + kOffWord);
+	float *crow = reinterpret_cast<float *>(sm + kOffCost);
 
-	// 1. One pass over the triangles: boxes (input order, buffer 1), centroids kept for
-	// the keys; centroid bounds of the finite triangles; Morton keys; bitonic sort.
+	// 1. One pass over the triangles: boxes (input order, into the cost rows, and to the
+	// leaf-box array for the collapse), centroids kept for the keys; centroid bounds of
+	// the finite triangles; Morton keys; bitonic sort.
 	float cen[kPer][3];
 	bool cfin[kPer];
 	{
@@ -201,7 +220,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
 				for (int q = 0; q < 9; ++q)
 					fin = fin && isfinite(t[q]);
-				store_box(box[1], i, tri_box(t, fin));
+				const Box b = tri_box(t, fin);
+				store_box(crow, i, b);
+				lbox[2 * i] = box_lo(b);
+				lbox[2 * i + 1] = box_hi(b);
 				cfin[k] = fin;
 #pragma unroll
 				for (int q = 0; q < 3; ++q) {
@@ -220,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 				mn[q] = fminf(mn[q], __shfl_xor_sync(0xFFFFFFFFu, mn[q], o));
 				mx[q] = fmaxf(mx[q], __shfl_xor_sync(0xFFFFFFFFu, mx[q], o));
 			}
-		float *red = reinterpret_cast<float *>(sm + kOffId0); // 32 x 6 words
+		float *red = reinterpret_cast<float *>(word); // 32 x 6 words
 		if ((tid & 31u) == 0)
 			for (int q = 0; q < 3; ++q) {
 				red[6 * (tid >> 5) + q] = mn[q];
@@ -251,7 +273,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 	uint32_t P = 2;
 	while (P < n)
 		P <<= 1;
-	unsigned long long *keys = reinterpret_cast<unsigned long long *>(sm + kOffBox0);
+	unsigned long long *keys = reinterpret_cast<unsigned long long *>(sm + kOffBox);
 	{
 		float lo[3], sc[3];
 		const bool any = __uint_as_float(scan[0]) <= __uint_as_float(scan[3]);
@@ -295,7 +317,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 			__syncthreads();
 		}
 
-	// 2. Leaves in Morton order (boxes gathered from buffer 1), then PLOC.
+	// 2. Leaves in Morton order (boxes gathered from the cost rows), then PLOC.
 	{
 		uint32_t prim[kPer];
 #pragma unroll
@@ -303,122 +325,134 @@ __global__ void __launch_bounds__(kThreads, 1)
 			const uint32_t i = tid + (uint32_t)k * kThreads;
 			prim[k] = i < n ? (uint32_t)(keys[i] & 0xFFFFFFFFull) : 0u;
 		}
-		__syncthreads(); // every key read before buffer 0 is overwritten
+		__syncthreads(); // every key read before the box rows are overwritten
 #pragma unroll
 		for (int k = 0; k < kPer; ++k) {
 			const uint32_t i = tid + (uint32_t)k * kThreads;
 			if (i < n) {
-				store_box(box[0], i, load_box(box[1], prim[k]));
-				ids[0][i] = kLeaf16 | prim[k] | (1u << 16);
+				store_box(box, i, load_box(crow, prim[k]));
+				word[i] = kLeaf16 | prim[k] | (1u << kCntShift);
 			}
 		}
 	}
 	__syncthreads();
+	uint32_t *list = reinterpret_cast<uint32_t *>(crow + 6u * kSmallMax);
 	uint32_t m = n, made = 0;
-	int cur = 0;
 	for (uint32_t iter = 0; m > 1; ++iter) {
-		const float *bc = box[cur];
-		uint16_t *nn = reinterpret_cast<uint16_t *>(ids[cur ^ 1]); // free until the writes
+		// (a) Each cluster's nearest neighbour, into its word.
 		for (uint32_t i = tid; i < m; i += kThreads) {
+			uint32_t bj;
 			if (iter >= kPlocRounds) {
-				nn[i] = (uint16_t)((i ^ 1u) < m ? (i ^ 1u) : i); // the last of odd m stays
-				continue;
-			}
-			const Box bi = load_box(bc, i);
-			const uint32_t lo = i > (uint32_t)kRadius ? i - kRadius : 0u;
-			const uint32_t hi = min(m - 1u, i + (uint32_t)kRadius);
-			float best = INFINITY;
-			uint32_t best_tb = 0xFFFFFFFFu, bj = i;
-			for (uint32_t j = lo; j <= hi; ++j) {
-				if (j == i)
-					continue;
-				const float d = union_area(bi, load_box(bc, j));
-				// Tie-break of the pair {i, j}: distance, parity of the lower position,
-				// lower position (fields of 4, 1 and 12 bits).
-				const uint32_t low = min(i, j);
-				const uint32_t tb = ((j > i ? j - i : i - j) << 13) | ((low & 1u) << 12) | low;
-				if (d < best || (d == best && tb < best_tb)) {
-					best = d;
-					best_tb = tb;
-					bj = j;
+				bj = (i ^ 1u) < m ? (i ^ 1u) : i; // the last of odd m stays
+			} else {
+				const Box bi = load_box(box, i);
+				const uint32_t lo = i > (uint32_t)kRadius ? i - kRadius : 0u;
+				const uint32_t hi = min(m - 1u, i + (uint32_t)kRadius);
+				float best = INFINITY;
+				uint32_t best_tb = 0xFFFFFFFFu;
+				bj = i;
+				for (uint32_t j = lo; j <= hi; ++j) {
+					if (j == i)
+						continue;
+					const float d = union_area(bi, load_box(box, j));
+					// Tie-break of the pair {i, j}: distance, parity of the lower
+					// position, lower position (fields of 4, 1 and 12 bits).
+					const uint32_t low = min(i, j);
+					const uint32_t tb = ((j > i ? j - i : i - j) << 13) | ((low & 1u) << 12) | low;
+					if (d < best || (d == best && tb < best_tb)) {
+						best = d;
+						best_tb = tb;
+						bj = j;
+					}
 				}
 			}
-			nn[i] = (uint16_t)bj;
+			word[i] = (word[i] & ~(kNnMask << kNnShift)) | (bj << kNnShift);
 		}
 		__syncthreads();
-		// Survivors and merges over contiguous chunks of kPer positions per thread,
-		// packed (kept | merges << 16) for one scan; the partners read before the scan's
-		// barriers, after which the neighbour words are overwritten.
-		uint32_t flag[kPer], part[kPer], local = 0;
+		// (b) Survivors and merges over contiguous chunks of kPer positions per thread,
+		// packed (kept | merges << 16) for one scan.  Survivor r is staged at index
+		// made + merged + r of the cost rows (boxes in rows 0-5, words in row 6: nodes
+		// not made yet, and kept <= n - made - merged of them are free); a merge's
+		// position and rank are listed in row 6 of the node it makes.
+		uint32_t keepm = 0, mergem = 0, local = 0;
 #pragma unroll
 		for (int k = 0; k < kPer; ++k) {
 			const uint32_t i = tid * (uint32_t)kPer + (uint32_t)k;
-			uint32_t f = 0, j = 0;
 			if (i < m) {
-				j = nn[i];
-				const bool mutual = nn[j] == i;
-				f = (mutual && i > j) ? 0u : (1u | ((mutual && i < j) ? 0x10000u : 0u));
+				const uint32_t j = (word[i] >> kNnShift) & kNnMask;
+				const bool mutual = ((word[j] >> kNnShift) & kNnMask) == i;
+				if (!(mutual && i > j)) {
+					keepm |= 1u << k;
+					local += 1u;
+					if (mutual && i < j) {
+						mergem |= 1u << k;
+						local += 0x10000u;
+					}
+				}
 			}
-			flag[k] = f;
-			part[k] = j;
-			local += f;
 		}
 		uint32_t total;
-		uint32_t pre = block_scan(local, scan, total);
+		const uint32_t pre = block_scan(local, scan, total);
 		const uint32_t kept = total & 0xFFFFu, merged = total >> 16;
-		const float *bs = box[cur];
-		float *bd = box[cur ^ 1];
-		const uint32_t *is = ids[cur];
-		uint32_t *id_out = ids[cur ^ 1];
+		uint32_t *stage_w = list; // row 6
+		const uint32_t tbase = made + merged;
+		{
+			uint32_t q = made + (pre >> 16), pos = pre & 0xFFFFu;
 #pragma unroll
-		for (int k = 0; k < kPer; ++k) {
-			const uint32_t i = tid * (uint32_t)kPer + (uint32_t)k;
-			const uint32_t f = flag[k];
-			if (f) {
-				const uint32_t pos = pre & 0xFFFFu;
-				Box b = load_box(bs, i);
-				uint32_t word = is[i];
-				if (f >> 16) {
-					const uint32_t j = part[k];
-					const Box bj = load_box(bs, j);
-					const uint32_t node = made + (pre >> 16);
-					const uint32_t wa = word, wc = is[j];
-					const uint32_t a = wa & 0xFFFFu, c = wc & 0xFFFFu;
-					const uint32_t count = (wa >> 16) + (wc >> 16);
-					const Box u = join(b, bj);
-					if (use_cost) {
-						float cl[8], cr[8];
-						if (a & kLeaf16) {
-							leaf_costs(cl);
-						} else {
-							const CostNode ca = load_cost(cost + a);
-							node_costs(ca, cl);
-						}
-						if (c & kLeaf16) {
-							leaf_costs(cr);
-						} else {
-							const CostNode cc = load_cost(cost + c);
-							node_costs(cc, cr);
-						}
-						cost[node] = merge_costs(cl, cr, half_extent(box_lo(b), box_hi(b)),
-						                         half_extent(box_lo(bj), box_hi(bj)),
-						                         half_extent(box_lo(u), box_hi(u)), count,
-						                         leaf_size);
-					}
-					lr[node] = a | (c << 16);
-					ibox[2 * node] = make_float4(u.lx, u.ly, u.lz, half_area(box_lo(u), box_hi(u)));
-					ibox[2 * node + 1] = make_float4(u.hx, u.hy, u.hz, __uint_as_float(count));
-					b = u;
-					word = node | (count << 16);
+			for (int k = 0; k < kPer; ++k) {
+				if (!((keepm >> k) & 1u))
+					continue;
+				const uint32_t i = tid * (uint32_t)kPer + (uint32_t)k;
+				if ((mergem >> k) & 1u) {
+					list[q++] = i | (pos << 16);
+				} else {
+					store_box(crow, tbase + pos, load_box(box, i));
+					stage_w[tbase + pos] = word[i];
 				}
-				store_box(bd, pos, b);
-				id_out[pos] = word;
+				++pos;
 			}
-			pre += f;
+		}
+		__syncthreads();
+		// (c) The merges, one per thread: node made + q joins the clusters at its listed
+		// position i and at i's neighbour j, and is staged at its survivor rank.  Each
+		// position belongs to one pair, and nothing writes the clusters until (d).
+		for (uint32_t q = tid; q < merged; q += kThreads) {
+			const uint32_t node = made + q;
+			const uint32_t e = list[node], i = e & 0xFFFFu, pos = e >> 16;
+			const uint32_t wi = word[i], j = (wi >> kNnShift) & kNnMask, wj = word[j];
+			const Box bi = load_box(box, i), bj = load_box(box, j), u = join(bi, bj);
+			const uint32_t a = wi & 0xFFFFu, c = wj & 0xFFFFu;
+			const uint32_t count = min((wi >> kCntShift) + (wj >> kCntShift), kCntMax);
+			const float area = half_area(box_lo(u), box_hi(u));
+			if (use_cost) {
+				float cl[8], cr[8];
+				row_costs(a, crow, cl);
+				row_costs(c, crow, cr);
+				const CostNode cn = merge_costs(cl, cr, half_extent(box_lo(bi), box_hi(bi)),
+				                                half_extent(box_lo(bj), box_hi(bj)),
+				                                half_extent(box_lo(u), box_hi(u)), count, leaf_size);
+				crow[node] = cn.c1;
+#pragma unroll
+				for (uint32_t s = 2; s < 8; ++s) // row 6 last: this merge's list entry
+					crow[(s - 1u) * kSmallMax + node] = fminf(cn.c1, cn.cd[s - 2u]);
+				cost[node].bits = cn.bits;
+			} else {
+				crow[node] = area;
+			}
+			lr[node] = a | (c << 16);
+			ibox[2 * node] = make_float4(u.lx, u.ly, u.lz, area);
+			ibox[2 * node + 1] = make_float4(u.hx, u.hy, u.hz, __uint_as_float(count));
+			store_box(crow, tbase + pos, u);
+			stage_w[tbase + pos] = node | (count << kCntShift);
+		}
+		__syncthreads();
+		// (d) The staged survivors become clusters 0 .. kept - 1.
+		for (uint32_t r = tid; r < kept; r += kThreads) {
+			store_box(box, r, load_box(crow, tbase + r));
+			word[r] = stage_w[tbase + r];
 		}
 		made += merged;
 		m = kept;
-		cur ^= 1;
 		if (merged == 0u || iter >= n) { // cannot happen (see above); reported, not looped
 			if (tid == 0)
 				atomicOr(err, kErrCollapse);
@@ -429,22 +463,35 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 	// 3. The 8-wide collapse from shared-memory copies of the binary nodes: eight lanes
 	// per frontier node, lane c on child c.
-	const uint32_t root = ids[cur][0] & 0xFFFFu;
+	const uint32_t root = word[0] & 0xFFFFu;
 	__syncthreads(); // everything of PLOC read before its space is reused
-	CostNode *cs = reinterpret_cast<CostNode *>(sm + kOffCost);
-	float *area = reinterpret_cast<float *>(sm + kOffCost);
+	uint16_t *perm = reinterpret_cast<uint16_t *>(sm + kOffPerm);
 	uint32_t *lr_s = reinterpret_cast<uint32_t *>(sm + kOffLr);
+	uint32_t *bits_s = reinterpret_cast<uint32_t *>(sm + kOffBits);
 	uint16_t *cnt_s = reinterpret_cast<uint16_t *>(sm + kOffCnt);
 	uint32_t *fr[2] = {reinterpret_cast<uint32_t *>(sm + kOffFr0),
 	                   reinterpret_cast<uint32_t *>(sm + kOffFr1)};
-	for (uint32_t k = tid; k < made; k += kThreads) {
-		lr_s[k] = __ldcg(&lr[k]);
-		const float4 lo = __ldcg(&ibox[2 * k]);
-		cnt_s[k] = (uint16_t)__float_as_uint(__ldcg(&ibox[2 * k + 1].w));
-		if (use_cost)
-			cs[k] = load_cost(cost + k);
-		else
-			area[k] = lo.w;
+	{
+		// All of a thread's loads before its stores (one wait, not one per node).
+		uint32_t w[kPer], cn[kPer], bt[kPer];
+#pragma unroll
+		for (int u = 0; u < kPer; ++u) {
+			const uint32_t k = tid + (uint32_t)u * kThreads;
+			if (k < made) {
+				w[u] = __ldcg(&lr[k]);
+				cn[u] = __float_as_uint(__ldcg(&ibox[2 * k + 1].w));
+				bt[u] = use_cost ? __ldcg(&cost[k].bits) : 0u;
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < kPer; ++u) {
+			const uint32_t k = tid + (uint32_t)u * kThreads;
+			if (k < made) {
+				lr_s[k] = w[u];
+				cnt_s[k] = (uint16_t)cn[u];
+				bits_s[k] = bt[u];
+			}
+		}
 	}
 	if (tid == 0)
 		fr[0][0] = root; // slot 0
@@ -475,8 +522,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 					C[0] = r;
 					nc = 1;
 				} else if (use_cost) {
+					// A binary node opened into i slots when its cost there (row i - 1)
+					// is below its cost in one (row 0); a child's share from the splits.
 					uint32_t py[8], pi[8];
-					const uint32_t a0 = split_of(cs[r].bits, 8u);
+					const uint32_t a0 = split_of(bits_s[r], 8u);
 					py[0] = lr_s[r] >> 16;
 					pi[0] = 8u - a0;
 					py[1] = lr_s[r] & 0xFFFFu;
@@ -488,8 +537,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 						bool open = false;
 						uint32_t a = 1;
 						if (!(y & kLeaf16) && i > 1u) {
-							open = cs[y].cd[i - 2u] < cs[y].c1;
-							a = split_of(cs[y].bits, i);
+							open = crow[(i - 1u) * kSmallMax + y] < crow[y];
+							a = split_of(bits_s[y], i);
 						}
 						if (open && top <= 6) {
 							py[top] = lr_s[y] >> 16;
@@ -508,7 +557,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 						int best = -1;
 						float best_area = -1.0f;
 						for (int c = 0; c < nc; ++c) {
-							const float ac = (C[c] & kLeaf16) ? -1.0f : area[C[c]];
+							const float ac = (C[c] & kLeaf16) ? -1.0f : crow[C[c]];
 							if (ac > best_area) {
 								best_area = ac;
 								best = c;
@@ -528,7 +577,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 			for (int c = 0; c < nc; ++c) {
 				const uint32_t z = C[c];
 				const uint32_t nz = (z & kLeaf16) ? 1u : cnt_s[z];
-				const bool in = child_inner(z, nz, leaf_size, use_cost, cs);
+				const bool in = child_inner(z, nz, leaf_size, use_cost, bits_s);
 				if ((uint32_t)c == c8) {
 					my_inner = n_inner;
 					my_tris = n_tris;
@@ -558,43 +607,19 @@ __global__ void __launch_bounds__(kThreads, 1)
 					if (inner_y) {
 						ref = nb + my_inner;
 						fout[ob + my_inner] = y | (ref << 16);
-						lo = __ldcg(&ibox[2 * y]);
-						hi = __ldcg(&ibox[2 * y + 1]);
 					} else {
-						// A leaf: its triangles in subtree order (at most leaf_size <= 8),
-						// re-laid out here; a single triangle's box comes from the triangle.
+						// A leaf: its triangles' positions in subtree order (at most
+						// leaf_size <= 8) go to the permutation; the triangles are copied
+						// after the last level, all at once.
 						uint32_t dst = tb + my_tris;
 						ref = make_leaf(dst, cnt_y);
-						if (!(y & kLeaf16)) {
-							lo = __ldcg(&ibox[2 * y]);
-							hi = __ldcg(&ibox[2 * y + 1]);
-						}
 						uint32_t stack[8];
 						int sp = 0;
 						stack[sp++] = y;
 						while (sp > 0) {
 							const uint32_t z = stack[--sp];
 							if (z & kLeaf16) {
-								const uint32_t p = z & ~kLeaf16;
-								float t[9];
-#pragma unroll
-								for (int q = 0; q < 9; ++q)
-									t[q] = __ldg(tris + 9 * (size_t)p + q);
-								bool fin = true;
-#pragma unroll
-								for (int q = 0; q < 9; ++q)
-									fin = fin && isfinite(t[q]);
-								if (y & kLeaf16) {
-									const Box tb9 = tri_box(t, fin);
-									lo = box_lo(tb9);
-									hi = box_hi(tb9);
-								}
-								// As k_relayout: the second word's w flags a non-finite vertex.
-								tri4[3 * (size_t)dst] = make_float4(t[0], t[1], t[2], __uint_as_float(p));
-								tri4[3 * (size_t)dst + 1] = make_float4(t[3], t[4], t[5], fin ? 0.0f : 1.0f);
-								tri4[3 * (size_t)dst + 2] = make_float4(t[6], t[7], t[8], 0.0f);
-								inv[p] = dst;
-								++dst;
+								perm[dst++] = (uint16_t)(z & ~kLeaf16);
 							} else if (sp <= 6) {
 								stack[sp++] = lr_s[z] >> 16;
 								stack[sp++] = lr_s[z] & 0xFFFFu;
@@ -603,6 +628,11 @@ __global__ void __launch_bounds__(kThreads, 1)
 							}
 						}
 					}
+					// The child's box: a binary node's from its record, a single
+					// triangle's from the leaf-box array (one wait per level step).
+					const float4 *src = (y & kLeaf16) ? lbox + 2 * (y & ~kLeaf16) : ibox + 2 * y;
+					lo = __ldcg(src);
+					hi = __ldcg(src + 1);
 				}
 				Child8 ch;
 				ch.lo_x = lo.x;
@@ -631,6 +661,47 @@ __global__ void __launch_bounds__(kThreads, 1)
 		ctr[kCtrNodes] = n_nodes;
 		ctr[kCtrTris] = n_placed;
 	}
+	// 4. The triangles in leaf order (as k_relayout; the second word's w flags a
+	// non-finite vertex): copied into shared memory by consecutive words, every load of a
+	// batch issued before its stores, then written out in permutation order.
+	__syncthreads();
+	float *stage = reinterpret_cast<float *>(sm + kOffStage);
+	const uint32_t words = 9u * n;
+	constexpr uint32_t kBatch = 12;
+	for (uint32_t base = 0; base < words; base += kBatch * kThreads) {
+		float v[kBatch];
+#pragma unroll
+		for (uint32_t u = 0; u < kBatch; ++u) {
+			const uint32_t w = base + u * kThreads + tid;
+			v[u] = w < words ? __ldg(tris + w) : 0.0f;
+		}
+#pragma unroll
+		for (uint32_t u = 0; u < kBatch; ++u) {
+			const uint32_t w = base + u * kThreads + tid;
+			if (w < words)
+				stage[w] = v[u];
+		}
+	}
+	__syncthreads();
+	const uint32_t placed = min(n_placed, n);
+#pragma unroll
+	for (int k = 0; k < kPer; ++k) {
+		const uint32_t d = tid + (uint32_t)k * kThreads;
+		const uint32_t p = d < placed ? perm[d] : 0xFFFFu;
+		if (p >= n)
+			continue;
+		float t[9];
+		bool fin = true;
+#pragma unroll
+		for (int q = 0; q < 9; ++q) {
+			t[q] = stage[9u * p + q];
+			fin = fin && isfinite(t[q]);
+		}
+		tri4[3 * (size_t)d] = make_float4(t[0], t[1], t[2], __uint_as_float(p));
+		tri4[3 * (size_t)d + 1] = make_float4(t[3], t[4], t[5], fin ? 0.0f : 1.0f);
+		tri4[3 * (size_t)d + 2] = make_float4(t[6], t[7], t[8], 0.0f);
+		inv[p] = d;
+	}
 }
 
 } // namespace
@@ -655,9 +726,9 @@ cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_si
 		attr_set.fetch_or(bit);
 	}
 	k_build_small<<<1, kThreads, kSmemBytes, st>>>(
-	    d_tris, n, leaf_size, use_cost ? 1 : 0, ws.ibox.as<float4>(), ws.left.as<uint32_t>(),
-	    use_cost ? ws.cost.as<CostNode>() : nullptr, sc.nodes.as<Node8>(), node_cap,
-	    sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr, d_err);
+	    d_tris, n, leaf_size, use_cost ? 1 : 0, ws.ibox.as<float4>(), ws.lbox.as<float4>(),
+	    ws.left.as<uint32_t>(), use_cost ? ws.cost.as<CostNode>() : nullptr,
+	    sc.nodes.as<Node8>(), node_cap, sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr, d_err);
 	return cudaGetLastError();
 }
 
