@@ -65,8 +65,9 @@ static_assert((uint32_t)kMaxLeaf < kCntMax, "saturated counts must exceed every 
 // input order the cost rows; within an iteration, row 6 of the nodes it is about to make
 // lists its merges, and the rows of the nodes after those stage its survivors.
 // Collapse, over the box and word rows: the leaf permutation, the binary nodes'
-// children, slot splits and counts, and two frontiers (the cost rows stay).  Re-layout:
-// the permutation, then the triangles as loaded.  The block-scan words last.
+// children, slot splits and counts, two frontiers and the groups' exchange words (the
+// cost rows stay).  Re-layout: the permutation, then the triangles as loaded.  The
+// block-scan words last.
 constexpr uint32_t kRow = 4u * kSmallMax;
 constexpr uint32_t kOffBox = 0;
 constexpr uint32_t kOffWord = 6u * kRow;
@@ -79,8 +80,9 @@ constexpr uint32_t kOffBits = kOffLr + kRow;              // slot splits (CostNo
 constexpr uint32_t kOffCnt = kOffBits + kRow;             // counts (16 bits)
 constexpr uint32_t kOffFr0 = kOffCnt + 2u * kSmallMax;    // frontier: ref | slot << 16
 constexpr uint32_t kOffFr1 = kOffFr0 + kRow;
+constexpr uint32_t kOffXch = kOffFr1 + kRow;             // one word per thread
 constexpr uint32_t kOffStage = kOffPerm + 2u * kSmallMax; // 9 words per triangle
-static_assert(kOffFr1 + kRow <= kOffCost, "collapse tables overlap the cost rows");
+static_assert(kOffXch + 4u * kThreads <= kOffCost, "collapse tables overlap the cost rows");
 static_assert(kOffStage + 36u * kSmallMax <= kOffScan, "staged triangles overlap the scan words");
 static_assert(kSmemBytes <= 232448u, "more shared memory than a block can have");
 constexpr int kPer = (int)(kSmallMax / kThreads); // positions per thread
@@ -179,6 +181,20 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t *words, uint
 	__syncthreads();
 	total = words[63];
 	return (warp ? words[32 + warp - 1] : 0u) + x - v;
+}
+
+// An 8-wide node's child record (an empty slot: NaN bounds and kNone).
+__device__ __forceinline__ Child8 make_child(float4 lo, float4 hi, uint32_t ref) {
+	Child8 ch;
+	ch.lo_x = lo.x;
+	ch.lo_y = lo.y;
+	ch.lo_z = lo.z;
+	ch.ref = ref;
+	ch.hi_x = hi.x;
+	ch.hi_y = hi.y;
+	ch.hi_z = hi.z;
+	ch.pad = 0u;
+	return ch;
 }
 
 // Whether child y (16-bit reference) of an 8-wide node becomes a node of its own.
@@ -306,8 +322,9 @@ __global__ void __launch_bounds__(kThreads, 1)
 	__syncthreads();
 	for (uint32_t size = 2; size <= P; size <<= 1)
 		for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+			const uint32_t ls = (uint32_t)__ffs((int)stride) - 1u; // log2(stride)
 			for (uint32_t t = tid; t < P / 2; t += kThreads) {
-				const uint32_t i = (t / stride) * 2u * stride + (t % stride), j = i + stride;
+				const uint32_t i = ((t >> ls) << (ls + 1u)) | (t & (stride - 1u)), j = i + stride;
 				const unsigned long long a = keys[i], b = keys[j];
 				if ((a > b) == ((i & size) == 0u)) {
 					keys[i] = b;
@@ -324,6 +341,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 		for (int k = 0; k < kPer; ++k) {
 			const uint32_t i = tid + (uint32_t)k * kThreads;
 			prim[k] = i < n ? (uint32_t)(keys[i] & 0xFFFFFFFFull) : 0u;
+			if (prim[k] >= n) { // cannot happen: the keys of [0, n) sort first
+				atomicOr(err, kErrCollapse);
+				prim[k] = 0;
+			}
 		}
 		__syncthreads(); // every key read before the box rows are overwritten
 #pragma unroll
@@ -471,6 +492,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 	uint16_t *cnt_s = reinterpret_cast<uint16_t *>(sm + kOffCnt);
 	uint32_t *fr[2] = {reinterpret_cast<uint32_t *>(sm + kOffFr0),
 	                   reinterpret_cast<uint32_t *>(sm + kOffFr1)};
+	uint32_t *xch = reinterpret_cast<uint32_t *>(sm + kOffXch);
 	{
 		// All of a thread's loads before its stores (one wait, not one per node).
 		uint32_t w[kPer], cn[kPer], bt[kPer];
@@ -511,87 +533,108 @@ __global__ void __launch_bounds__(kThreads, 1)
 		for (uint32_t b0 = 0; b0 < n_items; b0 += kThreads / 8u) {
 			const uint32_t it = b0 + tid / 8u;
 			const bool live = it < n_items;
-			// Every lane of the group computes the node's children (same smem reads).
-			uint32_t C[8];
-			int nc = 0;
-			uint32_t slot = 0;
-			if (live) {
-				const uint32_t r = fin[it] & 0xFFFFu;
+			uint32_t slot = 0, y = 0, k = c8;
+			bool has = false;
+			const uint32_t r = live ? fin[it] & 0xFFFFu : 0u;
+			if (live)
 				slot = fin[it] >> 16;
-				if (r & kLeaf16) {
-					C[0] = r;
-					nc = 1;
-				} else if (use_cost) {
-					// A binary node opened into i slots when its cost there (row i - 1)
-					// is below its cost in one (row 0); a child's share from the splits.
-					uint32_t py[8], pi[8];
-					const uint32_t a0 = split_of(bits_s[r], 8u);
-					py[0] = lr_s[r] >> 16;
-					pi[0] = 8u - a0;
-					py[1] = lr_s[r] & 0xFFFFu;
-					pi[1] = a0;
-					int top = 2;
-					while (top > 0) {
-						--top;
-						const uint32_t y = py[top], i = pi[top];
-						bool open = false;
-						uint32_t a = 1;
-						if (!(y & kLeaf16) && i > 1u) {
-							open = crow[(i - 1u) * kSmallMax + y] < crow[y];
-							a = split_of(bits_s[y], i);
-						}
-						if (open && top <= 6) {
-							py[top] = lr_s[y] >> 16;
-							pi[top] = i - a;
-							py[top + 1] = lr_s[y] & 0xFFFFu;
-							pi[top + 1] = a;
-							top += 2;
-						} else if (nc < 8) {
-							C[nc++] = y;
-						}
+			if (use_cost) {
+				// The node's children as slot ranges: lane c8 holds the subtree covering
+				// slots [c8, c8 + span).  A subtree opened into its span (the root always;
+				// another when its cost in `span` slots, row span - 1, is below its cost
+				// in one, row 0) splits it: the left child keeps the first split_of(span)
+				// slots, the right child goes to the lane after them.  Every subtree
+				// splits at once, at most 7 rounds; the ranges end in the order of the
+				// depth-first opening (left subtrees first), which is the slot order.
+				uint32_t span = (live && c8 == 0u) ? 8u : 0u;
+				y = r;
+				uint32_t *x = xch + (tid & ~7u);
+				for (int round = 0; round < 8; ++round) {
+					uint32_t give = 0, a = 0;
+					if (span > 1u && !(y & kLeaf16) &&
+					    (round == 0 || crow[(span - 1u) * kSmallMax + y] < crow[y])) {
+						a = split_of(bits_s[y], span);
+						const uint32_t w = lr_s[y];
+						give = (w >> 16) | ((span - a) << 16); // nonzero: span - a >= 1
+						y = w & 0xFFFFu;
+						span = a;
 					}
-				} else {
-					C[0] = r;
-					nc = 1;
-					while (nc < 8) {
-						int best = -1;
-						float best_area = -1.0f;
-						for (int c = 0; c < nc; ++c) {
-							const float ac = (C[c] & kLeaf16) ? -1.0f : crow[C[c]];
-							if (ac > best_area) {
-								best_area = ac;
-								best = c;
-							}
-						}
-						if (best < 0)
-							break;
-						const uint32_t x = C[best];
-						C[best] = lr_s[x] & 0xFFFFu;
-						C[nc++] = lr_s[x] >> 16;
+					if (!__any_sync(0xFFFFFFFFu, give != 0u))
+						break;
+					x[c8] = 0u; // only this lane reads its word (below)
+					__syncwarp();
+					if (give)
+						x[c8 + a] = give; // inside the giver's range: no other holder there
+					__syncwarp();
+					const uint32_t got = x[c8];
+					if (got) {
+						y = got & 0xFFFFu;
+						span = got >> 16;
 					}
 				}
-			}
-			// This lane's child: inner children before it, triangles before it.
-			uint32_t n_inner = 0, n_tris = 0, my_inner = 0, my_tris = 0, y = 0, cnt_y = 0;
-			bool mine = false, inner_y = false;
-			for (int c = 0; c < nc; ++c) {
-				const uint32_t z = C[c];
-				const uint32_t nz = (z & kLeaf16) ? 1u : cnt_s[z];
-				const bool in = child_inner(z, nz, leaf_size, use_cost, bits_s);
-				if ((uint32_t)c == c8) {
-					my_inner = n_inner;
-					my_tris = n_tris;
-					y = z;
-					cnt_y = nz;
-					inner_y = in;
-					mine = true;
+				has = span > 0u;
+				const uint32_t held = (__ballot_sync(0xFFFFFFFFu, has) >> (lane & 24u)) & 0xFFu;
+				k = __popc(held & ((1u << c8) - 1u));
+			} else if (live) {
+				// Largest child first (the group's lanes all compute the same list).
+				uint32_t C[8];
+				int nc = 1;
+				C[0] = r;
+				while (nc < 8) {
+					int best = -1;
+					float best_area = -1.0f;
+					for (int c = 0; c < nc; ++c) {
+						const float ac = (C[c] & kLeaf16) ? -1.0f : crow[C[c]];
+						if (ac > best_area) {
+							best_area = ac;
+							best = c;
+						}
+					}
+					if (best < 0)
+						break;
+					const uint32_t x = C[best];
+					C[best] = lr_s[x] & 0xFFFFu;
+					C[nc++] = lr_s[x] >> 16;
 				}
-				n_inner += in ? 1u : 0u;
-				n_tris += in ? 0u : nz;
+				has = (int)c8 < nc;
+				for (int c = 0; c < 8; ++c)
+					if ((uint32_t)c == c8 && has)
+						y = C[c];
 			}
+			// This lane's child (slot k): its count, whether it becomes a node, and its box
+			// (loaded now: the wait overlaps the scan).  A binary node's box comes from its
+			// record, a single triangle's from the leaf-box array.
+			uint32_t nz = 0;
+			bool in = false;
+			const float4 none = make_float4(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000),
+			                                __int_as_float(0x7FC00000), 0.f);
+			float4 lo = none, hi = none;
+			if (has) {
+				nz = (y & kLeaf16) ? 1u : cnt_s[y];
+				in = child_inner(y, nz, leaf_size, use_cost, bits_s);
+				const float4 *src = (y & kLeaf16) ? lbox + 2 * (y & ~kLeaf16) : ibox + 2 * y;
+				lo = __ldcg(src);
+				hi = __ldcg(src + 1);
+			}
+			// Inner children and triangles before this one, and the group's totals (lane
+			// order is child order).
+			const uint32_t gsh = lane & 24u;
+			const uint32_t nc = __popc((__ballot_sync(0xFFFFFFFFu, has) >> gsh) & 0xFFu);
+			const uint32_t inm = (__ballot_sync(0xFFFFFFFFu, has && in) >> gsh) & 0xFFu;
+			const uint32_t my_inner = __popc(inm & ((1u << c8) - 1u)), n_inner = __popc(inm);
+			const uint32_t mine_t = (has && !in) ? nz : 0u;
+			uint32_t tsum = mine_t;
+#pragma unroll
+			for (uint32_t o = 1; o < 8u; o <<= 1) {
+				const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, tsum, o, 8);
+				if (c8 >= o)
+					tsum += v;
+			}
+			const uint32_t n_tris = __shfl_sync(0xFFFFFFFFu, tsum, gsh | 7u);
+			const uint32_t my_tris = tsum - mine_t;
 			uint32_t total;
 			const uint32_t pre = block_scan(c8 == 0u ? (n_inner | (n_tris << 16)) : 0u, scan, total);
-			const uint32_t pg = __shfl_sync(0xFFFFFFFFu, pre, lane & 24u); // the group's lane 0
+			const uint32_t pg = __shfl_sync(0xFFFFFFFFu, pre, gsh); // the group's lane 0
 			const uint32_t nb = n_nodes + (pg & 0xFFFFu), ob = next_items + (pg & 0xFFFFu);
 			const uint32_t tb = n_placed + (pg >> 16);
 			const bool fits = nb + n_inner <= node_cap && ob + n_inner <= kSmallMax &&
@@ -599,12 +642,9 @@ __global__ void __launch_bounds__(kThreads, 1)
 			if (live && !fits && c8 == 0u)
 				atomicOr(err, kErrCollapse);
 			if (live && fits) {
-				float4 lo = make_float4(__int_as_float(0x7FC00000), __int_as_float(0x7FC00000),
-				                        __int_as_float(0x7FC00000), 0.f),
-				       hi = lo;
-				uint32_t ref = kNone;
-				if (mine) {
-					if (inner_y) {
+				if (has) {
+					uint32_t ref;
+					if (in) {
 						ref = nb + my_inner;
 						fout[ob + my_inner] = y | (ref << 16);
 					} else {
@@ -612,7 +652,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 						// leaf_size <= 8) go to the permutation; the triangles are copied
 						// after the last level, all at once.
 						uint32_t dst = tb + my_tris;
-						ref = make_leaf(dst, cnt_y);
+						ref = make_leaf(dst, nz);
 						uint32_t stack[8];
 						int sp = 0;
 						stack[sp++] = y;
@@ -628,22 +668,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 							}
 						}
 					}
-					// The child's box: a binary node's from its record, a single
-					// triangle's from the leaf-box array (one wait per level step).
-					const float4 *src = (y & kLeaf16) ? lbox + 2 * (y & ~kLeaf16) : ibox + 2 * y;
-					lo = __ldcg(src);
-					hi = __ldcg(src + 1);
+					nodes[slot].c[k] = make_child(lo, hi, ref);
 				}
-				Child8 ch;
-				ch.lo_x = lo.x;
-				ch.lo_y = lo.y;
-				ch.lo_z = lo.z;
-				ch.ref = ref;
-				ch.hi_x = hi.x;
-				ch.hi_y = hi.y;
-				ch.hi_z = hi.z;
-				ch.pad = 0u;
-				nodes[slot].c[c8] = ch;
+				if (c8 >= nc) // the slots after the last child
+					nodes[slot].c[c8] = make_child(none, none, kNone);
 			}
 			n_nodes += total & 0xFFFFu;
 			next_items += total & 0xFFFFu;
