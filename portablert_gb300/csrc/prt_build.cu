@@ -1083,14 +1083,13 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 		msg = "the SAH build reads its level counters on the host";
 		return PRT_ERR_ARG;
 	}
-	BUILD_TRY(write_dead_node(plan, sc, st));
 	if (plan.small) {
-		// One block: PLOC, collapse and re-layout in one launch; the compression reads the
-		// node count on the device, so the host waits once, at the end.
+		// One block: PLOC, collapse and re-layout in one launch, which also zeroes the
+		// counters and writes the empty node; the compression reads the node count on the
+		// device, so the host waits once, at the end.
 		uint32_t *ctr = ws.counters.as<uint32_t>();
-		BUILD_TRY(cudaMemsetAsync(ctr, 0, 4 * kCtrWords, st));
-		BUILD_TRY(launch_build_small(d_tris, n, (uint32_t)plan.leaf_size, plan.collapse_cost, ws,
-		                             sc, plan.node_cap, ctr, d_err, st));
+		BUILD_TRY(launch_build_small(d_tris, n, (uint32_t)plan.leaf_size, plan.collapse_cost,
+		                             plan.compressed, ws, sc, plan.node_cap, ctr, d_err, st));
 		sc.built_small = true;
 		if (plan.compressed) {
 			k_compress<<<blocks_for(8ull * plan.node_cap, 256), 256, 0, st>>>(
@@ -1100,6 +1099,7 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 		BUILD_TRY(cudaGetLastError());
 		return host_checks ? build_finish(sc, ws, st, msg) : PRT_OK;
 	}
+	BUILD_TRY(write_dead_node(plan, sc, st));
 	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
 	uint32_t *d_ioff = ws.int_off.as<uint32_t>();
 	uint32_t *scene_of = plan.multi ? ws.scene_of.as<uint32_t>() : nullptr;

@@ -157,10 +157,11 @@ int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed,
 
 // The one-block build (prt_build_small.cu): the largest scene it takes, and its launch
 // (PLOC binary tree, collapse, triangle re-layout; the level counters at `ctr` end as
-// the multi-launch build leaves them).
+// the multi-launch build leaves them; it also writes the empty node at sc.dead, in
+// cnodes too when `compressed`).
 uint32_t small_build_max();
 cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
-                               BuildScratch &ws, SceneGPU &sc, uint32_t node_cap, uint32_t *ctr,
-                               uint32_t *d_err, cudaStream_t st);
+                               bool compressed, BuildScratch &ws, SceneGPU &sc, uint32_t node_cap,
+                               uint32_t *ctr, uint32_t *d_err, cudaStream_t st);
 
 } // namespace prt

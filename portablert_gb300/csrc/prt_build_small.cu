@@ -197,6 +197,26 @@ __device__ __forceinline__ Child8 make_child(float4 lo, float4 hi, uint32_t ref)
 	return ch;
 }
 
+// Exclusive prefix over the warps of one value per warp (lane 0's), and the total, with
+// one barrier.  The caller separates two calls with a __syncthreads.
+static_assert(kThreads == 32 * 32, "one scan word per warp, one warp of them");
+__device__ __forceinline__ uint32_t warp_totals_scan(uint32_t v, uint32_t *words, uint32_t &total) {
+	const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+	if (lane == 0u)
+		words[warp] = v;
+	__syncthreads();
+	const uint32_t own = words[lane];
+	uint32_t x = own;
+#pragma unroll
+	for (int o = 1; o < 32; o <<= 1) {
+		const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+		if (lane >= (uint32_t)o)
+			x += y;
+	}
+	total = __shfl_sync(0xFFFFFFFFu, x, 31);
+	return __shfl_sync(0xFFFFFFFFu, x - own, warp);
+}
+
 // Whether child y (16-bit reference) of an 8-wide node becomes a node of its own.
 __device__ __forceinline__ bool child_inner(uint32_t y, uint32_t count, uint32_t leaf_size,
                                             int use_cost, const uint32_t *bits) {
@@ -208,13 +228,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                   float4 *__restrict__ ibox, float4 *__restrict__ lbox, uint32_t *__restrict__ lr,
                   CostNode *__restrict__ cost, Node8 *__restrict__ nodes, uint32_t node_cap,
                   float4 *__restrict__ tri4, uint32_t *__restrict__ inv, uint32_t *__restrict__ ctr,
-                  uint32_t *__restrict__ err) {
+                  Node8 *__restrict__ dead, CNode8 *__restrict__ cdead, uint32_t *__restrict__ err) {
 	extern __shared__ __align__(16) unsigned char sm[];
 	uint32_t *scan = reinterpret_cast<uint32_t *>(sm + kOffScan);
 	const uint32_t tid = threadIdx.x;
 	float *box = reinterpret_cast<float *>(sm + kOffBox);
 	uint32_t *word = reinterpret_cast<uint32_t *>(sm + kOffWord);
 	float *crow = reinterpret_cast<float *>(sm + kOffCost);
+	// The counters start at zero; the empty node (NaN boxes, no references; compressed:
+	// no masks, no counts) is written here rather than by separate copies.
+	if (tid < (uint32_t)kCtrWords)
+		ctr[tid] = 0u;
+	if (tid < sizeof(Node8) / 4u)
+		reinterpret_cast<uint32_t *>(dead)[tid] = 0xFFFFFFFFu;
+	if (cdead && tid < sizeof(CNode8) / 4u)
+		reinterpret_cast<uint32_t *>(cdead)[tid] = 0u;
 
 	// 1. One pass over the triangles: boxes (input order, into the cost rows, and to the
 	// leaf-box array for the collapse), centroids kept for the keys; centroid bounds of
@@ -286,9 +314,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 		}
 		__syncthreads();
 	}
-	uint32_t P = 2;
-	while (P < n)
-		P <<= 1;
 	unsigned long long *keys = reinterpret_cast<unsigned long long *>(sm + kOffBox);
 	{
 		float lo[3], sc[3];
@@ -302,9 +327,6 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
 		for (int k = 0; k < kPer; ++k) {
 			const uint32_t i = tid + (uint32_t)k * kThreads;
-			if (i >= P)
-				continue;
-			unsigned long long key = ~0ull;
 			if (i < n) {
 				uint32_t code = 0;
 				if (cfin[k] && any) {
@@ -314,25 +336,78 @@ __global__ void __launch_bounds__(kThreads, 1)
 						qv[q] = (uint32_t)fminf(fmaxf((cen[k][q] - lo[q]) * sc[q], 0.0f), 1023.0f);
 					code = (spread10(qv[0]) << 2) | (spread10(qv[1]) << 1) | spread10(qv[2]);
 				}
-				key = ((unsigned long long)code << 32) | i;
+				keys[i] = ((unsigned long long)code << 32) | i;
 			}
-			keys[i] = key;
 		}
 	}
 	__syncthreads();
-	for (uint32_t size = 2; size <= P; size <<= 1)
-		for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
-			const uint32_t ls = (uint32_t)__ffs((int)stride) - 1u; // log2(stride)
-			for (uint32_t t = tid; t < P / 2; t += kThreads) {
-				const uint32_t i = ((t >> ls) << (ls + 1u)) | (t & (stride - 1u)), j = i + stride;
-				const unsigned long long a = keys[i], b = keys[j];
-				if ((a > b) == ((i & size) == 0u)) {
-					keys[i] = b;
-					keys[j] = a;
+	// LSD radix sort of the keys by code, 8 bits a pass; each pass is stable, so equal
+	// codes keep index order (the order of the keys' low words).  Warp w holds positions
+	// 128w .. 128w + 127, round r at 128w + 32r + lane: a key's rank among the warp's keys
+	// of its digit comes from ballots, round by round; the digit's start for the warp
+	// from one scan over the counts in (digit, warp) order.
+	{
+		// Warp w's count of digit d at hist[w * 257 + d]: a warp's 32 lanes, on different
+		// digits, and a scan thread's 8 warps, on one digit, fall in different banks.
+		uint32_t *hist = reinterpret_cast<uint32_t *>(sm + kOffBox) + 2u * kSmallMax;
+		const uint32_t warp = tid >> 5, lane = tid & 31u, below = (1u << lane) - 1u;
+		unsigned long long kv[kPer];
+#pragma unroll
+		for (int r = 0; r < kPer; ++r) {
+			const uint32_t p = 128u * warp + 32u * (uint32_t)r + lane;
+			kv[r] = p < n ? keys[p] : 0ull;
+		}
+		for (uint32_t shift = 32; shift < 62; shift += 8) {
+			for (uint32_t j = tid; j < 32u * 257u; j += kThreads)
+				hist[j] = 0u;
+			__syncthreads();
+			uint32_t dg[kPer], rank[kPer];
+#pragma unroll
+			for (int r = 0; r < kPer; ++r) {
+				const bool valid = 128u * warp + 32u * (uint32_t)r + lane < n;
+				dg[r] = valid ? (uint32_t)(kv[r] >> shift) & 255u : 256u;
+				// The lanes whose digit equals this lane's, one ballot per digit bit.
+				uint32_t same = 0xFFFFFFFFu;
+#pragma unroll
+				for (int b = 0; b < 9; ++b) {
+					const uint32_t v = __ballot_sync(0xFFFFFFFFu, (dg[r] >> b) & 1u);
+					same &= ((dg[r] >> b) & 1u) ? v : ~v;
 				}
+				const uint32_t base = valid ? hist[257u * warp + dg[r]] : 0u;
+				__syncwarp();
+				if (valid && (same & below) == 0u) // the lowest lane of its digit
+					hist[257u * warp + dg[r]] = base + __popc(same);
+				__syncwarp();
+				rank[r] = base + __popc(same & below);
 			}
 			__syncthreads();
+			// Counts in (digit, warp) order: thread t has digit t / 4, warps 8 (t % 4) + j.
+			const uint32_t sd = tid >> 2, sw = 8u * (tid & 3u);
+			uint32_t c[8], sum = 0, total;
+#pragma unroll
+			for (int j = 0; j < 8; ++j) {
+				c[j] = hist[257u * (sw + (uint32_t)j) + sd];
+				sum += c[j];
+			}
+			uint32_t run = block_scan(sum, scan, total); // every count read before the writes
+#pragma unroll
+			for (int j = 0; j < 8; ++j) {
+				hist[257u * (sw + (uint32_t)j) + sd] = run;
+				run += c[j];
+			}
+			__syncthreads();
+#pragma unroll
+			for (int r = 0; r < kPer; ++r)
+				if (dg[r] < 256u)
+					keys[hist[257u * warp + dg[r]] + rank[r]] = kv[r];
+			__syncthreads();
+#pragma unroll
+			for (int r = 0; r < kPer; ++r) {
+				const uint32_t p = 128u * warp + 32u * (uint32_t)r + lane;
+				kv[r] = p < n ? keys[p] : 0ull;
+			}
 		}
+	}
 
 	// 2. Leaves in Morton order (boxes gathered from the cost rows), then PLOC.
 	{
@@ -390,47 +465,49 @@ __global__ void __launch_bounds__(kThreads, 1)
 			word[i] = (word[i] & ~(kNnMask << kNnShift)) | (bj << kNnShift);
 		}
 		__syncthreads();
-		// (b) Survivors and merges over contiguous chunks of kPer positions per thread,
-		// packed (kept | merges << 16) for one scan.  Survivor r is staged at index
-		// made + merged + r of the cost rows (boxes in rows 0-5, words in row 6: nodes
-		// not made yet, and kept <= n - made - merged of them are free); a merge's
-		// position and rank are listed in row 6 of the node it makes.
-		uint32_t keepm = 0, mergem = 0, local = 0;
+		// (b) Survivors and merges.  Warp w takes positions 128w .. 128w + 127, round k at
+		// 128w + 32k + lane; ballots give each position's rank within its warp, one scan
+		// of the warps' totals (kept | merges << 16) the warps' starts.  Survivor r is
+		// staged at index made + merged + r of the cost rows (boxes in rows 0-5, words in
+		// row 6: nodes not made yet, and kept <= n - made - merged of them are free); a
+		// merge's position and rank are listed in row 6 of the node it makes.
+		const uint32_t wp = tid >> 5, ln = tid & 31u, below = (1u << ln) - 1u;
+		uint32_t bk[kPer], bm[kPer], wsum = 0;
 #pragma unroll
 		for (int k = 0; k < kPer; ++k) {
-			const uint32_t i = tid * (uint32_t)kPer + (uint32_t)k;
+			const uint32_t i = 128u * wp + 32u * (uint32_t)k + ln;
+			bool keep = false, merge = false;
 			if (i < m) {
 				const uint32_t j = (word[i] >> kNnShift) & kNnMask;
 				const bool mutual = ((word[j] >> kNnShift) & kNnMask) == i;
-				if (!(mutual && i > j)) {
-					keepm |= 1u << k;
-					local += 1u;
-					if (mutual && i < j) {
-						mergem |= 1u << k;
-						local += 0x10000u;
-					}
-				}
+				keep = !(mutual && i > j);
+				merge = mutual && i < j;
 			}
+			bk[k] = __ballot_sync(0xFFFFFFFFu, keep);
+			bm[k] = __ballot_sync(0xFFFFFFFFu, merge);
+			wsum += (uint32_t)__popc(bk[k]) | ((uint32_t)__popc(bm[k]) << 16);
 		}
 		uint32_t total;
-		const uint32_t pre = block_scan(local, scan, total);
+		const uint32_t wpre = warp_totals_scan(wsum, scan, total);
 		const uint32_t kept = total & 0xFFFFu, merged = total >> 16;
 		uint32_t *stage_w = list; // row 6
 		const uint32_t tbase = made + merged;
 		{
-			uint32_t q = made + (pre >> 16), pos = pre & 0xFFFFu;
+			uint32_t pos0 = wpre & 0xFFFFu, q0 = made + (wpre >> 16);
 #pragma unroll
 			for (int k = 0; k < kPer; ++k) {
-				if (!((keepm >> k) & 1u))
-					continue;
-				const uint32_t i = tid * (uint32_t)kPer + (uint32_t)k;
-				if ((mergem >> k) & 1u) {
-					list[q++] = i | (pos << 16);
-				} else {
-					store_box(crow, tbase + pos, load_box(box, i));
-					stage_w[tbase + pos] = word[i];
+				const uint32_t i = 128u * wp + 32u * (uint32_t)k + ln;
+				if ((bk[k] >> ln) & 1u) {
+					const uint32_t pos = pos0 + __popc(bk[k] & below);
+					if ((bm[k] >> ln) & 1u) {
+						list[q0 + __popc(bm[k] & below)] = i | (pos << 16);
+					} else {
+						store_box(crow, tbase + pos, load_box(box, i));
+						stage_w[tbase + pos] = word[i];
+					}
 				}
-				++pos;
+				pos0 += __popc(bk[k]);
+				q0 += __popc(bm[k]);
 			}
 		}
 		__syncthreads();
@@ -449,9 +526,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 				float cl[8], cr[8];
 				row_costs(a, crow, cl);
 				row_costs(c, crow, cr);
-				const CostNode cn = merge_costs(cl, cr, half_extent(box_lo(bi), box_hi(bi)),
-				                                half_extent(box_lo(bj), box_hi(bj)),
-				                                half_extent(box_lo(u), box_hi(u)), count, leaf_size);
+				const CostNode cn = merge_costs<true>(cl, cr, half_extent(box_lo(bi), box_hi(bi)),
+				                                      half_extent(box_lo(bj), box_hi(bj)),
+				                                      half_extent(box_lo(u), box_hi(u)), count,
+				                                      leaf_size);
 				crow[node] = cn.c1;
 #pragma unroll
 				for (uint32_t s = 2; s < 8; ++s) // row 6 last: this merge's list entry
@@ -737,8 +815,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 uint32_t small_build_max() { return kSmallMax; }
 
 cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
-                               BuildScratch &ws, SceneGPU &sc, uint32_t node_cap, uint32_t *ctr,
-                               uint32_t *d_err, cudaStream_t st) {
+                               bool compressed, BuildScratch &ws, SceneGPU &sc, uint32_t node_cap,
+                               uint32_t *ctr, uint32_t *d_err, cudaStream_t st) {
 	// The shared-memory limit is a per-device attribute: set once per device.
 	static std::atomic<uint32_t> attr_set{0};
 	int dev = 0;
@@ -756,7 +834,9 @@ cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_si
 	k_build_small<<<1, kThreads, kSmemBytes, st>>>(
 	    d_tris, n, leaf_size, use_cost ? 1 : 0, ws.ibox.as<float4>(), ws.lbox.as<float4>(),
 	    ws.left.as<uint32_t>(), use_cost ? ws.cost.as<CostNode>() : nullptr,
-	    sc.nodes.as<Node8>(), node_cap, sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr, d_err);
+	    sc.nodes.as<Node8>(), node_cap, sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr,
+	    sc.nodes.as<Node8>() + sc.dead, compressed ? sc.cnodes.as<CNode8>() + sc.dead : nullptr,
+	    d_err);
 	return cudaGetLastError();
 }
 

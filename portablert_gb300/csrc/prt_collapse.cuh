@@ -82,14 +82,34 @@ __device__ __forceinline__ void node_costs(const CostNode &c, float cs[8]) {
 		cs[j] = fminf(c.c1, c.cd[j - 2]);
 }
 
+// Surface area of a box of half extents e in units of unit^2, given 1 / unit (0 when
+// unit is not positive): multiplications instead of divisions, rounded differently.
+__device__ __forceinline__ float scaled_area_rcp(float3 e, float rcp) {
+	const float x = fminf(e.x * rcp, 1.0f), y = fminf(e.y * rcp, 1.0f), z = fminf(e.z * rcp, 1.0f);
+	return x * y + x * z + y * z;
+}
+
 // The cost record of a binary node of `count` triangles from its children's costs (cl,
 // cr: in units of each child's own area) and the half extents of the three boxes.
+// kRcp: the area ratios from two reciprocals instead of eleven divisions (the one-block
+// build, whose merges are a chain of dependent work on one SM); the decisions may then
+// differ from the divided ones where two costs differ in the last bits.
+template <bool kRcp = false>
 __device__ __forceinline__ CostNode merge_costs(float cl[8], float cr[8], float3 el, float3 er,
                                                 float3 ep, uint32_t count, uint32_t leaf_size) {
 	const float unit = fmaxf(ep.x, fmaxf(ep.y, ep.z));
-	const float ap = scaled_area(ep, unit);
-	const float rl = ap > 0.0f ? fminf(scaled_area(el, unit) / ap, 1.0f) : 0.0f;
-	const float rr = ap > 0.0f ? fminf(scaled_area(er, unit) / ap, 1.0f) : 0.0f;
+	float ap, rl, rr;
+	if (kRcp) {
+		const float ru = unit > 0.0f ? 1.0f / unit : 0.0f;
+		ap = scaled_area_rcp(ep, ru);
+		const float ra = ap > 0.0f ? 1.0f / ap : 0.0f;
+		rl = fminf(scaled_area_rcp(el, ru) * ra, 1.0f);
+		rr = fminf(scaled_area_rcp(er, ru) * ra, 1.0f);
+	} else {
+		ap = scaled_area(ep, unit);
+		rl = ap > 0.0f ? fminf(scaled_area(el, unit) / ap, 1.0f) : 0.0f;
+		rr = ap > 0.0f ? fminf(scaled_area(er, unit) / ap, 1.0f) : 0.0f;
+	}
 #pragma unroll
 	for (int j = 1; j < 8; ++j) {
 		cl[j] *= rl;
