@@ -197,6 +197,63 @@ __device__ __forceinline__ Child8 make_child(float4 lo, float4 hi, uint32_t ref)
 	return ch;
 }
 
+// Position i's nearest neighbour within kRadius positions among m clusters: the least
+// pair in the order (union area, distance, parity of the lower position, lower position;
+// the last three as fields of 4, 1 and 12 bits), a total order, so the loop's order does
+// not matter; unrolled, so the neighbours' boxes load together.
+__device__ __forceinline__ uint32_t nearest(const float *box, uint32_t i, uint32_t m) {
+	const Box bi = load_box(box, i);
+	float best = INFINITY;
+	uint32_t best_tb = 0xFFFFFFFFu, bj = i;
+#pragma unroll
+	for (int o = -kRadius; o <= kRadius; ++o) {
+		const int jj = (int)i + o;
+		if (o == 0 || jj < 0 || jj >= (int)m)
+			continue;
+		const uint32_t j = (uint32_t)jj, low = min(i, j);
+		const float d = union_area(bi, load_box(box, j));
+		const uint32_t tb = ((uint32_t)(o < 0 ? -o : o) << 13) | ((low & 1u) << 12) | low;
+		if (d < best || (d == best && tb < best_tb)) {
+			best = d;
+			best_tb = tb;
+			bj = j;
+		}
+	}
+	return bj;
+}
+
+// Binary node `node` over clusters (bi, wi) and (bj, wj): its cost rows (row 0: its area
+// for the largest-child-first collapse), slot splits, children, box and count.  Returns
+// the node's cluster word; u gets its box.
+__device__ __forceinline__ uint32_t make_node(uint32_t node, const Box &bi, const Box &bj,
+                                              uint32_t wi, uint32_t wj, int use_cost,
+                                              uint32_t leaf_size, float *crow, CostNode *cost,
+                                              uint32_t *lr, float4 *ibox, Box &u) {
+	u = join(bi, bj);
+	const uint32_t a = wi & 0xFFFFu, c = wj & 0xFFFFu;
+	const uint32_t count = min((wi >> kCntShift) + (wj >> kCntShift), kCntMax);
+	const float area = half_area(box_lo(u), box_hi(u));
+	if (use_cost) {
+		float cl[8], cr[8];
+		row_costs(a, crow, cl);
+		row_costs(c, crow, cr);
+		const CostNode cn = merge_costs<true>(cl, cr, half_extent(box_lo(bi), box_hi(bi)),
+		                                      half_extent(box_lo(bj), box_hi(bj)),
+		                                      half_extent(box_lo(u), box_hi(u)), count, leaf_size);
+		crow[node] = cn.c1;
+#pragma unroll
+		for (uint32_t s = 2; s < 8; ++s)
+			crow[(s - 1u) * kSmallMax + node] = fminf(cn.c1, cn.cd[s - 2u]);
+		cost[node].bits = cn.bits;
+	} else {
+		crow[node] = area;
+	}
+	lr[node] = a | (c << 16);
+	ibox[2 * node] = make_float4(u.lx, u.ly, u.lz, area);
+	ibox[2 * node + 1] = make_float4(u.hx, u.hy, u.hz, __uint_as_float(count));
+	return node | (count << kCntShift);
+}
+
 // Exclusive prefix over the warps of one value per warp (lane 0's), and the total, with
 // one barrier.  The caller separates two calls with a __syncthreads.
 static_assert(kThreads == 32 * 32, "one scan word per warp, one warp of them");
@@ -434,34 +491,12 @@ __global__ void __launch_bounds__(kThreads, 1)
 	__syncthreads();
 	uint32_t *list = reinterpret_cast<uint32_t *>(crow + 6u * kSmallMax);
 	uint32_t m = n, made = 0;
-	for (uint32_t iter = 0; m > 1; ++iter) {
+	uint32_t iter = 0;
+	for (; m > 32u; ++iter) { // the last 32 clusters merge in one warp (below)
 		// (a) Each cluster's nearest neighbour, into its word.
 		for (uint32_t i = tid; i < m; i += kThreads) {
-			uint32_t bj;
-			if (iter >= kPlocRounds) {
-				bj = (i ^ 1u) < m ? (i ^ 1u) : i; // the last of odd m stays
-			} else {
-				const Box bi = load_box(box, i);
-				const uint32_t lo = i > (uint32_t)kRadius ? i - kRadius : 0u;
-				const uint32_t hi = min(m - 1u, i + (uint32_t)kRadius);
-				float best = INFINITY;
-				uint32_t best_tb = 0xFFFFFFFFu;
-				bj = i;
-				for (uint32_t j = lo; j <= hi; ++j) {
-					if (j == i)
-						continue;
-					const float d = union_area(bi, load_box(box, j));
-					// Tie-break of the pair {i, j}: distance, parity of the lower
-					// position, lower position (fields of 4, 1 and 12 bits).
-					const uint32_t low = min(i, j);
-					const uint32_t tb = ((j > i ? j - i : i - j) << 13) | ((low & 1u) << 12) | low;
-					if (d < best || (d == best && tb < best_tb)) {
-						best = d;
-						best_tb = tb;
-						bj = j;
-					}
-				}
-			}
+			const uint32_t bj = iter >= kPlocRounds ? ((i ^ 1u) < m ? (i ^ 1u) : i) // odd m: last stays
+			                                        : nearest(box, i, m);
 			word[i] = (word[i] & ~(kNnMask << kNnShift)) | (bj << kNnShift);
 		}
 		__syncthreads();
@@ -516,33 +551,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 		// position belongs to one pair, and nothing writes the clusters until (d).
 		for (uint32_t q = tid; q < merged; q += kThreads) {
 			const uint32_t node = made + q;
-			const uint32_t e = list[node], i = e & 0xFFFFu, pos = e >> 16;
+			const uint32_t e = list[node], i = e & 0xFFFFu, pos = e >> 16; // before row 6 is written
 			const uint32_t wi = word[i], j = (wi >> kNnShift) & kNnMask, wj = word[j];
-			const Box bi = load_box(box, i), bj = load_box(box, j), u = join(bi, bj);
-			const uint32_t a = wi & 0xFFFFu, c = wj & 0xFFFFu;
-			const uint32_t count = min((wi >> kCntShift) + (wj >> kCntShift), kCntMax);
-			const float area = half_area(box_lo(u), box_hi(u));
-			if (use_cost) {
-				float cl[8], cr[8];
-				row_costs(a, crow, cl);
-				row_costs(c, crow, cr);
-				const CostNode cn = merge_costs<true>(cl, cr, half_extent(box_lo(bi), box_hi(bi)),
-				                                      half_extent(box_lo(bj), box_hi(bj)),
-				                                      half_extent(box_lo(u), box_hi(u)), count,
-				                                      leaf_size);
-				crow[node] = cn.c1;
-#pragma unroll
-				for (uint32_t s = 2; s < 8; ++s) // row 6 last: this merge's list entry
-					crow[(s - 1u) * kSmallMax + node] = fminf(cn.c1, cn.cd[s - 2u]);
-				cost[node].bits = cn.bits;
-			} else {
-				crow[node] = area;
-			}
-			lr[node] = a | (c << 16);
-			ibox[2 * node] = make_float4(u.lx, u.ly, u.lz, area);
-			ibox[2 * node + 1] = make_float4(u.hx, u.hy, u.hz, __uint_as_float(count));
+			Box u;
+			const uint32_t w = make_node(node, load_box(box, i), load_box(box, j), wi, wj, use_cost,
+			                             leaf_size, crow, cost, lr, ibox, u);
 			store_box(crow, tbase + pos, u);
-			stage_w[tbase + pos] = node | (count << kCntShift);
+			stage_w[tbase + pos] = w;
 		}
 		__syncthreads();
 		// (d) The staged survivors become clusters 0 .. kept - 1.
@@ -558,6 +573,65 @@ __global__ void __launch_bounds__(kThreads, 1)
 			return;
 		}
 		__syncthreads();
+	}
+	// The last clusters (at most 32: about the last ten iterations) in warp 0, one per
+	// lane, with warp barriers: each merging lane makes its node, every survivor moves
+	// to its rank once all have read.  The other warps wait at the barrier after.
+	if (m > 1u) {
+		if (tid < 32u) {
+			const uint32_t i = tid, below = (1u << i) - 1u;
+			uint32_t failed = 0;
+			for (; m > 1u; ++iter) {
+				const bool act = i < m;
+				if (act) {
+					const uint32_t bj = iter >= kPlocRounds ? ((i ^ 1u) < m ? (i ^ 1u) : i)
+					                                        : nearest(box, i, m);
+					word[i] = (word[i] & ~(kNnMask << kNnShift)) | (bj << kNnShift);
+				}
+				__syncwarp();
+				bool keep = false, merge = false;
+				uint32_t j = i, wi = 0;
+				if (act) {
+					wi = word[i];
+					j = (wi >> kNnShift) & kNnMask;
+					const bool mutual = ((word[j] >> kNnShift) & kNnMask) == i;
+					keep = !(mutual && i > j);
+					merge = mutual && i < j;
+				}
+				const uint32_t bk = __ballot_sync(0xFFFFFFFFu, keep);
+				const uint32_t bm = __ballot_sync(0xFFFFFFFFu, merge);
+				Box ub;
+				uint32_t uw = wi;
+				if (merge)
+					uw = make_node(made + __popc(bm & below), load_box(box, i), load_box(box, j), wi,
+					               word[j], use_cost, leaf_size, crow, cost, lr, ibox, ub);
+				else if (keep)
+					ub = load_box(box, i);
+				__syncwarp(); // every cluster read before any moves
+				if (keep) {
+					const uint32_t pos = __popc(bk & below);
+					store_box(box, pos, ub);
+					word[pos] = uw;
+				}
+				__syncwarp();
+				made += (uint32_t)__popc(bm);
+				m = (uint32_t)__popc(bk);
+				if (bm == 0u || iter >= n) { // cannot happen (see above); reported, not looped
+					failed = 1u;
+					break;
+				}
+			}
+			if (i == 0u) {
+				scan[0] = made;
+				scan[1] = failed;
+				if (failed)
+					atomicOr(err, kErrCollapse);
+			}
+		}
+		__syncthreads();
+		made = scan[0];
+		if (scan[1])
+			return;
 	}
 
 	// 3. The 8-wide collapse from shared-memory copies of the binary nodes: eight lanes
