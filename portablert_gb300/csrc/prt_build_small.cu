@@ -42,7 +42,7 @@ namespace prt {
 
 namespace {
 
-constexpr uint32_t kSmallMax = 4096; // triangles; a power of two (the sort's size)
+constexpr uint32_t kSmallMax = 4096; // triangles: four positions per thread
 constexpr int kThreads = 1024;
 #ifndef PRT_PLOC_RADIUS
 #define PRT_PLOC_RADIUS 3 // 3 / 4 / 6 / 8 / 12 measured: 3 fastest, and no worse a tree
@@ -61,13 +61,13 @@ static_assert((uint32_t)kMaxLeaf < kCntMax, "saturated counts must exceed every 
 // Shared memory, in rows of one word per triangle.  PLOC: the clusters' boxes (six rows,
 // structure of arrays), their words, and seven rows of the binary nodes' costs in 1..7
 // child slots (row k - 1 for k slots; row 0 holds the area for the largest-child-first
-// collapse).  Before PLOC the sort's keys take the box rows and the triangles' boxes in
-// input order the cost rows; within an iteration, row 6 of the nodes it is about to make
-// lists its merges, and the rows of the nodes after those stage its survivors.
-// Collapse, over the box and word rows: the leaf permutation, the binary nodes'
-// children, slot splits and counts, two frontiers and the groups' exchange words (the
-// cost rows stay).  Re-layout: the permutation, then the triangles as loaded.  The
-// block-scan words last.
+// collapse).  Before PLOC the sort's keys and per-warp digit counts take the box rows
+// and the triangles' boxes in input order the cost rows; within an iteration, row 6 of
+// the nodes it is about to make lists its merges, and the rows of the nodes after those
+// stage its survivors.  Collapse, over the box and word rows: the leaf permutation, the
+// binary nodes' children, slot splits and counts, two frontiers and the groups' exchange
+// words (the cost rows stay).  Re-layout: the permutation, then the triangles as
+// loaded.  The block-scan words last.
 constexpr uint32_t kRow = 4u * kSmallMax;
 constexpr uint32_t kOffBox = 0;
 constexpr uint32_t kOffWord = 6u * kRow;
@@ -85,6 +85,7 @@ constexpr uint32_t kOffStage = kOffPerm + 2u * kSmallMax; // 9 words per triangl
 static_assert(kOffXch + 4u * kThreads <= kOffCost, "collapse tables overlap the cost rows");
 static_assert(kOffStage + 36u * kSmallMax <= kOffScan, "staged triangles overlap the scan words");
 static_assert(kSmemBytes <= 232448u, "more shared memory than a block can have");
+static_assert(8u * kSmallMax + 4u * 32u * 257u <= kOffWord, "sort keys and counts overlap the words");
 constexpr int kPer = (int)(kSmallMax / kThreads); // positions per thread
 
 struct Box {
