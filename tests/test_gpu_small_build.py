@@ -1,9 +1,10 @@
 """The one-block build of small scenes (option build_small, prt_build_small.cu: Morton
 order, PLOC, the collapse and the re-layout in one launch): every field of every record
 equals the oracle's exhaustive search and the binned-SAH build's records, at sizes from 1
-to the largest it takes (4,096), for both collapses, leaf sizes 1 and 8 and both node
-formats; identical and non-finite triangles; a scene of 4,097 triangles goes to the
-binned-SAH build; a chain too deep for the traversal falls back to the LBVH."""
+to the largest it takes (4,096), for both collapses, leaf sizes 1 to 8 and both node
+formats; identical and non-finite triangles, equal Morton codes, points, segments and a
+flat scene; a scene of 4,097 triangles goes to the binned-SAH build; a chain too deep
+for the traversal falls back to the LBVH."""
 import numpy as np
 import pytest
 
@@ -132,3 +133,38 @@ def test_chain_scene(small, oracle_lib):
     got = small.nearest_hits(rays, TAGS)
     _same(got, oracle_lib.brute_force(tris, rays))
     assert (got["valid"] != 0).sum() > 100
+
+
+@pytest.mark.parametrize("n", [37, 4096])
+def test_every_leaf_size(small, oracle_lib, n):
+    """Leaf sizes 2 to 7 (1 and 8 above): leaves of several triangles take the counts the
+    clusters carry (exact up to the largest leaf) and the permutation's subtree walk."""
+    tris = W.soup_tris(9800 + n, n)
+    rays = W.soup_rays(9801 + n, 2000)
+    want = oracle_lib.brute_force(tris, rays)
+    for leaf in range(2, 8):
+        small.set_option("leaf_size", leaf)
+        small.set_tris(tris)
+        assert small.stat("build_small") == 1.0
+        _same(small.nearest_hits(rays, TAGS), want)
+
+
+def test_morton_ties_and_degenerate_triangles(small, oracle_lib):
+    """Groups of triangles with one centroid (equal Morton codes, which the sort keeps in
+    index order), zero-area triangles (points and segments) and a flat scene (one axis of
+    zero extent, so every code has one coordinate's bits zero)."""
+    rng = np.random.default_rng(77)
+    base = W.soup_tris(78, 512)
+    tris = np.concatenate([np.repeat(base[:64], 40, 0),  # 2,560 triangles, 64 centroids
+                           base[64:]])
+    tris[100] = [1, 1, 1, 1, 1, 1, 1, 1, 1]          # a point
+    tris[200] = [0, 0, 0, 1, 1, 1, 2, 2, 2]          # a segment
+    flat = tris.copy()
+    flat[:, [2, 5, 8]] = 0.5
+    rays = np.concatenate([W.soup_rays(79, 2000),
+                           np.column_stack([rng.uniform(-1, 2, (500, 2)), np.full(500, -1.0),
+                                            np.zeros((500, 2)), np.ones(500)])]).astype(np.float32)
+    for scene in (tris, flat):
+        small.set_tris(scene)
+        assert small.stat("build_small") == 1.0
+        _same(small.nearest_hits(rays, TAGS), oracle_lib.brute_force(scene, rays))
