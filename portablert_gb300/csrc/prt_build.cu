@@ -1085,11 +1085,13 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 	}
 	if (plan.small) {
 		// One block: PLOC, collapse and re-layout in one launch, which also zeroes the
-		// counters and writes the empty node; the compression reads the node count on the
-		// device, so the host waits once, at the end.
+		// counters, writes the empty node and leaves the counters in the pinned host
+		// buffer; the compression reads the node count on the device, so the host only
+		// waits, once, at the end.
 		uint32_t *ctr = ws.counters.as<uint32_t>();
 		BUILD_TRY(launch_build_small(d_tris, n, (uint32_t)plan.leaf_size, plan.collapse_cost,
-		                             plan.compressed, ws, sc, plan.node_cap, ctr, d_err, st));
+		                             plan.compressed, ws, sc, plan.node_cap, ctr, ws.h_counters,
+		                             d_err, st));
 		sc.built_small = true;
 		if (plan.compressed) {
 			k_compress<<<blocks_for(8ull * plan.node_cap, 256), 256, 0, st>>>(
@@ -1097,7 +1099,7 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 			sc.has_cnodes = true;
 		}
 		BUILD_TRY(cudaGetLastError());
-		return host_checks ? build_finish(sc, ws, st, msg) : PRT_OK;
+		return host_checks ? build_finish(sc, ws, st, msg, true) : PRT_OK;
 	}
 	BUILD_TRY(write_dead_node(plan, sc, st));
 	uint32_t *d_toff = sc.tri_off.as<uint32_t>();
@@ -1179,9 +1181,11 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
 	return PRT_OK;
 }
 
-int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg) {
-	BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ws.counters.p, 4 * kCtrWords, cudaMemcpyDeviceToHost,
-	                          st));
+int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg,
+                 bool on_host) {
+	if (!on_host)
+		BUILD_TRY(cudaMemcpyAsync(ws.h_counters, ws.counters.p, 4 * kCtrWords,
+		                          cudaMemcpyDeviceToHost, st));
 	BUILD_TRY(cudaStreamSynchronize(st));
 	uint32_t depth = 0;
 	while (depth < (uint32_t)kMaxLevels && ws.h_counters[depth])

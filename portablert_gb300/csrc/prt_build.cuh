@@ -139,7 +139,9 @@ int build_enqueue(const float *d_tris, const BuildPlan &plan, SceneGPU &sc, Buil
                   cudaStream_t st, uint32_t *d_err, bool host_checks, std::string &msg);
 
 // Reads the build's counters (synchronises `st`): node count, depth, placement check.
-int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg);
+// on_host: the build wrote them to the pinned host buffer itself (no copy is queued).
+int build_finish(SceneGPU &sc, BuildScratch &ws, cudaStream_t st, std::string &msg,
+                 bool on_host = false);
 
 // Builds the 8-wide trees of the scenes [tri_off[s], tri_off[s+1]) of the triangles at
 // d_tris (n x 9 floats, device memory) into `sc`.  tri_off is host memory with
@@ -157,11 +159,11 @@ int build_scene(const float *d_tris, uint64_t n, int leaf_size, bool compressed,
 
 // The one-block build (prt_build_small.cu): the largest scene it takes, and its launch
 // (PLOC binary tree, collapse, triangle re-layout; the level counters at `ctr` end as
-// the multi-launch build leaves them; it also writes the empty node at sc.dead, in
-// cnodes too when `compressed`).
+// the multi-launch build leaves them, and are copied to the pinned host buffer h_ctr;
+// it also writes the empty node at sc.dead, in cnodes too when `compressed`).
 uint32_t small_build_max();
 cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
                                bool compressed, BuildScratch &ws, SceneGPU &sc, uint32_t node_cap,
-                               uint32_t *ctr, uint32_t *d_err, cudaStream_t st);
+                               uint32_t *ctr, uint32_t *h_ctr, uint32_t *d_err, cudaStream_t st);
 
 } // namespace prt

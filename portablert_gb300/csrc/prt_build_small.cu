@@ -29,7 +29,8 @@
 //      shared-memory permutation;
 //   4. the triangles re-laid out in leaf order (as k_relayout): copied into shared
 //      memory with coalesced loads, then written out in permutation order.
-// The counters end as the multi-launch build leaves them (build_finish reads them).
+// The counters end as the multi-launch build leaves them, and in the host's pinned copy
+// (build_finish reads that after its wait).
 // No thread waits on another except at __syncthreads; every loop is bounded.
 #include <atomic>
 #include <cfloat>
@@ -286,17 +287,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                   float4 *__restrict__ ibox, float4 *__restrict__ lbox, uint32_t *__restrict__ lr,
                   CostNode *__restrict__ cost, Node8 *__restrict__ nodes, uint32_t node_cap,
                   float4 *__restrict__ tri4, uint32_t *__restrict__ inv, uint32_t *__restrict__ ctr,
-                  Node8 *__restrict__ dead, CNode8 *__restrict__ cdead, uint32_t *__restrict__ err) {
+                  uint32_t *__restrict__ hctr, Node8 *__restrict__ dead, CNode8 *__restrict__ cdead,
+                  uint32_t *__restrict__ err) {
 	extern __shared__ __align__(16) unsigned char sm[];
 	uint32_t *scan = reinterpret_cast<uint32_t *>(sm + kOffScan);
 	const uint32_t tid = threadIdx.x;
 	float *box = reinterpret_cast<float *>(sm + kOffBox);
 	uint32_t *word = reinterpret_cast<uint32_t *>(sm + kOffWord);
 	float *crow = reinterpret_cast<float *>(sm + kOffCost);
-	// The counters start at zero; the empty node (NaN boxes, no references; compressed:
-	// no masks, no counts) is written here rather than by separate copies.
-	if (tid < (uint32_t)kCtrWords)
+	// The counters (on the device, and the host's copy in mapped pinned memory) start at
+	// zero; the empty node (NaN boxes, no references; compressed: no masks, no counts) is
+	// written here rather than by separate copies.
+	if (tid < (uint32_t)kCtrWords) {
 		ctr[tid] = 0u;
+		hctr[tid] = 0u;
+	}
 	if (tid < sizeof(Node8) / 4u)
 		reinterpret_cast<uint32_t *>(dead)[tid] = 0xFFFFFFFFu;
 	if (cdead && tid < sizeof(CNode8) / 4u)
@@ -883,6 +888,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 		tri4[3 * (size_t)d + 2] = make_float4(t[6], t[7], t[8], 0.0f);
 		inv[p] = d;
 	}
+	// The counters' host copy, which the host reads after its wait without a copy of its
+	// own (thread 0 wrote the device counters before the barriers above).
+	if (tid < (uint32_t)kCtrWords)
+		hctr[tid] = __ldcg(&ctr[tid]);
 }
 
 } // namespace
@@ -891,11 +900,16 @@ uint32_t small_build_max() { return kSmallMax; }
 
 cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_size, bool use_cost,
                                bool compressed, BuildScratch &ws, SceneGPU &sc, uint32_t node_cap,
-                               uint32_t *ctr, uint32_t *d_err, cudaStream_t st) {
+                               uint32_t *ctr, uint32_t *h_ctr, uint32_t *d_err, cudaStream_t st) {
 	// The shared-memory limit is a per-device attribute: set once per device.
 	static std::atomic<uint32_t> attr_set{0};
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess)
+		return e;
+	// The host's pinned counters, as the device addresses them.
+	uint32_t *h_dev = nullptr;
+	e = cudaHostGetDevicePointer(reinterpret_cast<void **>(&h_dev), h_ctr, 0);
 	if (e != cudaSuccess)
 		return e;
 	const uint32_t bit = (dev >= 0 && dev < 32) ? (1u << dev) : 0u;
@@ -909,7 +923,7 @@ cudaError_t launch_build_small(const float *d_tris, uint32_t n, uint32_t leaf_si
 	k_build_small<<<1, kThreads, kSmemBytes, st>>>(
 	    d_tris, n, leaf_size, use_cost ? 1 : 0, ws.ibox.as<float4>(), ws.lbox.as<float4>(),
 	    ws.left.as<uint32_t>(), use_cost ? ws.cost.as<CostNode>() : nullptr,
-	    sc.nodes.as<Node8>(), node_cap, sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr,
+	    sc.nodes.as<Node8>(), node_cap, sc.tri4.as<float4>(), sc.inv.as<uint32_t>(), ctr, h_dev,
 	    sc.nodes.as<Node8>() + sc.dead, compressed ? sc.cnodes.as<CNode8>() + sc.dead : nullptr,
 	    d_err);
 	return cudaGetLastError();
