@@ -62,6 +62,7 @@ void BuildScratch::release() {
 	if (h_counters)
 		cudaFreeHost(h_counters);
 	h_counters = nullptr;
+	h_sah = nullptr;
 }
 
 namespace {
@@ -990,7 +991,8 @@ int build_plan(const uint64_t *tri_off64, uint32_t S, int leaf_size, bool compre
 	// Work items hold 27-bit node indices; a tree's nodes stay below n - 1 < 2^27 - 1.
 	sc.dead = std::min<uint32_t>(plan.node_cap, kIndexMask);
 	if (!ws.h_counters)
-		BUILD_TRY(cudaMallocHost(&ws.h_counters, 4 * kCtrWords));
+		BUILD_TRY(cudaMallocHost(&ws.h_counters, 4 * (kCtrWords + kHostSahWords)));
+	ws.h_sah = ws.h_counters + kCtrWords;
 	if (plan.small)
 		return PRT_OK; // the one-block build reads no offset table
 	BUILD_TRY(cudaMemcpyAsync(sc.tri_off.p, plan.toff.data(), 4ull * (S + 1),

@@ -83,6 +83,10 @@ struct SceneGPU {
 	}
 };
 
+// Pinned words after the collapse's counter mirror: the SAH tiers' counters and error
+// word as the host reads them between levels (a copy into pageable memory is staged).
+constexpr int kHostSahWords = 16;
+
 // Scratch reused across builds (grow-only).
 struct BuildScratch {
 	DevBuf keys, vals, keys2, vals2;  // Morton keys (u32 or u64) and triangle indices
@@ -102,6 +106,7 @@ struct BuildScratch {
 	DevBuf roots;                     // SAH build: root binary node of each scene
 	DevBuf cost;                      // cost-optimal collapse: 36 B per binary node
 	uint32_t *h_counters = nullptr;   // pinned mirror of `counters`
+	uint32_t *h_sah = nullptr;        // pinned, kHostSahWords (in the same allocation)
 	void release();
 };
 

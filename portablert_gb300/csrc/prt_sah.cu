@@ -56,6 +56,7 @@ enum : int {
 	kCtrChunks = 6,
 	kCtrWordsSah = 8
 };
+static_assert(kCtrWordsSah + 1 <= kHostSahWords, "the SAH counters' pinned words");
 
 struct alignas(16) SahTask {
 	uint32_t begin, count, node, parent; // parent = (node << 1 | side), kNone at a root
@@ -1184,8 +1185,8 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 			}
 			k_sah_mid<<<g_mid, 128, 0, st>>>(A, par);
 		}
-		uint32_t h[kCtrWordsSah];
-		cudaError_t e = cudaMemcpyAsync(h, A.ctr, sizeof(h), cudaMemcpyDeviceToHost, st);
+		uint32_t *h = ws.h_sah;
+		cudaError_t e = cudaMemcpyAsync(h, A.ctr, 4 * kCtrWordsSah, cudaMemcpyDeviceToHost, st);
 		if (e == cudaSuccess)
 			e = cudaStreamSynchronize(st);
 		if (e != cudaSuccess) {
@@ -1211,12 +1212,13 @@ int sah_build_enqueue(const float *d_tris, const BuildPlan &plan, BuildScratch &
 		const uint32_t ns = plan.toff[s + 1] - plan.toff[s];
 		want += ns >= 2 ? ns - 2 : 0;
 	}
-	uint32_t h[kCtrWordsSah], h_err = 0;
-	cudaError_t e = cudaMemcpyAsync(h, A.ctr, sizeof(h), cudaMemcpyDeviceToHost, st);
+	uint32_t *h = ws.h_sah, *h_errw = h + kCtrWordsSah;
+	cudaError_t e = cudaMemcpyAsync(h, A.ctr, 4 * kCtrWordsSah, cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess)
-		e = cudaMemcpyAsync(&h_err, d_err, 4, cudaMemcpyDeviceToHost, st);
+		e = cudaMemcpyAsync(h_errw, d_err, 4, cudaMemcpyDeviceToHost, st);
 	if (e == cudaSuccess)
 		e = cudaStreamSynchronize(st);
+	const uint32_t h_err = *h_errw;
 	if (e != cudaSuccess) {
 		msg = std::string("sah build: ") + cudaGetErrorString(e);
 		return PRT_ERR_CUDA;
